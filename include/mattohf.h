@@ -1,0 +1,145 @@
+/* C ABI of the GB300-native mATTOHF hot path.
+ *
+ * The reference (Fortran 90, Yasushi-Shinohara/mATTOHF) has no plugin API: its
+ * hot path is a set of module procedures in src/Functions.f90 and external
+ * subroutines in src/RT_calculation.f90 / src/GS_calculation.f90, operating on
+ * global module state (src/Global_variables.f90).  Each entry point below
+ * names the reference routine it replaces.  All functions are iso_c_binding
+ * compatible: scalars by value, arrays as plain pointers, `int` status return.
+ *
+ * Array conventions
+ *   orbitals   complex128 interleaved (re, im), Fortran layout ubk(1:NG,1:NB,1:NK),
+ *              i.e. C [NK][NB][NG][2] doubles; blocks of `nbw` bands use
+ *              [NK][nbw][NG][2].
+ *   real grids double[NG]; per-band reals double[NK][NB] (= Fortran (NB,NK)).
+ *   Host pointers are caller-owned; the library copies in and out.  Functions
+ *   with the `_device` suffix take device pointers and run asynchronously on the
+ *   context's stream.
+ *
+ * Threading: one context per host thread; every call on a context is ordered
+ * on that context's CUDA stream.  The library never aborts or exits.
+ */
+#ifndef MATTOHF_H
+#define MATTOHF_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MATTOHF_OK 0
+#define MATTOHF_ERR_ARG 1        /* invalid argument or configuration */
+#define MATTOHF_ERR_CUDA 2       /* a CUDA runtime call failed */
+#define MATTOHF_ERR_NONFINITE 3  /* non-finite state detected (e.g. unstable dt) */
+#define MATTOHF_ERR_TIMEOUT 4    /* a bounded device wait gave up */
+#define MATTOHF_ERR_NOTCONV 5    /* eigensolver / orthonormalisation did not converge */
+#define MATTOHF_ERR_ALLOC 6      /* device allocation failed */
+#define MATTOHF_ERR_STATE 7      /* call not valid in the context's current state */
+
+/* options for mattohf_set_option */
+#define MATTOHF_OPT_GRAPH 1        /* 1: replay RK4 steps from a captured CUDA graph (default 1) */
+#define MATTOHF_OPT_FOCK_CHUNKS 2  /* pair chunks per Fock output column; 0 = automatic */
+#define MATTOHF_OPT_KERNEL_TIMING 3 /* 1: bracket every Fock launch with CUDA events (no graph) */
+#define MATTOHF_OPT_SYMMETRIC 4    /* 1: use the occupied-pair Hermitian symmetry when w == u (default 1) */
+
+typedef struct mattohf_ctx mattohf_ctx;
+
+/* Run configuration: the subset of src/Global_variables.f90 the hot path
+ * reads (NG, NK, NB, NBocc, acell, functional) plus the atoms block of
+ * src/mATTOHF.f90:229-240 (species charges/softening, ion positions in reduced
+ * coordinates, 1-based species index). */
+typedef struct mattohf_config {
+  int NG;              /* grid points per cell: power of two, 16..512 */
+  int NK;              /* k-points */
+  int NB;              /* bands */
+  int NBocc;           /* occupied bands, 1..NB */
+  double acell;        /* lattice constant [bohr] */
+  int functional_hf;   /* 1: 'HF' (Fock exchange on), 0: Hartree only */
+  int device;          /* CUDA device ordinal */
+  int nspecies;
+  const double* Zeff;  /* [nspecies] */
+  const double* alpha; /* [nspecies] */
+  int nion;
+  const double* Rion;  /* [nion] reduced positions */
+  const int* Kion;     /* [nion] 1-based species index */
+} mattohf_config;
+
+/* Initialization (src/Initialization.f90:2-276) + Prep_periodic_ion_potential
+ * (src/Prep_periodic_ion_potential.f90:2-31): grids, soft-Coulomb tables
+ * k_vCk (src/Functions.f90:33-52), occupations, ion potential. */
+int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out);
+int mattohf_destroy(mattohf_ctx* ctx);
+const char* mattohf_last_error(const mattohf_ctx* ctx);
+const char* mattohf_status_string(int status);
+int mattohf_set_option(mattohf_ctx* ctx, int option, long long value);
+
+/* Grids of src/Initialization.f90:93-112 and cell factors (I:46-49, I:62):
+ * rx[NG], Gx[NG], kx[NK], cell[3] = {vcell, dvcell, bx}.  Any pointer may be NULL. */
+int mattohf_get_grids(mattohf_ctx* ctx, double* rx, double* Gx, double* kx, double* cell);
+/* Coulomb tables: vCG[NG] (I:143-146) and vCq[(2NK-1)][NG] = k_vCk(Gx+kx(kr)-kx(kc))
+ * indexed by kr-kc+NK-1 (the distinct columns of vCGkk, I:130-137). */
+int mattohf_get_coulomb(mattohf_ctx* ctx, double* vCG, double* vCq);
+/* Ion potential vion[NG]; set replaces it. */
+int mattohf_get_vion(mattohf_ctx* ctx, double* vion);
+int mattohf_set_vion(mattohf_ctx* ctx, const double* vion);
+
+/* Device-resident orbitals ubk (the state of RT_calculation / GS_calculation). */
+int mattohf_set_orbitals(mattohf_ctx* ctx, const double* ubk);
+int mattohf_get_orbitals(mattohf_ctx* ctx, double* ubk);
+/* Init_wf + quickrnd (src/mATTOHF.f90:159-196): the reference's Gaussian guess. */
+int mattohf_init_wf(mattohf_ctx* ctx);
+/* Gram_Schmidt (src/mATTOHF.f90:134-157) on the device orbitals. */
+int mattohf_gram_schmidt(mattohf_ctx* ctx);
+
+/* ubkwbk_hwbk (src/Functions.f90:187-209): hwbk = h[ubk](A) wbk.
+ * ubk [NK][NB][NG], wbk/hwbk [NK][nbw][NG] complex128, host memory. */
+int mattohf_hpsi(mattohf_ctx* ctx, const double* ubk, const double* wbk, int nbw, double A,
+                 double* hwbk);
+/* Same on device pointers, asynchronous on the context stream. */
+int mattohf_hpsi_device(mattohf_ctx* ctx, const double* d_ubk, const double* d_wbk, int nbw,
+                        double A, double* d_hwbk);
+/* ubkwbk_vFwbk (src/Functions.f90:237-261): the Fock term alone. */
+int mattohf_fock(mattohf_ctx* ctx, const double* ubk, const double* wbk, int nbw, double* vFwbk);
+/* ubk_tubk (src/Functions.f90:212-234): the kinetic term alone. */
+int mattohf_kinetic(mattohf_ctx* ctx, const double* wbk, int nbw, double A, double* tbk);
+/* ubk_dns (F:55-71) and dns_vH (F:147-162). */
+int mattohf_density(mattohf_ctx* ctx, const double* ubk, double* dns, double* vH);
+
+/* ubk_Ecomps / ubk_Etot (F:74-91, F:265-286), ubk_Je (F:289-318) and
+ * Nele = sum(dns)*dvcell (RT:43-45) of the device orbitals at field A.
+ * Ecomps = {Ekin, Eion, EH, Exc}.  Any output pointer may be NULL. */
+int mattohf_observables(mattohf_ctx* ctx, double A, double* Ecomps, double* Etot, double* Je,
+                        double* Nele);
+
+/* RT_RK4_ubk (src/RT_calculation.f90:154-173): one RK4 step of the device
+ * orbitals with stage fields 2*Aave-A, Aave, Aave, A. */
+int mattohf_rk4_step(mattohf_ctx* ctx, double Aave, double A, double dt);
+/* The RT_calculation loop body (RT:38-60) for nt steps: RK4 then Nele, Etot,
+ * Jtot at A[it].  A, Aave: [nt] host arrays (Define_Afield, RT:175-244);
+ * Etot, Je, Nele: [nt] host outputs (may be NULL).  Returns
+ * MATTOHF_ERR_NONFINITE (with the first bad step in mattohf_last_error) if the
+ * state overflows. */
+int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const double* Aave,
+                    double* Etot, double* Je, double* Nele);
+/* Device time of the last mattohf_rk4_run in milliseconds, and (with
+ * MATTOHF_OPT_KERNEL_TIMING) the summed device time and launch count of the
+ * Fock pair kernel inside it. */
+int mattohf_last_run_timing(mattohf_ctx* ctx, double* run_ms, double* fock_ms, int* fock_launches);
+
+/* GS_calculation (src/GS_calculation.f90:2-121) SCF loop: per iteration
+ * Gram_Schmidt, KS_ubk2_SVD (Krylov block of NB*ncg columns, GS:124-194),
+ * Gram_Schmidt, Subspace_diag (GS:197-237), Etot, Je, epsbk, epserrorbk.
+ * Etot_iter [nscf+1] (Etotscf(0:Nscf)), Je_iter [nscf], dnsdiff [nscf]
+ * (sum|dnsscf(iter+1)-dnsscf(iter)|/NG), epsbk / epserrorbk [NK][NB] of the
+ * last iteration.  Any output may be NULL. */
+int mattohf_gs_run(mattohf_ctx* ctx, int nscf, int ncg, double* Etot_iter, double* Je_iter,
+                   double* dnsdiff, double* epsbk, double* epserrorbk);
+/* ubk_epsbk / ubk_epserrorbk (F:321-358) of the device orbitals, [NK][NB]. */
+int mattohf_eps(mattohf_ctx* ctx, double* epsbk, double* epserrorbk);
+
+int mattohf_synchronize(mattohf_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MATTOHF_H */

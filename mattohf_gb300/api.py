@@ -1,0 +1,227 @@
+"""Host-side mirror of the reference's hot-path interface over the C ABI.
+
+Names follow the reference's Fortran procedures (src/Functions.f90,
+src/RT_calculation.f90, src/GS_calculation.f90); arrays are numpy complex128
+with shape (NK, NB, NG) — the bytes of Fortran ``ubk(1:NG,1:NB,1:NK)``.
+Every call goes through ``libmattohf.so``; errors raise ``MattohfError``
+carrying the library's status code and message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import _capi
+from .inputs import RunConfig
+
+_D = C.POINTER(C.c_double)
+
+
+class MattohfError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"mattohf status {status}: {msg}")
+        self.status = status
+
+
+def _dp(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_D)
+
+
+def _c128(a, shape) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    if a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+    return a
+
+
+class Context:
+    """One device-resident run (``mattohf_ctx``)."""
+
+    def __init__(self, cfg: RunConfig, device: int = 0):
+        self.lib = _capi.load()
+        self.cfg = cfg
+        self.NG, self.NK, self.NB, self.NBocc = cfg.NG, cfg.NK, cfg.NB, cfg.NBocc
+        z = np.ascontiguousarray(cfg.Zeff, dtype=np.float64)
+        al = np.ascontiguousarray(cfg.alpha, dtype=np.float64)
+        R = np.ascontiguousarray(cfg.Rion, dtype=np.float64)
+        K = np.ascontiguousarray(cfg.Kion, dtype=np.int32)
+        self._keep = (z, al, R, K)
+        c = _capi.mattohf_config()
+        c.NG, c.NK, c.NB, c.NBocc = cfg.NG, cfg.NK, cfg.NB, cfg.NBocc
+        c.acell = cfg.acell
+        c.functional_hf = 1 if cfg.functional.strip() == "HF" else 0
+        c.device = device
+        c.nspecies = z.size
+        c.Zeff = _dp(z)
+        c.alpha = _dp(al)
+        c.nion = R.size
+        c.Rion = _dp(R)
+        c.Kion = K.ctypes.data_as(C.POINTER(C.c_int))
+        h = C.c_void_p()
+        st = self.lib.mattohf_create(C.byref(c), C.byref(h))
+        if st != _capi.OK:
+            raise MattohfError(st, self.lib.mattohf_status_string(st).decode())
+        self.h = h
+
+    # -- plumbing -----------------------------------------------------------
+    def _check(self, st: int):
+        if st != _capi.OK:
+            raise MattohfError(st, self.lib.mattohf_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mattohf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_option(self, opt: int, value: int):
+        self._check(self.lib.mattohf_set_option(self.h, opt, int(value)))
+
+    @property
+    def shape(self):
+        return (self.NK, self.NB, self.NG)
+
+    # -- tables -------------------------------------------------------------
+    def grids(self) -> Dict[str, np.ndarray]:
+        rx, Gx, kx, cell = np.empty(self.NG), np.empty(self.NG), np.empty(self.NK), np.empty(3)
+        self._check(self.lib.mattohf_get_grids(self.h, _dp(rx), _dp(Gx), _dp(kx), _dp(cell)))
+        return {"rx": rx, "Gx": Gx, "kx": kx, "vcell": cell[0], "dvcell": cell[1], "bx": cell[2]}
+
+    def coulomb(self):
+        vCG = np.empty(self.NG)
+        vCq = np.empty((2 * self.NK - 1, self.NG))
+        self._check(self.lib.mattohf_get_coulomb(self.h, _dp(vCG), _dp(vCq)))
+        return vCG, vCq
+
+    @property
+    def vion(self) -> np.ndarray:
+        v = np.empty(self.NG)
+        self._check(self.lib.mattohf_get_vion(self.h, _dp(v)))
+        return v
+
+    @vion.setter
+    def vion(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        self._check(self.lib.mattohf_set_vion(self.h, _dp(v)))
+
+    # -- state --------------------------------------------------------------
+    def set_orbitals(self, ubk):
+        u = _c128(ubk, self.shape)
+        self._check(self.lib.mattohf_set_orbitals(self.h, _dp(u.view(np.float64))))
+
+    def get_orbitals(self) -> np.ndarray:
+        u = np.empty(self.shape, dtype=np.complex128)
+        self._check(self.lib.mattohf_get_orbitals(self.h, _dp(u.view(np.float64))))
+        return u
+
+    ubk = property(get_orbitals, set_orbitals)
+
+    def Init_wf(self):
+        self._check(self.lib.mattohf_init_wf(self.h))
+
+    def Gram_Schmidt(self):
+        self._check(self.lib.mattohf_gram_schmidt(self.h))
+
+    # -- operator kernels (src/Functions.f90) -----------------------------------
+    def ubkwbk_hwbk(self, ubk, wbk, A: float) -> np.ndarray:
+        u = _c128(ubk, self.shape)
+        w = np.ascontiguousarray(wbk, dtype=np.complex128)
+        nbw = w.shape[1]
+        _c128(w, (self.NK, nbw, self.NG))
+        out = np.empty_like(w)
+        self._check(self.lib.mattohf_hpsi(self.h, _dp(u.view(np.float64)), _dp(w.view(np.float64)),
+                                          nbw, float(A), _dp(out.view(np.float64))))
+        return out
+
+    def ubkwbk_vFwbk(self, ubk, wbk) -> np.ndarray:
+        u = _c128(ubk, self.shape)
+        w = np.ascontiguousarray(wbk, dtype=np.complex128)
+        nbw = w.shape[1]
+        out = np.empty_like(w)
+        self._check(self.lib.mattohf_fock(self.h, _dp(u.view(np.float64)), _dp(w.view(np.float64)),
+                                          nbw, _dp(out.view(np.float64))))
+        return out
+
+    def ubk_tubk(self, wbk, A: float) -> np.ndarray:
+        w = np.ascontiguousarray(wbk, dtype=np.complex128)
+        out = np.empty_like(w)
+        self._check(self.lib.mattohf_kinetic(self.h, _dp(w.view(np.float64)), w.shape[1], float(A),
+                                             _dp(out.view(np.float64))))
+        return out
+
+    def ubk_dns(self, ubk) -> np.ndarray:
+        u = _c128(ubk, self.shape)
+        d = np.empty(self.NG)
+        self._check(self.lib.mattohf_density(self.h, _dp(u.view(np.float64)), _dp(d), None))
+        return d
+
+    def dns_vH_of(self, ubk) -> np.ndarray:
+        """Hartree potential of the density of ``ubk`` (dns_vH(ubk_dns(ubk)))."""
+        u = _c128(ubk, self.shape)
+        vH = np.empty(self.NG)
+        self._check(self.lib.mattohf_density(self.h, _dp(u.view(np.float64)), None, _dp(vH)))
+        return vH
+
+    def observables(self, A: float = 0.0) -> Dict[str, float]:
+        """Ecomps/Etot (F:74-91, F:265-286), Je (F:289-318), Nele of the device orbitals."""
+        ec = np.empty(4)
+        et, je, ne = C.c_double(), C.c_double(), C.c_double()
+        self._check(self.lib.mattohf_observables(self.h, float(A), _dp(ec), C.byref(et), C.byref(je),
+                                                 C.byref(ne)))
+        return {"Etot": et.value, "Ekin": ec[0], "Eion": ec[1], "EH": ec[2], "Exc": ec[3],
+                "Je": je.value, "Nele": ne.value}
+
+    def ubk_epsbk(self):
+        eps = np.empty((self.NK, self.NB))
+        err = np.empty((self.NK, self.NB))
+        self._check(self.lib.mattohf_eps(self.h, _dp(eps), _dp(err)))
+        return eps, err
+
+    # -- propagation (src/RT_calculation.f90) ------------------------------------
+    def RT_RK4_ubk(self, Aave: float, A: float, dt: float):
+        self._check(self.lib.mattohf_rk4_step(self.h, float(Aave), float(A), float(dt)))
+
+    def rk4_run(self, A, Aave, dt: float):
+        """nt RK4 steps with per-step (Etot, Je, Nele) at A[it] (RT:38-60)."""
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        Aave = np.ascontiguousarray(Aave, dtype=np.float64)
+        nt = A.size
+        E, J, N = np.empty(nt), np.empty(nt), np.empty(nt)
+        st = self.lib.mattohf_rk4_run(self.h, nt, float(dt), _dp(A), _dp(Aave), _dp(E), _dp(J), _dp(N))
+        self._check(st)
+        return E, J, N
+
+    def last_run_timing(self):
+        r, f = C.c_double(), C.c_double()
+        n = C.c_int()
+        self._check(self.lib.mattohf_last_run_timing(self.h, C.byref(r), C.byref(f), C.byref(n)))
+        return r.value, f.value, n.value
+
+    # -- ground state (src/GS_calculation.f90) -----------------------------------
+    def GS_calculation(self, nscf: int, ncg: int) -> Dict[str, np.ndarray]:
+        Et = np.empty(nscf + 1)
+        Je = np.empty(max(nscf, 1))
+        dd = np.empty(max(nscf, 1))
+        eps = np.empty((self.NK, self.NB))
+        err = np.empty((self.NK, self.NB))
+        self._check(self.lib.mattohf_gs_run(self.h, int(nscf), int(ncg), _dp(Et), _dp(Je), _dp(dd),
+                                             _dp(eps), _dp(err)))
+        return {"Etot": Et, "Je": Je[:nscf], "dnsdiff": dd[:nscf], "epsbk": eps, "epserrorbk": err}
+
+    def synchronize(self):
+        self._check(self.lib.mattohf_synchronize(self.h))

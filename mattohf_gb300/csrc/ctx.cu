@@ -1,0 +1,948 @@
+// Host runtime and C ABI (include/mattohf.h).
+//
+// Owns the device-resident state of one run (orbitals, tables, potentials,
+// Krylov blocks, Fock partial-sum scratch) and sequences the kernels of
+// k_hpsi.cu / k_gs.cu / k_table.cu on one CUDA stream.  The RK4 step is
+// captured once into a CUDA graph and replayed; the step index lives on the
+// device so one graph serves every step.
+#include "internal.h"
+#include "../../include/mattohf.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+using namespace mattohf;
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+
+__global__ void k_twiddles(double2* tw, int n) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < n) {
+    double s, c;
+    sincospi(-2.0 * (double)m / (double)n, &s, &c);
+    tw[m] = make_double2(c, s);
+  }
+}
+
+__global__ void k_zero_int(int* p, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0;
+}
+
+}  // namespace
+
+struct mattohf_ctx {
+  int NG = 0, NK = 0, NB = 0, NBocc = 0, hf = 1, device = 0;
+  double acell = 0, vcell = 0, dvcell = 0, bx = 0, occ = 0;
+  std::vector<double> rx, Gx, kx, vion;
+  std::vector<double> Zeff, alpha, Rion;
+  std::vector<int> Kion;
+  cudaStream_t st = nullptr;
+  // tables
+  double2* tw = nullptr;
+  double *d_Gx = nullptr, *d_kx = nullptr, *d_vCG = nullptr, *d_vcq = nullptr, *d_kern = nullptr;
+  double *d_vion = nullptr, *d_vloc = nullptr, *d_rho = nullptr, *d_scal = nullptr, *d_out = nullptr;
+  // state
+  double2 *d_u = nullptr, *d_us = nullptr, *d_k[4] = {nullptr, nullptr, nullptr, nullptr};
+  // staging for host-array entry points
+  double2 *d_a = nullptr, *d_b = nullptr, *d_c = nullptr;
+  size_t stage_cap = 0;
+  // Fock partial sums
+  double2* d_scratch = nullptr;
+  size_t scratch_cap = 0;
+  double* d_colbuf = nullptr;
+  size_t colbuf_cap = 0;
+  int* d_int = nullptr;  // [0] = step counter, [1] = non-finite flag, [2] = solver flag
+  // RT series
+  double *d_A = nullptr, *d_Aave = nullptr, *d_sE = nullptr, *d_sJ = nullptr, *d_sN = nullptr;
+  int series_cap = 0;
+  // GS work
+  double2 *d_work = nullptr, *d_hwork = nullptr, *d_M = nullptr, *d_V = nullptr;
+  double* d_evals = nullptr;
+  size_t gs_cap = 0;
+  double *d_eps = nullptr, *d_err = nullptr;
+  // options
+  int opt_graph = 1, opt_chunks = 0, opt_timing = 0, opt_sym = 1;
+  // graph of one RK4 step
+  cudaGraphExec_t step_exec = nullptr;
+  double step_dt = 0;
+  // timing
+  double last_run_ms = 0, last_fock_ms = 0;
+  int last_fock_launches = 0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> fock_events;
+  size_t fock_event_used = 0;
+  bool capturing = false;
+  std::string err;
+};
+
+namespace {
+
+void destroy_graph(mattohf_ctx* c);
+
+int fail(mattohf_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail(ctx, MATTOHF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define CKR(expr)              \
+  do {                         \
+    int r_ = (expr);           \
+    if (r_ != MATTOHF_OK) return r_; \
+  } while (0)
+
+template <typename T>
+int dalloc(mattohf_ctx* ctx, T** p, size_t n) {
+  if (*p) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  if (n == 0) return MATTOHF_OK;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return fail(ctx, MATTOHF_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  return MATTOHF_OK;
+}
+
+size_t orb_elems(const mattohf_ctx* c, int nb) { return (size_t)c->NK * nb * c->NG; }
+
+int ensure_stage(mattohf_ctx* ctx, size_t elems) {
+  if (elems <= ctx->stage_cap) return MATTOHF_OK;
+  CKR(dalloc(ctx, &ctx->d_a, elems));
+  CKR(dalloc(ctx, &ctx->d_b, elems));
+  CKR(dalloc(ctx, &ctx->d_c, elems));
+  ctx->stage_cap = elems;
+  return MATTOHF_OK;
+}
+
+// Pair chunking of the Fock kernel: enough items to fill 152 SMs several
+// times over, each chunk a whole number of team rounds.
+void fock_split(const mattohf_ctx* c, int ncols, int* nchunks, int* chunk) {
+  const int npairs = c->NK * c->NBocc;
+  int nch = c->opt_chunks;
+  if (nch <= 0) {
+    const int target = 152 * 8;
+    nch = (target + ncols - 1) / ncols;
+  }
+  nch = std::max(1, std::min(nch, npairs));
+  int ch = (npairs + nch - 1) / nch;
+  nch = (npairs + ch - 1) / ch;
+  *nchunks = nch;
+  *chunk = ch;
+}
+
+int ensure_scratch(mattohf_ctx* ctx, int ncols) {
+  int nch, ch;
+  fock_split(ctx, ncols, &nch, &ch);
+  const size_t need = (size_t)ncols * nch * ctx->NG;
+  if (need > ctx->scratch_cap) {
+    if (ctx->capturing) return fail(ctx, MATTOHF_ERR_STATE, "scratch growth during capture");
+    destroy_graph(ctx);  // the captured step holds the old pointer
+    CKR(dalloc(ctx, &ctx->d_scratch, need));
+    ctx->scratch_cap = need;
+  }
+  const size_t cb = (size_t)ncols * 4;
+  if (cb > ctx->colbuf_cap) {
+    if (ctx->capturing) return fail(ctx, MATTOHF_ERR_STATE, "colbuf growth during capture");
+    destroy_graph(ctx);
+    CKR(dalloc(ctx, &ctx->d_colbuf, cb));
+    ctx->colbuf_cap = cb;
+  }
+  return MATTOHF_OK;
+}
+
+AField aval(double A) {
+  AField f;
+  f.mode = AVAL;
+  f.val = A;
+  f.A = nullptr;
+  f.Aave = nullptr;
+  f.it = nullptr;
+  return f;
+}
+
+int enq_density(mattohf_ctx* ctx, Block u) {
+  DensArgs a;
+  a.u = u;
+  a.nbocc = ctx->NBocc;
+  a.occ = ctx->occ;
+  a.vCG = ctx->d_vCG;
+  a.vion = ctx->d_vion;
+  a.tw = ctx->tw;
+  a.dvcell = ctx->dvcell;
+  a.rho = ctx->d_rho;
+  a.vloc = ctx->d_vloc;
+  a.scal = ctx->d_scal;
+  a.nk = ctx->NK;
+  CK(launch_density(ctx->NG, a, ctx->st));
+  return MATTOHF_OK;
+}
+
+int enq_fock(mattohf_ctx* ctx, Block u, Block w, int* nchunks_out) {
+  const int ncols = ctx->NK * w.nb;
+  CKR(ensure_scratch(ctx, ncols));
+  FockArgs a;
+  a.u = u;
+  a.w = w;
+  a.nk = ctx->NK;
+  a.nbocc = ctx->NBocc;
+  a.kern = ctx->d_kern;
+  a.tw = ctx->tw;
+  a.scratch = ctx->d_scratch;
+  fock_split(ctx, ncols, &a.nchunks, &a.chunk);
+  *nchunks_out = a.nchunks;
+  const bool timed = ctx->opt_timing && !ctx->capturing;
+  if (timed) {
+    if (ctx->fock_event_used == ctx->fock_events.size()) {
+      cudaEvent_t e0, e1;
+      CK(cudaEventCreate(&e0));
+      CK(cudaEventCreate(&e1));
+      ctx->fock_events.push_back({e0, e1});
+    }
+    CK(cudaEventRecord(ctx->fock_events[ctx->fock_event_used].first, ctx->st));
+  }
+  CK(launch_fock(ctx->NG, a, ncols, ctx->st));
+  if (timed) {
+    CK(cudaEventRecord(ctx->fock_events[ctx->fock_event_used].second, ctx->st));
+    ctx->fock_event_used++;
+  }
+  return MATTOHF_OK;
+}
+
+CombineArgs combine_base(mattohf_ctx* ctx, Block w, AField af, int mode, int nchunks) {
+  CombineArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.w = w;
+  a.scratch = (ctx->hf && mode != CM_T) ? ctx->d_scratch : nullptr;
+  a.nchunks = nchunks;
+  a.vloc = ctx->d_vloc;
+  a.Gx = ctx->d_Gx;
+  a.kx = ctx->d_kx;
+  a.tw = ctx->tw;
+  a.af = af;
+  a.mode = mode;
+  a.nk = ctx->NK;
+  a.nbocc = ctx->NBocc;
+  a.occ = ctx->occ;
+  a.colbuf = ctx->d_colbuf;
+  a.nonfinite = ctx->d_int + 1;
+  a.u0 = ctx->d_u;
+  for (int s = 0; s < 4; ++s) a.kbuf[s] = ctx->d_k[s];
+  return a;
+}
+
+// h[u] w -> out  (mode CM_H), or the exchange / kinetic term alone.
+int enq_hpsi(mattohf_ctx* ctx, Block u, Block w, BlockOut out, AField af, int mode) {
+  int nch = 1;
+  if (mode == CM_H) CKR(enq_density(ctx, u));
+  if (ctx->hf && mode != CM_T) CKR(enq_fock(ctx, u, w, &nch));
+  else if (mode == CM_F) {
+    CK(cudaMemsetAsync(out.p, 0, sizeof(double2) * (size_t)ctx->NK * out.kstride, ctx->st));
+    return MATTOHF_OK;
+  }
+  CombineArgs a = combine_base(ctx, w, af, mode, nch);
+  a.out = out;
+  CK(launch_combine(ctx->NG, a, ctx->NK * w.nb, ctx->st));
+  return MATTOHF_OK;
+}
+
+Block blk(const double2* p, int ld, int NG, int nb) {
+  Block b;
+  b.p = p;
+  b.kstride = ld * NG;
+  b.nb = nb;
+  return b;
+}
+BlockOut blko(double2* p, int ld, int NG, int nb) {
+  BlockOut b;
+  b.p = p;
+  b.kstride = ld * NG;
+  b.nb = nb;
+  return b;
+}
+
+// Observables of `u` at field af (RT:43-47): density scalars, Fock partials,
+// per-column Ekin/Je/<u|F u>, then the ordered reduction.
+int enq_observables(mattohf_ctx* ctx, const double2* u, AField af, bool advance) {
+  const int NG = ctx->NG, NB = ctx->NB;
+  Block ub = blk(u, NB, NG, NB);
+  CKR(enq_density(ctx, ub));
+  int nch = 1;
+  if (ctx->hf) CKR(enq_fock(ctx, ub, ub, &nch));
+  else CKR(ensure_scratch(ctx, ctx->NK * NB));
+  CombineArgs a = combine_base(ctx, ub, af, CM_OBS, nch);
+  CK(launch_combine(NG, a, ctx->NK * NB, ctx->st));
+  ObsReduceArgs r;
+  r.colbuf = ctx->d_colbuf;
+  r.scal = ctx->d_scal;
+  r.nk = ctx->NK;
+  r.nb = NB;
+  r.nbocc = ctx->NBocc;
+  r.occ = ctx->occ;
+  r.dvcell = ctx->dvcell;
+  r.vcell = ctx->vcell;
+  r.NGd = (double)NG;
+  r.hf = ctx->hf;
+  r.out = ctx->d_out;
+  r.series_E = advance ? ctx->d_sE : nullptr;
+  r.series_J = advance ? ctx->d_sJ : nullptr;
+  r.series_N = advance ? ctx->d_sN : nullptr;
+  r.it = ctx->d_int;
+  r.advance = advance ? 1 : 0;
+  r.nonfinite = ctx->d_int + 1;
+  CK(launch_obs_reduce(r, ctx->st));
+  return MATTOHF_OK;
+}
+
+// One RK4 step (RT:165-170); fields either from host values or from the
+// device series indexed by the device step counter.
+int enq_rk4(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt) {
+  const int NG = ctx->NG, NB = ctx->NB;
+  const int modes[4] = {CM_RK0, CM_RK1, CM_RK2, CM_RK3};
+  const AField fs[4] = {f_m, f_ave, f_ave, f_cur};
+  for (int s = 0; s < 4; ++s) {
+    const double2* in = (s == 0) ? ctx->d_u : ctx->d_us;
+    Block ub = blk(in, NB, NG, NB);
+    CKR(enq_density(ctx, ub));
+    int nch = 1;
+    if (ctx->hf) CKR(enq_fock(ctx, ub, ub, &nch));
+    CombineArgs a = combine_base(ctx, ub, fs[s], modes[s], nch);
+    a.out = blko(ctx->d_us, NB, NG, NB);
+    a.dt = dt;
+    CK(launch_combine(NG, a, ctx->NK * NB, ctx->st));
+  }
+  return MATTOHF_OK;
+}
+
+int check_ctx(mattohf_ctx* ctx) {
+  if (!ctx) return MATTOHF_ERR_ARG;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return fail(ctx, MATTOHF_ERR_CUDA, cudaGetErrorString(e));
+  return MATTOHF_OK;
+}
+
+int sync_and_flag(mattohf_ctx* ctx) {
+  CK(cudaStreamSynchronize(ctx->st));
+  return MATTOHF_OK;
+}
+
+void destroy_graph(mattohf_ctx* c) {
+  if (c->step_exec) {
+    cudaGraphExecDestroy(c->step_exec);
+    c->step_exec = nullptr;
+  }
+}
+
+int compute_tables(mattohf_ctx* ctx) {
+  const int NG = ctx->NG, NK = ctx->NK;
+  const int nd = 2 * NK - 1;
+  std::vector<double> q((size_t)nd * NG + NG);
+  for (int d = 0; d < nd; ++d) {
+    const int diff = d - (NK - 1);              // kr - kc
+    const int kr = std::max(0, diff);
+    const int kc = kr - diff;
+    for (int g = 0; g < NG; ++g) q[(size_t)d * NG + g] = (ctx->Gx[g] + ctx->kx[kr]) - ctx->kx[kc];
+  }
+  for (int g = 0; g < NG; ++g) q[(size_t)nd * NG + g] = ctx->Gx[g];
+  double* d_q = nullptr;
+  double* d_all = nullptr;
+  CKR(dalloc(ctx, &d_q, q.size()));
+  CKR(dalloc(ctx, &d_all, q.size()));
+  CK(cudaMemcpyAsync(d_q, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+  CK(launch_vck_table(NG, NK, ctx->acell, d_q, (int)q.size(), d_all, ctx->st));
+  CKR(dalloc(ctx, &ctx->d_vcq, (size_t)nd * NG));
+  CKR(dalloc(ctx, &ctx->d_vCG, NG));
+  CKR(dalloc(ctx, &ctx->d_kern, (size_t)nd * NG));
+  CK(cudaMemcpyAsync(ctx->d_vcq, d_all, sizeof(double) * nd * NG, cudaMemcpyDeviceToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->d_vCG, d_all + (size_t)nd * NG, sizeof(double) * NG,
+                     cudaMemcpyDeviceToDevice, ctx->st));
+  CK(cudaMemsetAsync(ctx->d_vCG, 0, sizeof(double), ctx->st));  // vCG(1) = 0 (I:146)
+  CK(launch_make_kern(NG, NK, ctx->d_vcq, ctx->d_kern, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  cudaFree(d_q);
+  cudaFree(d_all);
+  return MATTOHF_OK;
+}
+
+void compute_vion(mattohf_ctx* c) {
+  const int NG = c->NG;
+  c->vion.assign(NG, 0.0);
+  const double ax = c->acell;
+  for (size_t ii = 0; ii < c->Rion.size(); ++ii) {
+    const int sp = c->Kion[ii] - 1;
+    const double Za = c->Zeff[sp], al = c->alpha[sp];
+    for (int icell = -4 * c->NK; icell <= 4 * c->NK; ++icell) {
+      for (int g = 0; g < NG; ++g) {
+        const double dist = std::fabs(c->rx[g] - ax * c->Rion[ii] - ax * (double)icell);
+        c->vion[g] = c->vion[g] - Za / std::sqrt(dist * dist + al * al);
+      }
+    }
+  }
+  double top = c->vion.empty() ? 0.0 : c->vion[0];
+  for (double v : c->vion) top = std::max(top, v);
+  for (double& v : c->vion) v = v - top;
+}
+
+int ensure_series(mattohf_ctx* ctx, int nt) {
+  if (nt <= ctx->series_cap) return MATTOHF_OK;
+  destroy_graph(ctx);  // graph holds the old pointers
+  CKR(dalloc(ctx, &ctx->d_A, nt));
+  CKR(dalloc(ctx, &ctx->d_Aave, nt));
+  CKR(dalloc(ctx, &ctx->d_sE, nt));
+  CKR(dalloc(ctx, &ctx->d_sJ, nt));
+  CKR(dalloc(ctx, &ctx->d_sN, nt));
+  ctx->series_cap = nt;
+  return MATTOHF_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* mattohf_status_string(int s) {
+  switch (s) {
+    case MATTOHF_OK: return "ok";
+    case MATTOHF_ERR_ARG: return "invalid argument";
+    case MATTOHF_ERR_CUDA: return "CUDA error";
+    case MATTOHF_ERR_NONFINITE: return "non-finite state";
+    case MATTOHF_ERR_TIMEOUT: return "device wait timed out";
+    case MATTOHF_ERR_NOTCONV: return "not converged";
+    case MATTOHF_ERR_ALLOC: return "device allocation failed";
+    case MATTOHF_ERR_STATE: return "invalid state";
+    default: return "unknown status";
+  }
+}
+
+const char* mattohf_last_error(const mattohf_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out) {
+  if (!cfg || !out) return MATTOHF_ERR_ARG;
+  *out = nullptr;
+  const int NG = cfg->NG;
+  if (!(NG == 16 || NG == 32 || NG == 64 || NG == 128 || NG == 256 || NG == 512)) return MATTOHF_ERR_ARG;
+  if (cfg->NK < 1 || cfg->NB < 1 || cfg->NBocc < 1 || cfg->NBocc > cfg->NB) return MATTOHF_ERR_ARG;
+  if (!(cfg->acell > 0.0) || !std::isfinite(cfg->acell)) return MATTOHF_ERR_ARG;
+  if (cfg->nion < 0 || cfg->nspecies < 0) return MATTOHF_ERR_ARG;
+  if (cfg->nspecies > 0 && (!cfg->Zeff || !cfg->alpha)) return MATTOHF_ERR_ARG;
+  if (cfg->nion > 0 && (!cfg->Rion || !cfg->Kion || !cfg->Zeff || !cfg->alpha)) return MATTOHF_ERR_ARG;
+  for (int i = 0; i < cfg->nion; ++i)
+    if (cfg->Kion[i] < 1 || cfg->Kion[i] > cfg->nspecies) return MATTOHF_ERR_ARG;
+  if ((long long)cfg->NK * cfg->NB * NG > (1LL << 28)) return MATTOHF_ERR_ARG;
+
+  mattohf_ctx* ctx = new mattohf_ctx();
+  ctx->NG = NG;
+  ctx->NK = cfg->NK;
+  ctx->NB = cfg->NB;
+  ctx->NBocc = cfg->NBocc;
+  ctx->hf = cfg->functional_hf ? 1 : 0;
+  ctx->device = cfg->device;
+  ctx->acell = cfg->acell;
+  ctx->Zeff.assign(cfg->Zeff, cfg->Zeff + cfg->nspecies);
+  ctx->alpha.assign(cfg->alpha, cfg->alpha + cfg->nspecies);
+  ctx->Rion.assign(cfg->Rion, cfg->Rion + cfg->nion);
+  ctx->Kion.assign(cfg->Kion, cfg->Kion + cfg->nion);
+  // cell and grids (I:46-49, I:62, I:93-112)
+  ctx->vcell = std::fabs(cfg->acell);
+  ctx->bx = 2.0 * kPi / cfg->acell;
+  ctx->dvcell = ctx->vcell / (double)NG;
+  ctx->occ = 2.0 / (double)cfg->NK;
+  ctx->rx.resize(NG);
+  ctx->Gx.resize(NG);
+  for (int i = 0; i < NG; ++i) {
+    ctx->rx[i] = (double)i / (double)NG * cfg->acell;
+    ctx->Gx[i] = (i < NG / 2 ? (double)i : (double)(i - NG)) * ctx->bx;
+  }
+  ctx->kx.resize(cfg->NK);
+  for (int i = 1; i <= cfg->NK; ++i)
+    ctx->kx[i - 1] = (-0.5 + (2.0 * i - 1.0) / (double)(2 * cfg->NK)) * ctx->bx;
+  compute_vion(ctx);
+
+  int rc = MATTOHF_OK;
+  auto bail = [&](int r) {
+    mattohf_destroy(ctx);
+    return r;
+  };
+  {
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
+    e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
+  }
+  const size_t nu = orb_elems(ctx, ctx->NB);
+  if ((rc = dalloc(ctx, &ctx->tw, NG)) || (rc = dalloc(ctx, &ctx->d_Gx, NG)) ||
+      (rc = dalloc(ctx, &ctx->d_kx, ctx->NK)) || (rc = dalloc(ctx, &ctx->d_vion, NG)) ||
+      (rc = dalloc(ctx, &ctx->d_vloc, NG)) || (rc = dalloc(ctx, &ctx->d_rho, NG)) ||
+      (rc = dalloc(ctx, &ctx->d_scal, 8)) || (rc = dalloc(ctx, &ctx->d_out, 8)) ||
+      (rc = dalloc(ctx, &ctx->d_u, nu)) || (rc = dalloc(ctx, &ctx->d_us, nu)) ||
+      (rc = dalloc(ctx, &ctx->d_int, 8)))
+    return bail(rc);
+  for (int s = 0; s < 4; ++s)
+    if ((rc = dalloc(ctx, &ctx->d_k[s], nu))) return bail(rc);
+  if (cudaMemsetAsync(ctx->d_u, 0, nu * sizeof(double2), ctx->st) != cudaSuccess ||
+      cudaMemsetAsync(ctx->d_int, 0, 8 * sizeof(int), ctx->st) != cudaSuccess ||
+      cudaMemcpyAsync(ctx->d_Gx, ctx->Gx.data(), NG * sizeof(double), cudaMemcpyHostToDevice, ctx->st) != cudaSuccess ||
+      cudaMemcpyAsync(ctx->d_kx, ctx->kx.data(), ctx->NK * sizeof(double), cudaMemcpyHostToDevice, ctx->st) != cudaSuccess ||
+      cudaMemcpyAsync(ctx->d_vion, ctx->vion.data(), NG * sizeof(double), cudaMemcpyHostToDevice, ctx->st) != cudaSuccess)
+    return bail(MATTOHF_ERR_CUDA);
+  k_twiddles<<<(NG + 127) / 128, 128, 0, ctx->st>>>(ctx->tw, NG);
+  if (cudaGetLastError() != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
+  if ((rc = compute_tables(ctx))) return bail(rc);
+  *out = ctx;
+  return MATTOHF_OK;
+}
+
+int mattohf_destroy(mattohf_ctx* ctx) {
+  if (!ctx) return MATTOHF_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  destroy_graph(ctx);
+  for (auto& ev : ctx->fock_events) {
+    cudaEventDestroy(ev.first);
+    cudaEventDestroy(ev.second);
+  }
+  void* ptrs[] = {ctx->tw, ctx->d_Gx, ctx->d_kx, ctx->d_vCG, ctx->d_vcq, ctx->d_kern, ctx->d_vion,
+                  ctx->d_vloc, ctx->d_rho, ctx->d_scal, ctx->d_out, ctx->d_u, ctx->d_us, ctx->d_k[0],
+                  ctx->d_k[1], ctx->d_k[2], ctx->d_k[3], ctx->d_a, ctx->d_b, ctx->d_c,
+                  ctx->d_scratch, ctx->d_colbuf, ctx->d_int, ctx->d_A, ctx->d_Aave, ctx->d_sE,
+                  ctx->d_sJ, ctx->d_sN, ctx->d_work, ctx->d_hwork, ctx->d_M, ctx->d_V, ctx->d_evals,
+                  ctx->d_eps, ctx->d_err};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (ctx->st) cudaStreamDestroy(ctx->st);
+  delete ctx;
+  return MATTOHF_OK;
+}
+
+int mattohf_set_option(mattohf_ctx* ctx, int option, long long value) {
+  if (!ctx) return MATTOHF_ERR_ARG;
+  switch (option) {
+    case MATTOHF_OPT_GRAPH: ctx->opt_graph = value ? 1 : 0; break;
+    case MATTOHF_OPT_FOCK_CHUNKS:
+      if (value < 0) return fail(ctx, MATTOHF_ERR_ARG, "chunks must be >= 0");
+      ctx->opt_chunks = (int)value;
+      break;
+    case MATTOHF_OPT_KERNEL_TIMING: ctx->opt_timing = value ? 1 : 0; break;
+    case MATTOHF_OPT_SYMMETRIC: ctx->opt_sym = value ? 1 : 0; break;
+    default: return fail(ctx, MATTOHF_ERR_ARG, "unknown option");
+  }
+  destroy_graph(ctx);
+  return MATTOHF_OK;
+}
+
+int mattohf_get_grids(mattohf_ctx* ctx, double* rx, double* Gx, double* kx, double* cell) {
+  if (!ctx) return MATTOHF_ERR_ARG;
+  if (rx) std::memcpy(rx, ctx->rx.data(), sizeof(double) * ctx->NG);
+  if (Gx) std::memcpy(Gx, ctx->Gx.data(), sizeof(double) * ctx->NG);
+  if (kx) std::memcpy(kx, ctx->kx.data(), sizeof(double) * ctx->NK);
+  if (cell) {
+    cell[0] = ctx->vcell;
+    cell[1] = ctx->dvcell;
+    cell[2] = ctx->bx;
+  }
+  return MATTOHF_OK;
+}
+
+int mattohf_get_coulomb(mattohf_ctx* ctx, double* vCG, double* vCq) {
+  CKR(check_ctx(ctx));
+  if (vCG) CK(cudaMemcpyAsync(vCG, ctx->d_vCG, sizeof(double) * ctx->NG, cudaMemcpyDeviceToHost, ctx->st));
+  if (vCq)
+    CK(cudaMemcpyAsync(vCq, ctx->d_vcq, sizeof(double) * ctx->NG * (2 * ctx->NK - 1),
+                       cudaMemcpyDeviceToHost, ctx->st));
+  return sync_and_flag(ctx);
+}
+
+int mattohf_get_vion(mattohf_ctx* ctx, double* vion) {
+  if (!ctx || !vion) return MATTOHF_ERR_ARG;
+  std::memcpy(vion, ctx->vion.data(), sizeof(double) * ctx->NG);
+  return MATTOHF_OK;
+}
+
+int mattohf_set_vion(mattohf_ctx* ctx, const double* vion) {
+  CKR(check_ctx(ctx));
+  if (!vion) return fail(ctx, MATTOHF_ERR_ARG, "null vion");
+  ctx->vion.assign(vion, vion + ctx->NG);
+  CK(cudaMemcpyAsync(ctx->d_vion, ctx->vion.data(), sizeof(double) * ctx->NG, cudaMemcpyHostToDevice, ctx->st));
+  return sync_and_flag(ctx);
+}
+
+int mattohf_set_orbitals(mattohf_ctx* ctx, const double* ubk) {
+  CKR(check_ctx(ctx));
+  if (!ubk) return fail(ctx, MATTOHF_ERR_ARG, "null ubk");
+  CK(cudaMemcpyAsync(ctx->d_u, ubk, sizeof(double2) * orb_elems(ctx, ctx->NB), cudaMemcpyHostToDevice, ctx->st));
+  return sync_and_flag(ctx);
+}
+
+int mattohf_get_orbitals(mattohf_ctx* ctx, double* ubk) {
+  CKR(check_ctx(ctx));
+  if (!ubk) return fail(ctx, MATTOHF_ERR_ARG, "null ubk");
+  CK(cudaMemcpyAsync(ubk, ctx->d_u, sizeof(double2) * orb_elems(ctx, ctx->NB), cudaMemcpyDeviceToHost, ctx->st));
+  return sync_and_flag(ctx);
+}
+
+int mattohf_init_wf(mattohf_ctx* ctx) {
+  CKR(check_ctx(ctx));
+  // Init_wf (M:159-184) with quickrnd (M:186-196)
+  std::vector<double> u(2 * orb_elems(ctx, ctx->NB));
+  int iseed = 123;
+  for (int ik = 0; ik < ctx->NK; ++ik)
+    for (int ib = 0; ib < ctx->NB; ++ib) {
+      iseed = (iseed * 106 + 1283) % 6075;
+      const double rnd = (double)iseed / 6075.0;
+      const double rxc = rnd * ctx->acell;
+      for (int g = 0; g < ctx->NG; ++g) {
+        const double d = ctx->rx[g] - rxc;
+        const size_t o = 2 * (((size_t)ik * ctx->NB + ib) * ctx->NG + g);
+        u[o] = std::exp(-0.5 * (d * d));
+        u[o + 1] = 0.0;
+      }
+    }
+  return mattohf_set_orbitals(ctx, u.data());
+}
+
+int mattohf_gram_schmidt(mattohf_ctx* ctx) {
+  CKR(check_ctx(ctx));
+  GsArgs a;
+  a.u = ctx->d_u;
+  a.kstride = ctx->NB * ctx->NG;
+  a.nb = ctx->NB;
+  a.weight = ctx->vcell / (double)ctx->NG;
+  a.flag = ctx->d_int + 2;
+  CK(launch_gram_schmidt(ctx->NG, a, ctx->NK, ctx->st));
+  return sync_and_flag(ctx);
+}
+
+static int hpsi_host(mattohf_ctx* ctx, const double* ubk, const double* wbk, int nbw, double A,
+                     double* out, int mode) {
+  CKR(check_ctx(ctx));
+  if (!wbk || !out || nbw < 1 || (mode != CM_T && !ubk))
+    return fail(ctx, MATTOHF_ERR_ARG, "bad hpsi arguments");
+  const int NG = ctx->NG, NB = ctx->NB;
+  const size_t nw = orb_elems(ctx, nbw), nu = orb_elems(ctx, NB);
+  CKR(ensure_stage(ctx, std::max(nw, nu)));
+  if (mode != CM_T)
+    CK(cudaMemcpyAsync(ctx->d_a, ubk, sizeof(double2) * nu, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->d_b, wbk, sizeof(double2) * nw, cudaMemcpyHostToDevice, ctx->st));
+  CKR(enq_hpsi(ctx, blk(ctx->d_a, NB, NG, NB), blk(ctx->d_b, nbw, NG, nbw),
+               blko(ctx->d_c, nbw, NG, nbw), aval(A), mode));
+  CK(cudaMemcpyAsync(out, ctx->d_c, sizeof(double2) * nw, cudaMemcpyDeviceToHost, ctx->st));
+  return sync_and_flag(ctx);
+}
+
+int mattohf_hpsi(mattohf_ctx* ctx, const double* ubk, const double* wbk, int nbw, double A, double* hwbk) {
+  return hpsi_host(ctx, ubk, wbk, nbw, A, hwbk, CM_H);
+}
+
+int mattohf_fock(mattohf_ctx* ctx, const double* ubk, const double* wbk, int nbw, double* vF) {
+  return hpsi_host(ctx, ubk, wbk, nbw, 0.0, vF, CM_F);
+}
+
+int mattohf_kinetic(mattohf_ctx* ctx, const double* wbk, int nbw, double A, double* tbk) {
+  return hpsi_host(ctx, nullptr, wbk, nbw, A, tbk, CM_T);
+}
+
+int mattohf_hpsi_device(mattohf_ctx* ctx, const double* d_ubk, const double* d_wbk, int nbw, double A,
+                        double* d_hwbk) {
+  CKR(check_ctx(ctx));
+  if (!d_ubk || !d_wbk || !d_hwbk || nbw < 1) return fail(ctx, MATTOHF_ERR_ARG, "bad hpsi arguments");
+  const int NG = ctx->NG, NB = ctx->NB;
+  return enq_hpsi(ctx, blk((const double2*)d_ubk, NB, NG, NB), blk((const double2*)d_wbk, nbw, NG, nbw),
+                  blko((double2*)d_hwbk, nbw, NG, nbw), aval(A), CM_H);
+}
+
+int mattohf_density(mattohf_ctx* ctx, const double* ubk, double* dns, double* vH) {
+  CKR(check_ctx(ctx));
+  if (!ubk) return fail(ctx, MATTOHF_ERR_ARG, "null ubk");
+  const size_t nu = orb_elems(ctx, ctx->NB);
+  CKR(ensure_stage(ctx, nu));
+  CK(cudaMemcpyAsync(ctx->d_a, ubk, sizeof(double2) * nu, cudaMemcpyHostToDevice, ctx->st));
+  CKR(enq_density(ctx, blk(ctx->d_a, ctx->NB, ctx->NG, ctx->NB)));
+  std::vector<double> vloc(ctx->NG);
+  if (dns) CK(cudaMemcpyAsync(dns, ctx->d_rho, sizeof(double) * ctx->NG, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(vloc.data(), ctx->d_vloc, sizeof(double) * ctx->NG, cudaMemcpyDeviceToHost, ctx->st));
+  CKR(sync_and_flag(ctx));
+  // vloc = vH + vion on the device; the Hartree part alone is recovered exactly
+  // only up to rounding, so vH is recomputed from a zero-vion pass instead.
+  if (vH) {
+    CK(cudaMemsetAsync(ctx->d_vion, 0, sizeof(double) * ctx->NG, ctx->st));
+    CKR(enq_density(ctx, blk(ctx->d_a, ctx->NB, ctx->NG, ctx->NB)));
+    CK(cudaMemcpyAsync(vH, ctx->d_vloc, sizeof(double) * ctx->NG, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(ctx->d_vion, ctx->vion.data(), sizeof(double) * ctx->NG, cudaMemcpyHostToDevice, ctx->st));
+    CKR(sync_and_flag(ctx));
+  }
+  return MATTOHF_OK;
+}
+
+int mattohf_observables(mattohf_ctx* ctx, double A, double* Ecomps, double* Etot, double* Je, double* Nele) {
+  CKR(check_ctx(ctx));
+  CKR(enq_observables(ctx, ctx->d_u, aval(A), false));
+  double o[8];
+  CK(cudaMemcpyAsync(o, ctx->d_out, sizeof(double) * 7, cudaMemcpyDeviceToHost, ctx->st));
+  CKR(sync_and_flag(ctx));
+  if (Ecomps) {
+    Ecomps[0] = o[1];
+    Ecomps[1] = o[2];
+    Ecomps[2] = o[3];
+    Ecomps[3] = o[4];
+  }
+  if (Etot) *Etot = o[0];
+  if (Je) *Je = o[5];
+  if (Nele) *Nele = o[6];
+  return MATTOHF_OK;
+}
+
+int mattohf_rk4_step(mattohf_ctx* ctx, double Aave, double A, double dt) {
+  CKR(check_ctx(ctx));
+  CK(cudaMemsetAsync(ctx->d_int + 1, 0, sizeof(int), ctx->st));
+  CKR(enq_rk4(ctx, aval(2.0 * Aave - A), aval(Aave), aval(A), dt));
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, ctx->d_int + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CKR(sync_and_flag(ctx));
+  if (flag) return fail(ctx, MATTOHF_ERR_NONFINITE, "non-finite orbitals after RK4 step");
+  return MATTOHF_OK;
+}
+
+int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const double* Aave,
+                    double* Etot, double* Je, double* Nele) {
+  CKR(check_ctx(ctx));
+  if (nt < 0 || (nt > 0 && (!A || !Aave))) return fail(ctx, MATTOHF_ERR_ARG, "bad rk4_run arguments");
+  if (nt == 0) return MATTOHF_OK;
+  CKR(ensure_series(ctx, nt));
+  CKR(ensure_scratch(ctx, ctx->NK * ctx->NB));
+  CK(cudaMemcpyAsync(ctx->d_A, A, sizeof(double) * nt, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->d_Aave, Aave, sizeof(double) * nt, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemsetAsync(ctx->d_int, 0, 2 * sizeof(int), ctx->st));
+  AField fm, fave, fcur;
+  fm.A = fave.A = fcur.A = ctx->d_A;
+  fm.Aave = fave.Aave = fcur.Aave = ctx->d_Aave;
+  fm.it = fave.it = fcur.it = ctx->d_int;
+  fm.val = fave.val = fcur.val = 0.0;
+  fm.mode = AM;
+  fave.mode = AAVE;
+  fcur.mode = ACUR;
+  const bool use_graph = ctx->opt_graph && !ctx->opt_timing;
+  if (use_graph && (!ctx->step_exec || ctx->step_dt != dt)) {
+    destroy_graph(ctx);
+    cudaGraph_t g;
+    ctx->capturing = true;
+    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+    int rc = enq_rk4(ctx, fm, fave, fcur, dt);
+    if (rc == MATTOHF_OK) rc = enq_observables(ctx, ctx->d_u, fcur, true);
+    cudaError_t ec = cudaStreamEndCapture(ctx->st, &g);
+    ctx->capturing = false;
+    if (rc != MATTOHF_OK) return rc;
+    CK(ec);
+    cudaError_t ei = cudaGraphInstantiate(&ctx->step_exec, g, 0);
+    cudaGraphDestroy(g);
+    CK(ei);
+    ctx->step_dt = dt;
+  }
+  ctx->fock_event_used = 0;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, ctx->st));
+  int flag = 0;
+  int bad_at = -1;
+  for (int it = 0; it < nt; ++it) {
+    if (use_graph) {
+      CK(cudaGraphLaunch(ctx->step_exec, ctx->st));
+    } else {
+      CKR(enq_rk4(ctx, fm, fave, fcur, dt));
+      CKR(enq_observables(ctx, ctx->d_u, fcur, true));
+    }
+    // bounded detection of a blow-up: poll the flag every 256 steps
+    if ((it & 255) == 255 && it + 1 < nt) {
+      CK(cudaMemcpyAsync(&flag, ctx->d_int + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+      CK(cudaStreamSynchronize(ctx->st));
+      if (flag) {
+        bad_at = it;
+        break;
+      }
+    }
+  }
+  CK(cudaEventRecord(e1, ctx->st));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->last_run_ms = ms;
+  ctx->last_fock_ms = 0;
+  ctx->last_fock_launches = (int)ctx->fock_event_used;
+  for (size_t i = 0; i < ctx->fock_event_used; ++i) {
+    float f = 0;
+    CK(cudaEventElapsedTime(&f, ctx->fock_events[i].first, ctx->fock_events[i].second));
+    ctx->last_fock_ms += f;
+  }
+  const int ndone = bad_at >= 0 ? bad_at + 1 : nt;
+  std::vector<double> sE(ndone), sJ(ndone), sN(ndone);
+  CK(cudaMemcpyAsync(sE.data(), ctx->d_sE, sizeof(double) * ndone, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(sJ.data(), ctx->d_sJ, sizeof(double) * ndone, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(sN.data(), ctx->d_sN, sizeof(double) * ndone, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(&flag, ctx->d_int + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CKR(sync_and_flag(ctx));
+  if (Etot) std::copy(sE.begin(), sE.end(), Etot);
+  if (Je) std::copy(sJ.begin(), sJ.end(), Je);
+  if (Nele) std::copy(sN.begin(), sN.end(), Nele);
+  if (flag) {
+    int first = ndone - 1;
+    for (int i = 0; i < ndone; ++i)
+      if (!(std::isfinite(sE[i]) && std::isfinite(sJ[i]) && std::isfinite(sN[i]))) {
+        first = i;
+        break;
+      }
+    char buf[160];
+    std::snprintf(buf, sizeof(buf), "non-finite state at RK4 step %d (1-based it=%d); %d steps run",
+                  first, first + 1, ndone);
+    return fail(ctx, MATTOHF_ERR_NONFINITE, buf);
+  }
+  return MATTOHF_OK;
+}
+
+int mattohf_last_run_timing(mattohf_ctx* ctx, double* run_ms, double* fock_ms, int* fock_launches) {
+  if (!ctx) return MATTOHF_ERR_ARG;
+  if (run_ms) *run_ms = ctx->last_run_ms;
+  if (fock_ms) *fock_ms = ctx->last_fock_ms;
+  if (fock_launches) *fock_launches = ctx->last_fock_launches;
+  return MATTOHF_OK;
+}
+
+static int ensure_gs(mattohf_ctx* ctx, int m) {
+  const size_t need = orb_elems(ctx, m);
+  if (need <= ctx->gs_cap) return MATTOHF_OK;
+  CKR(dalloc(ctx, &ctx->d_work, need));
+  CKR(dalloc(ctx, &ctx->d_hwork, need));
+  CKR(dalloc(ctx, &ctx->d_M, (size_t)ctx->NK * m * m));
+  CKR(dalloc(ctx, &ctx->d_V, (size_t)ctx->NK * m * m));
+  CKR(dalloc(ctx, &ctx->d_evals, (size_t)ctx->NK * m));
+  CKR(dalloc(ctx, &ctx->d_eps, (size_t)ctx->NK * ctx->NB));
+  CKR(dalloc(ctx, &ctx->d_err, (size_t)ctx->NK * ctx->NB));
+  ctx->gs_cap = need;
+  return MATTOHF_OK;
+}
+
+// Rayleigh-Ritz of the m columns in x (their h-images in hx) keeping the
+// lowest nout Ritz vectors into out.
+static int enq_rayleigh_ritz(mattohf_ctx* ctx, const double2* x, const double2* hx, int m, int nout,
+                             double2* out) {
+  const int NG = ctx->NG;
+  CK(launch_project(NG, x, hx, m * NG, m, ctx->dvcell, ctx->d_M, ctx->NK, ctx->st));
+  CK(launch_jacobi(ctx->d_M, m, ctx->d_evals, ctx->d_V, ctx->NK, ctx->d_int + 2, ctx->st));
+  CK(launch_rotate(NG, x, m * NG, m, ctx->d_V, nout, out, ctx->NB * NG, ctx->NK, ctx->st));
+  return MATTOHF_OK;
+}
+
+int mattohf_eps(mattohf_ctx* ctx, double* epsbk, double* epserrorbk) {
+  CKR(check_ctx(ctx));
+  const int NG = ctx->NG, NB = ctx->NB;
+  CKR(ensure_gs(ctx, NB));
+  Block ub = blk(ctx->d_u, NB, NG, NB);
+  CKR(enq_hpsi(ctx, ub, ub, blko(ctx->d_hwork, NB, NG, NB), aval(0.0), CM_H));
+  CK(launch_eps(NG, ctx->d_u, ctx->d_hwork, NB * NG, NB, ctx->dvcell, ctx->d_eps, ctx->d_err, ctx->NK, ctx->st));
+  if (epsbk) CK(cudaMemcpyAsync(epsbk, ctx->d_eps, sizeof(double) * ctx->NK * NB, cudaMemcpyDeviceToHost, ctx->st));
+  if (epserrorbk)
+    CK(cudaMemcpyAsync(epserrorbk, ctx->d_err, sizeof(double) * ctx->NK * NB, cudaMemcpyDeviceToHost, ctx->st));
+  return sync_and_flag(ctx);
+}
+
+int mattohf_gs_run(mattohf_ctx* ctx, int nscf, int ncg, double* Etot_iter, double* Je_iter,
+                   double* dnsdiff, double* epsbk, double* epserrorbk) {
+  CKR(check_ctx(ctx));
+  const int NG = ctx->NG, NB = ctx->NB, NK = ctx->NK;
+  if (nscf < 0 || ncg < 1) return fail(ctx, MATTOHF_ERR_ARG, "nscf >= 0 and ncg >= 1 required");
+  const int m = NB * ncg;
+  if (m > 64 || m > NG) return fail(ctx, MATTOHF_ERR_ARG, "NB*NCG must be <= 64 and <= NG");
+  CKR(ensure_gs(ctx, m));
+  CK(cudaMemsetAsync(ctx->d_int + 2, 0, sizeof(int), ctx->st));
+  const double dnsmix = 0.5;
+  std::vector<double> dprev(NG), dnew(NG);
+  double o[8];
+  // Etotscf(0) and dnsscf(:,1) (GS:26-27)
+  CKR(enq_observables(ctx, ctx->d_u, aval(0.0), false));
+  CK(cudaMemcpyAsync(o, ctx->d_out, sizeof(double) * 7, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(dprev.data(), ctx->d_rho, sizeof(double) * NG, cudaMemcpyDeviceToHost, ctx->st));
+  CKR(sync_and_flag(ctx));
+  if (Etot_iter) Etot_iter[0] = o[0];
+  GsArgs gsa;
+  gsa.u = ctx->d_u;
+  gsa.kstride = NB * NG;
+  gsa.nb = NB;
+  gsa.weight = ctx->vcell / (double)NG;
+  gsa.flag = ctx->d_int + 2;
+  Block ub = blk(ctx->d_u, NB, NG, NB);
+  for (int iter = 0; iter < nscf; ++iter) {
+    CK(launch_gram_schmidt(NG, gsa, NK, ctx->st));
+    // KS_ubk2_SVD (GS:124-194): Krylov block [u, h u, h^2 u, ...]
+    CK(cudaMemcpy2DAsync(ctx->d_work, sizeof(double2) * m * NG, ctx->d_u, sizeof(double2) * NB * NG,
+                         sizeof(double2) * NB * NG, NK, cudaMemcpyDeviceToDevice, ctx->st));
+    for (int icg = 1; icg < ncg; ++icg) {
+      Block wb = blk(ctx->d_work + (size_t)(icg - 1) * NB * NG, m, NG, NB);
+      BlockOut ob = blko(ctx->d_work + (size_t)icg * NB * NG, m, NG, NB);
+      CKR(enq_hpsi(ctx, ub, wb, ob, aval(0.0), CM_H));
+    }
+    CK(launch_block_orth(NG, ctx->d_work, m * NG, m, ctx->dvcell, NK, ctx->d_int + 2, ctx->st));
+    CKR(enq_hpsi(ctx, ub, blk(ctx->d_work, m, NG, m), blko(ctx->d_hwork, m, NG, m), aval(0.0), CM_H));
+    CKR(enq_rayleigh_ritz(ctx, ctx->d_work, ctx->d_hwork, m, NB, ctx->d_u));
+    CK(launch_gram_schmidt(NG, gsa, NK, ctx->st));
+    // Subspace_diag (GS:197-237)
+    CKR(enq_hpsi(ctx, ub, ub, blko(ctx->d_hwork, NB, NG, NB), aval(0.0), CM_H));
+    CK(cudaMemcpyAsync(ctx->d_work, ctx->d_u, sizeof(double2) * orb_elems(ctx, NB), cudaMemcpyDeviceToDevice, ctx->st));
+    CKR(enq_rayleigh_ritz(ctx, ctx->d_work, ctx->d_hwork, NB, NB, ctx->d_u));
+    // Etot, Je (GS:36-38); the Fock partials of h[u]u are then reused for the
+    // Ritz values and residuals (GS:42-43), which apply the same operator.
+    CKR(enq_observables(ctx, ctx->d_u, aval(0.0), false));
+    {
+      int nch, ch;
+      fock_split(ctx, NK * NB, &nch, &ch);
+      if (!ctx->hf) nch = 1;
+      CombineArgs a = combine_base(ctx, ub, aval(0.0), CM_H, nch);
+      a.out = blko(ctx->d_hwork, NB, NG, NB);
+      CK(launch_combine(NG, a, NK * NB, ctx->st));
+    }
+    CK(launch_eps(NG, ctx->d_u, ctx->d_hwork, NB * NG, NB, ctx->dvcell, ctx->d_eps, ctx->d_err, NK, ctx->st));
+    CK(cudaMemcpyAsync(o, ctx->d_out, sizeof(double) * 7, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(dnew.data(), ctx->d_rho, sizeof(double) * NG, cudaMemcpyDeviceToHost, ctx->st));
+    CKR(sync_and_flag(ctx));
+    if (Etot_iter) Etot_iter[iter + 1] = o[0];
+    if (Je_iter) Je_iter[iter] = o[5];
+    double dd = 0.0;
+    for (int g = 0; g < NG; ++g) {
+      const double mixed = dnsmix * dnew[g] + (1.0 - dnsmix) * dprev[g];  // GS:44
+      dd += std::fabs(mixed - dprev[g]);
+      dprev[g] = mixed;
+    }
+    if (dnsdiff) dnsdiff[iter] = dd / (double)NG;
+  }
+  if (epsbk) CK(cudaMemcpyAsync(epsbk, ctx->d_eps, sizeof(double) * NK * NB, cudaMemcpyDeviceToHost, ctx->st));
+  if (epserrorbk) CK(cudaMemcpyAsync(epserrorbk, ctx->d_err, sizeof(double) * NK * NB, cudaMemcpyDeviceToHost, ctx->st));
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, ctx->d_int + 2, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CKR(sync_and_flag(ctx));
+  if (flag) return fail(ctx, MATTOHF_ERR_NOTCONV, flag == 2 ? "Jacobi eigensolver did not converge"
+                                                             : "orthonormalisation met a zero column");
+  return MATTOHF_OK;
+}
+
+int mattohf_synchronize(mattohf_ctx* ctx) {
+  CKR(check_ctx(ctx));
+  return sync_and_flag(ctx);
+}
+
+}  // extern "C"

@@ -1,0 +1,155 @@
+// Internal declarations shared by the host runtime and the kernel translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace mattohf {
+
+constexpr int kThreads = 128;  // threads per CTA for the column/pair kernels (4 warps)
+
+// How a kernel obtains the vector potential of the current launch.
+//   AVAL : use `A_val` directly
+//   AM   : A(it-1) recovered as 2*Aave(it) - A(it)        (src/RT_calculation.f90:165)
+//   AAVE : Aave(it)
+//   ACUR : A(it)
+enum AMode : int { AVAL = 0, AM = 1, AAVE = 2, ACUR = 3 };
+
+struct AField {
+  int mode;
+  double val;
+  const double* A;      // device, per time step
+  const double* Aave;   // device, per time step
+  const int* it;        // device step counter (0-based)
+};
+
+__device__ __forceinline__ double afield_value(const AField& f) {
+  if (f.mode == AVAL) return f.val;
+  const int it = *f.it;
+  if (f.mode == AM) return 2.0 * f.Aave[it] - f.A[it];
+  if (f.mode == AAVE) return f.Aave[it];
+  return f.A[it];
+}
+
+// Orbital-like arrays are [NK][ld][NG] complex128; a "block" view selects `nb`
+// consecutive bands starting at band offset `b0` of every k.
+struct Block {
+  const double2* p;  // points at band b0 of k = 0
+  int kstride;       // complex elements between consecutive k (ld * NG)
+  int nb;            // bands per k in this view
+};
+struct BlockOut {
+  double2* p;
+  int kstride;
+  int nb;
+};
+
+struct DensArgs {
+  Block u;            // all NB bands
+  int nbocc;
+  double occ;         // 2/NK for occupied bands, 0 otherwise (src/Initialization.f90:179-186)
+  const double* vCG;  // NG
+  const double* vion; // NG
+  const double2* tw;  // NG forward twiddles
+  double dvcell;
+  double* rho;        // NG out
+  double* vloc;       // NG out: vH + vion
+  double* scal;       // out: [0]=Nele, [1]=Eion, [2]=EH
+  int nk;
+};
+
+struct FockArgs {
+  Block u;              // occupied orbitals (bands 0..nbocc-1 used)
+  Block w;              // rows the exchange operator acts on
+  int nk, nbocc;
+  const double* kern;   // (2NK-1) x NG : -v(G + kx(kr) - kx(kc)) / (NG*NK), index d = kr-kc+NK-1
+  const double2* tw;
+  double2* scratch;     // [ncols*nchunks][NG] partial sums
+  int nchunks;
+  int chunk;            // pairs per chunk
+};
+
+enum CombineMode : int {
+  CM_H = 0,     // out = T_A w + vloc w + F
+  CM_RK0 = 1,   // k0 = -i h ; next = u0 + (0.5 dt) k0
+  CM_RK1 = 2,   // k1 = -i h ; next = u0 + (0.5 dt) k1
+  CM_RK2 = 3,   // k2 = -i h ; next = u0 + dt k2
+  CM_RK3 = 4,   // u0 += (k0 + 2 k1 + 2 k2 + k3) dt / 6
+  CM_OBS = 5,   // per-column Ekin, Je, <w|F> partials (no array output)
+  CM_F = 6,     // out = F only (exchange term alone)
+  CM_T = 7,     // out = T_A w only (kinetic term alone)
+};
+
+struct CombineArgs {
+  Block w;                  // columns being processed (the h-apply's wbk)
+  BlockOut out;             // h output (CM_H / CM_F / CM_T) or stage input (CM_RK0..2)
+  double2* u0;              // RK4 base state [NK][NB][NG] (CM_RK*)
+  double2* kbuf[4];         // RK4 stage derivatives [NK][NB][NG]
+  const double2* scratch;   // Fock partials (may be null when the Fock term is off)
+  int nchunks;
+  const double* vloc;       // NG
+  const double* Gx;         // NG
+  const double* kx;         // NK
+  const double2* tw;
+  AField af;
+  double dt;
+  int mode;
+  int nk;
+  int nbocc;
+  double occ;
+  double* colbuf;           // CM_OBS: [ncols][4] = Ekin part, J part, Re<w|F>, Im<w|F>
+  int* nonfinite;           // set to 1 if any output is not finite
+};
+
+struct ObsReduceArgs {
+  const double* colbuf;     // [nk*nb][4]
+  const double* scal;       // dens scalars: Nele, Eion, EH
+  int nk, nb, nbocc;
+  double occ, dvcell, vcell, NGd;
+  int hf;
+  double* out;              // [0]=Etot [1]=Ekin [2]=Eion [3]=EH [4]=Ex [5]=Je [6]=Nele
+  double* series_E;         // per step (may be null)
+  double* series_J;
+  double* series_N;
+  int* it;                  // step counter, incremented when `advance`
+  int advance;
+  int* nonfinite;
+};
+
+// Launchers (defined in k_hpsi.cu); all return cudaGetLastError() of the launch.
+cudaError_t launch_density(int NG, const DensArgs& a, cudaStream_t s);
+cudaError_t launch_fock(int NG, const FockArgs& a, int ncols, cudaStream_t s);
+cudaError_t launch_combine(int NG, const CombineArgs& a, int ncols, cudaStream_t s);
+cudaError_t launch_obs_reduce(const ObsReduceArgs& a, cudaStream_t s);
+
+// Tables (k_table.cu)
+cudaError_t launch_vck_table(int NG, int NK, double acell, const double* d_q, int nq,
+                             double* d_out, cudaStream_t s);
+cudaError_t launch_make_kern(int NG, int NK, const double* vcq, double* kern, cudaStream_t s);
+
+// Ground-state kernels (k_gs.cu)
+struct GsArgs {
+  double2* u;      // [NK][ld][NG]
+  int kstride;     // ld*NG
+  int nb;          // columns per k to process
+  double weight;   // inner-product weight (vcell/NG or dvcell)
+  int* flag;       // error flag
+};
+cudaError_t launch_gram_schmidt(int NG, const GsArgs& a, int nk, cudaStream_t s);
+// Projected matrix M[k][i][j] = <x_i|y_j>*weight for i,j < m
+cudaError_t launch_project(int NG, const double2* x, const double2* y, int kstride, int m,
+                           double weight, double2* M, int nk, cudaStream_t s);
+// Jacobi eigen-decomposition of nk Hermitian m x m matrices (hermitised from the
+// lower triangle, real diagonal); eigenvalues ascending, vectors in columns.
+cudaError_t launch_jacobi(const double2* M, int m, double* evals, double2* evecs, int nk,
+                          int* flag, cudaStream_t s);
+// out[k][b] = sum_c x[k][c] * C[k][c][b] for b < nout
+cudaError_t launch_rotate(int NG, const double2* x, int xkstride, int m, const double2* C,
+                          int nout, double2* out, int okstride, int nk, cudaStream_t s);
+// Orthonormalise m columns per k (two passes of MGS) under weight.
+cudaError_t launch_block_orth(int NG, double2* x, int kstride, int m, double weight,
+                              int nk, int* flag, cudaStream_t s);
+// eps[k][b] = Re<u|h u> w ; err[k][b] = sqrt(sum|h u - eps u| * w)
+cudaError_t launch_eps(int NG, const double2* u, const double2* hu, int kstride, int nb,
+                       double w, double* eps, double* err, int nk, cudaStream_t s);
+
+}  // namespace mattohf

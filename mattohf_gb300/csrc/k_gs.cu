@@ -1,0 +1,320 @@
+// Ground-state kernels: Gram-Schmidt (src/mATTOHF.f90:134-157), Krylov block
+// orthonormalisation (replaces ZGESVD('O','N') of src/GS_calculation.f90:161-166),
+// projected matrices (GS:175-181, GS:218-224), a Jacobi Hermitian eigensolver
+// (replaces ZHEEV('V','U') of GS:183, GS:226), the subspace rotation
+// (GS:184-190, GS:227-231) and Ritz values / residuals (src/Functions.f90:321-358).
+//
+// All reductions run in a fixed order so results are bitwise reproducible.
+#include "internal.h"
+#include <cfloat>
+
+namespace mattohf {
+
+constexpr int kGsThreads = 256;
+
+// Fixed-order CTA sum of a complex value (kGsThreads threads).
+__device__ double2 block_sum2(double2 v, double2* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = kGsThreads / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      red[threadIdx.x].x += red[threadIdx.x + o].x;
+      red[threadIdx.x].y += red[threadIdx.x + o].y;
+    }
+    __syncthreads();
+  }
+  const double2 r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// Modified Gram-Schmidt of nb columns per k, `passes` projection sweeps per
+// column.  One pass with weight vcell/NG is the reference's Gram_Schmidt; two
+// passes give the orthonormal basis of the Krylov block.
+__global__ void __launch_bounds__(kGsThreads) k_mgs(double2* u, int kstride, int nb, int NG,
+                                                    double weight, int passes, int* flag) {
+  __shared__ double2 red[kGsThreads];
+  double2* base = u + (size_t)blockIdx.x * kstride;
+  for (int ib = 0; ib < nb; ++ib) {
+    double2* ub = base + (size_t)ib * NG;
+    for (int pass = 0; pass < passes; ++pass) {
+      for (int ibt = 0; ibt < ib; ++ibt) {
+        const double2* ut = base + (size_t)ibt * NG;
+        double2 s = make_double2(0.0, 0.0);
+        for (int i = threadIdx.x; i < NG; i += kGsThreads) {
+          const double2 a = ut[i], b = ub[i];
+          s.x += a.x * b.x + a.y * b.y;   // conj(a)*b
+          s.y += a.x * b.y - a.y * b.x;
+        }
+        double2 zov = block_sum2(s, red);
+        zov.x = zov.x * weight;
+        zov.y = zov.y * weight;
+        for (int i = threadIdx.x; i < NG; i += kGsThreads) {
+          const double2 a = ut[i];
+          double2 b = ub[i];
+          b.x -= a.x * zov.x - a.y * zov.y;
+          b.y -= a.x * zov.y + a.y * zov.x;
+          ub[i] = b;
+        }
+        __syncthreads();
+      }
+    }
+    double2 s = make_double2(0.0, 0.0);
+    for (int i = threadIdx.x; i < NG; i += kGsThreads) {
+      const double2 b = ub[i];
+      s.x += b.x * b.x + b.y * b.y;
+    }
+    const double nrm = block_sum2(s, red).x * weight;
+    if (!(nrm > 0.0) || !isfinite(nrm)) {
+      if (threadIdx.x == 0 && flag) *flag = 1;
+      continue;
+    }
+    const double sq = sqrt(nrm);
+    for (int i = threadIdx.x; i < NG; i += kGsThreads) {
+      double2 b = ub[i];
+      b.x = b.x / sq;
+      b.y = b.y / sq;
+      ub[i] = b;
+    }
+    __syncthreads();
+  }
+}
+
+// M[k][i][j] = sum_x conj(x_i) y_j * weight ; one warp per (k, i, j).
+__global__ void k_project(const double2* __restrict__ x, const double2* __restrict__ y, int kstride,
+                          int m, int NG, double weight, double2* __restrict__ M, int total) {
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= total) return;
+  const int k = wid / (m * m), ij = wid % (m * m), i = ij / m, j = ij % m;
+  const double2* xi = x + (size_t)k * kstride + (size_t)i * NG;
+  const double2* yj = y + (size_t)k * kstride + (size_t)j * NG;
+  double sr = 0.0, si = 0.0;
+  for (int g = lane; g < NG; g += 32) {
+    const double2 a = xi[g], b = yj[g];
+    sr += a.x * b.x + a.y * b.y;
+    si += a.x * b.y - a.y * b.x;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+    si += __shfl_xor_sync(0xffffffffu, si, o);
+  }
+  if (lane == 0) M[wid] = make_double2(sr * weight, si * weight);
+}
+
+// Cyclic Jacobi for a complex Hermitian m x m matrix, one CTA per k.
+// The matrix is built from the lower triangle of M (i > j) with a real
+// diagonal, like the reference's whw/ubhub assembly.  Converged when the
+// off-diagonal Frobenius norm is below 1e-15 of the full norm or after 60
+// sweeps (flag set).  Eigenvalues ascending; vectors in columns of V.
+constexpr int kJacMax = 64;
+__global__ void __launch_bounds__(128) k_jacobi(const double2* __restrict__ Min, int m,
+                                               double* __restrict__ evals,
+                                               double2* __restrict__ evecs, int* flag) {
+  extern __shared__ double2 jsm[];
+  double2* A = jsm;            // m*m, A[i*m+j]
+  double2* V = jsm + m * m;    // m*m
+  __shared__ double red[128];
+  __shared__ int order[kJacMax];
+  const int k = blockIdx.x;
+  const double2* Mk = Min + (size_t)k * m * m;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < m * m; idx += blockDim.x) {
+    const int i = idx / m, j = idx % m;
+    double2 v;
+    if (i > j) v = Mk[i * m + j];
+    else if (i < j) { v = Mk[j * m + i]; v.y = -v.y; }
+    else v = make_double2(Mk[i * m + i].x, 0.0);
+    A[idx] = v;
+    V[idx] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  bool converged = false;
+  for (int sweep = 0; sweep < 60 && !converged; ++sweep) {
+    // off-diagonal and total norms
+    double off = 0.0, tot = 0.0;
+    for (int idx = tid; idx < m * m; idx += blockDim.x) {
+      const double2 v = A[idx];
+      const double a2 = v.x * v.x + v.y * v.y;
+      tot += a2;
+      if (idx / m != idx % m) off += a2;
+    }
+    red[tid] = off;
+    __syncthreads();
+    for (int o = 64; o > 0; o >>= 1) { if (tid < o) red[tid] += red[tid + o]; __syncthreads(); }
+    off = red[0];
+    __syncthreads();
+    red[tid] = tot;
+    __syncthreads();
+    for (int o = 64; o > 0; o >>= 1) { if (tid < o) red[tid] += red[tid + o]; __syncthreads(); }
+    tot = red[0];
+    __syncthreads();
+    if (off <= 1e-30 * tot || off == 0.0) { converged = true; break; }
+    for (int p = 0; p < m - 1; ++p) {
+      for (int q = p + 1; q < m; ++q) {
+        const double2 apq = A[p * m + q];
+        const double mag = sqrt(apq.x * apq.x + apq.y * apq.y);
+        const double app = A[p * m + p].x, aqq = A[q * m + q].x;
+        if (mag == 0.0 || mag <= 1e-300) continue;
+        // zero A[p][q]: with apq = mag*e^{i phi}, rotate columns p, q by
+        // J = [[c, -s e^{i phi}], [s e^{-i phi}, c]] acting as A <- J^H A J.
+        const double tau = (aqq - app) / (2.0 * mag);
+        const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+        const double c = 1.0 / sqrt(1.0 + t * t);
+        const double s = t * c;
+        const double ph_r = apq.x / mag, ph_i = apq.y / mag;  // e^{i phi}
+        // column update: A[:,p], A[:,q]
+        for (int r = tid; r < m; r += blockDim.x) {
+          const double2 xp = A[r * m + p], xq = A[r * m + q];
+          // new_p = c xp - s e^{-i phi} xq ; new_q = s e^{i phi} xp + c xq
+          double2 np, nq;
+          np.x = c * xp.x - s * (ph_r * xq.x + ph_i * xq.y);
+          np.y = c * xp.y - s * (ph_r * xq.y - ph_i * xq.x);
+          nq.x = c * xq.x + s * (ph_r * xp.x - ph_i * xp.y);
+          nq.y = c * xq.y + s * (ph_r * xp.y + ph_i * xp.x);
+          A[r * m + p] = np;
+          A[r * m + q] = nq;
+          const double2 vp = V[r * m + p], vq = V[r * m + q];
+          double2 wp, wq;
+          wp.x = c * vp.x - s * (ph_r * vq.x + ph_i * vq.y);
+          wp.y = c * vp.y - s * (ph_r * vq.y - ph_i * vq.x);
+          wq.x = c * vq.x + s * (ph_r * vp.x - ph_i * vp.y);
+          wq.y = c * vq.y + s * (ph_r * vp.y + ph_i * vp.x);
+          V[r * m + p] = wp;
+          V[r * m + q] = wq;
+        }
+        __syncthreads();
+        // row update: A[p,:], A[q,:] with the conjugate transpose
+        for (int r = tid; r < m; r += blockDim.x) {
+          const double2 xp = A[p * m + r], xq = A[q * m + r];
+          double2 np, nq;
+          // new_p = c xp - s e^{i phi} xq ; new_q = s e^{-i phi} xp + c xq
+          np.x = c * xp.x - s * (ph_r * xq.x - ph_i * xq.y);
+          np.y = c * xp.y - s * (ph_r * xq.y + ph_i * xq.x);
+          nq.x = c * xq.x + s * (ph_r * xp.x + ph_i * xp.y);
+          nq.y = c * xq.y + s * (ph_r * xp.y - ph_i * xp.x);
+          A[p * m + r] = np;
+          A[q * m + r] = nq;
+        }
+        __syncthreads();
+        if (tid == 0) {
+          A[p * m + q] = make_double2(0.0, 0.0);
+          A[q * m + p] = make_double2(0.0, 0.0);
+          A[p * m + p].y = 0.0;
+          A[q * m + q].y = 0.0;
+        }
+        __syncthreads();
+      }
+    }
+  }
+  if (!converged && tid == 0 && flag) *flag = 2;
+  // ascending order (stable selection by index on ties)
+  if (tid == 0) {
+    for (int i = 0; i < m; ++i) order[i] = i;
+    for (int i = 1; i < m; ++i) {
+      const int oi = order[i];
+      const double v = A[oi * m + oi].x;
+      int j = i - 1;
+      while (j >= 0 && A[order[j] * m + order[j]].x > v) { order[j + 1] = order[j]; --j; }
+      order[j + 1] = oi;
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < m; i += blockDim.x) evals[(size_t)k * m + i] = A[order[i] * m + order[i]].x;
+  for (int idx = tid; idx < m * m; idx += blockDim.x) {
+    const int r = idx / m, cidx = idx % m;
+    evecs[(size_t)k * m * m + idx] = V[r * m + order[cidx]];  // [row][col]
+  }
+}
+
+// out[k][b][g] = sum_c x[k][c][g] * C[k][c][b], c ascending (GS:184-190).
+__global__ void k_rotate(const double2* __restrict__ x, int xkstride, int m,
+                         const double2* __restrict__ C, int nout, double2* __restrict__ out,
+                         int okstride, int NG, int nk) {
+  const size_t total = (size_t)nk * nout * NG;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const int g = (int)(i % NG);
+  const int b = (int)((i / NG) % nout);
+  const int k = (int)(i / ((size_t)NG * nout));
+  const double2* xk = x + (size_t)k * xkstride + g;
+  const double2* Ck = C + (size_t)k * m * m;
+  double2 s = make_double2(0.0, 0.0);
+  for (int c = 0; c < m; ++c) {
+    const double2 a = xk[(size_t)c * NG], w = Ck[c * m + b];
+    s.x += a.x * w.x - a.y * w.y;
+    s.y += a.x * w.y + a.y * w.x;
+  }
+  out[(size_t)k * okstride + (size_t)b * NG + g] = s;
+}
+
+// Ritz value and residual per column, one warp per (k, b) (F:321-358).
+__global__ void k_eps(const double2* __restrict__ u, const double2* __restrict__ hu, int kstride,
+                      int nb, int NG, double w, double* __restrict__ eps, double* __restrict__ err,
+                      int total) {
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= total) return;
+  const int k = wid / nb, b = wid % nb;
+  const double2* uc = u + (size_t)k * kstride + (size_t)b * NG;
+  const double2* hc = hu + (size_t)k * kstride + (size_t)b * NG;
+  double sr = 0.0;
+  for (int g = lane; g < NG; g += 32) sr += uc[g].x * hc[g].x + uc[g].y * hc[g].y;
+  for (int o = 16; o > 0; o >>= 1) sr += __shfl_xor_sync(0xffffffffu, sr, o);
+  const double e = sr * w;
+  double sa = 0.0;
+  for (int g = lane; g < NG; g += 32) {
+    const double rx = hc[g].x - e * uc[g].x, ry = hc[g].y - e * uc[g].y;
+    sa += hypot(rx, ry);  // abs, not abs^2 (F:353)
+  }
+  for (int o = 16; o > 0; o >>= 1) sa += __shfl_xor_sync(0xffffffffu, sa, o);
+  if (lane == 0) {
+    eps[wid] = e;
+    err[wid] = sqrt(sa * w);
+  }
+}
+
+cudaError_t launch_gram_schmidt(int NG, const GsArgs& a, int nk, cudaStream_t s) {
+  k_mgs<<<nk, kGsThreads, 0, s>>>(a.u, a.kstride, a.nb, NG, a.weight, 1, a.flag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_block_orth(int NG, double2* x, int kstride, int m, double weight, int nk,
+                              int* flag, cudaStream_t s) {
+  k_mgs<<<nk, kGsThreads, 0, s>>>(x, kstride, m, NG, weight, 2, flag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_project(int NG, const double2* x, const double2* y, int kstride, int m,
+                           double weight, double2* M, int nk, cudaStream_t s) {
+  const int total = nk * m * m;
+  const int warps_per_block = 8;
+  k_project<<<(total + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0, s>>>(
+      x, y, kstride, m, NG, weight, M, total);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_jacobi(const double2* M, int m, double* evals, double2* evecs, int nk,
+                          int* flag, cudaStream_t s) {
+  if (m > kJacMax) return cudaErrorInvalidValue;
+  const size_t smem = sizeof(double2) * 2 * (size_t)m * m;
+  k_jacobi<<<nk, 128, smem, s>>>(M, m, evals, evecs, flag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rotate(int NG, const double2* x, int xkstride, int m, const double2* C,
+                          int nout, double2* out, int okstride, int nk, cudaStream_t s) {
+  const size_t total = (size_t)nk * nout * NG;
+  k_rotate<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(x, xkstride, m, C, nout, out, okstride,
+                                                           NG, nk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_eps(int NG, const double2* u, const double2* hu, int kstride, int nb, double w,
+                       double* eps, double* err, int nk, cudaStream_t s) {
+  const int total = nk * nb;
+  k_eps<<<(total + 7) / 8, 256, 0, s>>>(u, hu, kstride, nb, NG, w, eps, err, total);
+  return cudaGetLastError();
+}
+
+}  // namespace mattohf

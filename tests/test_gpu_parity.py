@@ -1,0 +1,243 @@
+"""CUDA path vs the oracle, through the C ABI (needs a GB300).
+
+Tolerances (all complex128 / FP64):
+  * tables, single operator applications: max|gpu-ref| <= 1e-12 * max|ref|
+  * RK4 series over a few steps: relative 1e-10 (the benchmark spec's bound)
+  * ground state: gauge-invariant quantities only (energies, Ritz values)
+"""
+from __future__ import annotations
+
+import dataclasses
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import to_oracle_config
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+TOL_OP = 1e-12
+TOL_RT = 1e-10
+
+
+def rel(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def make_cfg(**kw):
+    from mattohf_gb300 import RunConfig
+    base = dict(acell=10.0, NG=32, NK=4, NB=2, NBocc=2, Zeff=[2.0], alpha=[1.0], Rion=[0.5],
+                Kion=[1])
+    base.update(kw)
+    return RunConfig(**base)
+
+
+CONFIGS = {
+    "ng16_nk3_unocc": make_cfg(NG=16, NK=3, NB=3, NBocc=1, acell=8.0, Zeff=[1.5, 0.5],
+                               alpha=[1.0, 0.7], Rion=[0.25, 0.75], Kion=[1, 2]),
+    "ng32_nk4": make_cfg(),
+    "ng64_nk8": make_cfg(NG=64, NK=8),
+    "ng128_nk4_nb3": make_cfg(NG=128, NK=4, NB=3, NBocc=2),
+    "ng256_nk2": make_cfg(NG=256, NK=2, NB=2, NBocc=2),
+    "ng512_nk2": make_cfg(NG=512, NK=2, NB=2, NBocc=1),
+}
+
+_cache = {}
+
+
+def setup(name):
+    if name in _cache:
+        return _cache[name]
+    from mattohf_gb300 import Context
+    from oracle import mattohf_oracle as O
+    cfg = CONFIGS[name]
+    ctx = Context(cfg)
+    S = O.make_system(to_oracle_config(cfg))
+    _cache[name] = (cfg, ctx, S)
+    return _cache[name]
+
+
+def rand_orbs(S, seed, nb=None):
+    rng = np.random.default_rng(seed)
+    shape = (S.NK, S.NB if nb is None else nb, S.NG)
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(built_lib):
+    yield
+    for _, ctx, _ in _cache.values():
+        ctx.close()
+    _cache.clear()
+
+
+@pytest.mark.parametrize("name", list(CONFIGS))
+def test_tables(name):
+    cfg, ctx, S = setup(name)
+    g = ctx.grids()
+    assert np.array_equal(g["Gx"], S.Gx)
+    assert np.array_equal(g["kx"], S.kx)
+    assert np.array_equal(g["rx"], S.rx)
+    assert rel(ctx.vion, S.vion) <= 1e-14
+    vCG, vCq = ctx.coulomb()
+    assert rel(vCG, S.vCG) <= TOL_OP
+    NK = S.NK
+    for kr in range(NK):
+        for kc in range(NK):
+            assert rel(vCq[kr - kc + NK - 1], S.vCGkk[kr * NK + kc]) <= TOL_OP
+
+
+@pytest.mark.parametrize("name", list(CONFIGS))
+def test_hpsi(name):
+    from oracle import mattohf_oracle as O
+    cfg, ctx, S = setup(name)
+    u = O.gram_schmidt(S, rand_orbs(S, 1))
+    w = rand_orbs(S, 2)
+    for A in (0.0, 0.3):
+        ref = O.ubkwbk_hwbk(S, u, w, A)
+        got = ctx.ubkwbk_hwbk(u, w, A)
+        assert rel(got, ref) <= TOL_OP, (A, rel(got, ref))
+
+
+@pytest.mark.parametrize("name", ["ng16_nk3_unocc", "ng64_nk8", "ng256_nk2"])
+def test_fock_kinetic_density(name):
+    from oracle import mattohf_oracle as O
+    cfg, ctx, S = setup(name)
+    u = rand_orbs(S, 3)
+    w = rand_orbs(S, 4, nb=S.NB + 1)  # a Krylov-like block with another band count
+    assert rel(ctx.ubkwbk_vFwbk(u, w), O.ubkwbk_vFwbk(S, u, w)) <= TOL_OP
+    assert rel(ctx.ubk_tubk(w, -0.2), O.ubk_tubk(S, w, -0.2)) <= TOL_OP
+    assert rel(ctx.ubk_dns(u), O.ubk_dns(S, u)) <= 1e-14
+    assert rel(ctx.dns_vH_of(u), O.dns_vH(S, O.ubk_dns(S, u))) <= TOL_OP
+
+
+@pytest.mark.parametrize("name", ["ng16_nk3_unocc", "ng32_nk4", "ng128_nk4_nb3"])
+def test_observables(name):
+    from oracle import mattohf_oracle as O
+    cfg, ctx, S = setup(name)
+    u = O.gram_schmidt(S, rand_orbs(S, 5))
+    ctx.set_orbitals(u)
+    for A in (0.0, 0.11):
+        ob = ctx.observables(A)
+        ec = O.ubk_Ecomps(S, u, A)
+        for i, key in enumerate(("Ekin", "Eion", "EH", "Exc")):
+            assert abs(ob[key] - ec[i]) <= 1e-12 * max(1.0, abs(ec[i])), key
+        assert abs(ob["Etot"] - ec.sum()) <= 1e-12 * abs(ec.sum())
+        assert abs(ob["Je"] - O.ubk_Je(S, u, A)) <= 1e-12
+        assert abs(ob["Nele"] - 2.0 * S.NBocc) <= 1e-12
+
+
+@pytest.mark.parametrize("name", ["ng32_nk4", "ng64_nk8", "ng16_nk3_unocc"])
+def test_rk4_run(name):
+    from oracle import mattohf_oracle as O
+    from mattohf_gb300 import define_afield
+    cfg, ctx, S = setup(name)
+    cfg = dataclasses.replace(cfg, dt=0.004, NT=5, field_option="LP", omegac=1.55, Tpulse=0.1, E0=20.0)
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    _, A, Aave, _ = define_afield(cfg)
+    ctx.set_orbitals(u0)
+    E, J, N = ctx.rk4_run(A, Aave, cfg.dt)
+    S.cfg = to_oracle_config(cfg)
+    ref = O.rt_calculation(S, u0, nt=cfg.NT, A=A, Aave=Aave)
+    assert rel(E, ref.Etot) <= TOL_RT
+    assert rel(N, ref.Nele) <= TOL_RT
+    assert np.max(np.abs(J - ref.Jtot)) <= TOL_RT * max(1.0, np.max(np.abs(ref.Jtot)))
+    assert rel(ctx.get_orbitals(), ref.ubk) <= TOL_RT
+
+
+def test_rk4_step_matches_run():
+    """mattohf_rk4_step (host fields) == one step of mattohf_rk4_run (device fields)."""
+    from oracle import mattohf_oracle as O
+    cfg, ctx, S = setup("ng32_nk4")
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    ctx.set_orbitals(u0)
+    ctx.RT_RK4_ubk(0.01, 0.02, 0.005)
+    a = ctx.get_orbitals()
+    ctx.set_orbitals(u0)
+    ctx.rk4_run(np.array([0.02]), np.array([0.01]), 0.005)
+    b = ctx.get_orbitals()
+    assert np.array_equal(a, b)
+    ref = O.rk4_step(S, u0, 0.01, 0.02, 0.005)
+    assert rel(a, ref) <= TOL_OP
+
+
+def test_graph_equals_eager():
+    """The graph-replayed RT loop is bitwise identical to eager launches."""
+    from oracle import mattohf_oracle as O
+    from mattohf_gb300 import _capi
+    cfg, ctx, S = setup("ng64_nk8")
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    A = np.linspace(0.0, 0.05, 4)
+    Aave = np.concatenate([[A[0] / 2], 0.5 * (A[1:] + A[:-1])])
+    ctx.set_orbitals(u0)
+    r1 = ctx.rk4_run(A, Aave, 0.005)
+    u1 = ctx.get_orbitals()
+    ctx.set_option(_capi.OPT_GRAPH, 0)
+    ctx.set_orbitals(u0)
+    r2 = ctx.rk4_run(A, Aave, 0.005)
+    u2 = ctx.get_orbitals()
+    ctx.set_option(_capi.OPT_GRAPH, 1)
+    assert np.array_equal(u1, u2)
+    for x, y in zip(r1, r2):
+        assert np.array_equal(x, y)
+
+
+def test_nonfinite_detected():
+    """An unstable dt overflows; the run returns ERR_NONFINITE naming the step."""
+    from oracle import mattohf_oracle as O
+    from mattohf_gb300 import MattohfError, _capi
+    cfg, ctx, S = setup("ng64_nk8")
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    ctx.set_orbitals(u0)
+    nt = 600
+    A = np.zeros(nt)
+    with pytest.raises(MattohfError) as ei:
+        ctx.rk4_run(A, A, 0.5)   # eps_max*dt ~ 100 >> 2.83
+    assert ei.value.status == _capi.ERR_NONFINITE
+    assert "step" in str(ei.value)
+
+
+@pytest.mark.parametrize("name", ["ng32_nk4", "ng16_nk3_unocc"])
+def test_gs_gauge_invariants(name):
+    from oracle import mattohf_oracle as O
+    cfg, ctx, S = setup(name)
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    nscf, ncg = 4, 2 if S.NB == 3 else 4
+    S.cfg = dataclasses.replace(S.cfg, NCG=ncg)
+    ref = O.gs_calculation(S, u0, nscf=nscf)
+    ctx.set_orbitals(u0)
+    got = ctx.GS_calculation(nscf, ncg)
+    assert np.max(np.abs(got["Etot"] - ref.Etot)) <= 1e-9 * np.max(np.abs(ref.Etot))
+    assert np.max(np.abs(got["epsbk"] - ref.epsbk)) <= 1e-8 * np.max(np.abs(ref.epsbk))
+    assert np.max(np.abs(got["Je"] - ref.Je)) <= 1e-9
+    # density is gauge invariant
+    assert rel(ctx.ubk_dns(ctx.get_orbitals()), O.ubk_dns(S, ref.ubk)) <= 1e-8
+
+
+@pytest.mark.parametrize("case", ["hf_ng32_nk4", "hf_ng16_nk3_unocc"])
+def test_golden(case):
+    """GPU path against the committed oracle fixtures."""
+    from mattohf_gb300 import Context, RunConfig
+    g = np.load(os.path.join(GOLD, case + ".npz"))
+    with open(os.path.join(GOLD, case + ".json")) as fh:
+        d = json.load(fh)
+    cfg = RunConfig(**{f.name: d[f.name] for f in dataclasses.fields(RunConfig)})
+    with Context(cfg) as ctx:
+        A = float(g["A"])
+        assert rel(ctx.ubkwbk_hwbk(g["u"], g["w"], A), g["hw"]) <= TOL_OP
+        assert rel(ctx.ubkwbk_vFwbk(g["u"], g["w"]), g["vF"]) <= TOL_OP
+        ctx.set_orbitals(g["u"])
+        ob = ctx.observables(A)
+        assert abs(ob["Etot"] - g["Ecomps"].sum()) <= 1e-12 * abs(g["Ecomps"].sum())
+        from mattohf_gb300 import aave_from_samples
+        A_t = g["rt_A"]
+        E, J, N = ctx.rk4_run(A_t, aave_from_samples(A_t), cfg.dt)
+        assert rel(E, g["rt_Etot"]) <= TOL_RT
+        assert np.max(np.abs(J - g["rt_Jtot"])) <= TOL_RT
+        assert rel(ctx.get_orbitals(), g["rt_u"]) <= TOL_RT

@@ -1,0 +1,178 @@
+"""Oracle self-checks on CPU: golden fixtures, physics known answers, the C port.
+
+The reference ships no tests or golden vectors (parity unpinned), so the
+oracle is pinned by known answers of the physics it restates.
+"""
+from __future__ import annotations
+
+import dataclasses
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import mattohf_oracle as O
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def small(**kw):
+    base = dict(acell=10.0, NG=32, NK=4, NB=2, NBocc=2, Zeff=[2.0], alpha=[1.0], Rion=[0.5], Kion=[1])
+    base.update(kw)
+    return O.Config(**base)
+
+
+def rand(S, seed, nb=None):
+    rng = np.random.default_rng(seed)
+    sh = (S.NK, S.NB if nb is None else nb, S.NG)
+    return rng.standard_normal(sh) + 1j * rng.standard_normal(sh)
+
+
+@pytest.mark.parametrize("case", ["hf_ng32_nk4", "hf_ng16_nk3_unocc"])
+def test_oracle_reproduces_golden(case):
+    g = np.load(os.path.join(GOLD, case + ".npz"))
+    with open(os.path.join(GOLD, case + ".json")) as fh:
+        cfg = O.Config(**json.load(fh))
+    S = O.make_system(cfg)
+    np.testing.assert_allclose(S.vCGkk, g["vCGkk"], rtol=0, atol=1e-14 * np.abs(g["vCGkk"]).max())
+    hw = O.ubkwbk_hwbk(S, g["u"], g["w"], float(g["A"]))
+    assert np.max(np.abs(hw - g["hw"])) <= 1e-13 * np.max(np.abs(g["hw"]))
+    rt = O.rt_calculation(S, g["u"], nt=cfg.NT)
+    assert np.max(np.abs(rt.Etot - g["rt_Etot"])) <= 1e-12 * np.max(np.abs(g["rt_Etot"]))
+
+
+def test_free_particle_eigenvalues():
+    """No ions, no e-e: h = 1/2 (G+k+A)^2, plane waves are eigenvectors."""
+    cfg = small(functional="none", Zeff=[0.0])
+    S = O.make_system(cfg)
+    S.vCG[:] = 0.0
+    u = np.zeros((S.NK, S.NB, S.NG), dtype=np.complex128)
+    for ik in range(S.NK):
+        for ib, g in enumerate([0, 3]):
+            u[ik, ib] = np.exp(1j * S.Gx[g] * S.rx)
+    A = 0.07
+    h = O.ubkwbk_hwbk(S, u, u, A)
+    for ik in range(S.NK):
+        for ib, g in enumerate([0, 3]):
+            lam = 0.5 * (S.Gx[g] + S.kx[ik] + A) ** 2
+            assert np.max(np.abs(h[ik, ib] - lam * u[ik, ib])) < 1e-12
+
+
+def test_hermiticity():
+    S = O.make_system(small())
+    u = O.gram_schmidt(S, rand(S, 1))
+    a, b = rand(S, 2), rand(S, 3)
+    ha, hb = O.ubkwbk_hwbk(S, u, a, 0.2), O.ubkwbk_hwbk(S, u, b, 0.2)
+    assert abs(np.vdot(a, hb) - np.conj(np.vdot(b, ha))) < 1e-11 * abs(np.vdot(a, hb))
+
+
+def test_particle_number():
+    S = O.make_system(small(NB=3, NBocc=2))
+    u = O.gram_schmidt(S, rand(S, 4))
+    assert abs(O.ubk_dns(S, u).sum() * S.dvcell - 2 * S.NBocc) < 1e-12
+
+
+def test_soft_coulomb_transform_limit():
+    """2 int_0^L cos(qx)/sqrt(x^2+1) dx -> 2 K0(|q|) as L = NK*a grows."""
+    from scipy.special import k0
+    L = 64 * 10.0
+    for q in (0.5, 1.3, 2.7):
+        v = O.k_vCk_fast(q, 10.0, 64, 64)[0]
+        # the truncated tail of int cos(qx)/x oscillates with amplitude ~ 1/(q L)
+        assert abs(v - 2.0 * k0(q)) < 1.5 / (q * L)
+
+
+def test_k_vck_orders_agree():
+    ks = np.array([0.0, 0.3, 1.7, 5.5])
+    a = O.k_vCk(ks, 7.0, 16, 3)
+    b = O.k_vCk_fast(ks, 7.0, 16, 3)
+    assert np.max(np.abs(a - b)) < 1e-12 * np.max(np.abs(a))
+
+
+def test_gauge_uniform_A_is_k_shift():
+    """A uniform A enters the kinetic term as k -> k + A; the Fock term depends on k-k' only."""
+    S = O.make_system(small())
+    u = rand(S, 5)
+    A = 0.031
+    t1 = O.ubk_tubk(S, u, A)
+    S2 = O.make_system(small())
+    S2.kx = S.kx + A
+    t2 = O.ubk_tubk(S2, u, 0.0)
+    assert np.max(np.abs(t1 - t2)) < 1e-12 * np.max(np.abs(t1))
+
+
+def test_rk4_fourth_order():
+    """Global error of RK4 scales as dt^4 at stable dt."""
+    cfg = small(NG=16, NK=2, acell=6.0)
+    S = O.make_system(cfg)
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    T = 0.04
+
+    def run(n):
+        u = u0.copy()
+        dt = T / n
+        for _ in range(n):
+            u = O.rk4_step(S, u, 0.01, 0.01, dt)
+        return u
+
+    ref = run(64)
+    e1 = np.max(np.abs(run(4) - ref))
+    e2 = np.max(np.abs(run(8) - ref))
+    assert 10.0 < e1 / e2 < 24.0   # ~16 for a 4th-order method
+
+
+def test_energy_conserved_without_field():
+    cfg = small(NG=16, NK=2, acell=6.0, dt=0.002, NT=20, field_option="LR", dAc=0.0)
+    S = O.make_system(cfg)
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    rt = O.rt_calculation(S, u0)
+    assert np.max(np.abs(rt.Etot - rt.Etot0)) < 1e-7 * abs(rt.Etot0)
+
+
+def test_current_is_minus_dipole_rate():
+    """Je is the time derivative of -P; the dipole extension integrates it."""
+    t = np.linspace(0, 1, 11)
+    J = np.sin(t)
+    P = O.dipole_from_current(t, J[1:], J[0], t[1] - t[0])
+    assert abs(P[-1] - (-(1 - math.cos(1.0)))) < 1e-2
+
+
+def test_c_port_matches_numpy_oracle():
+    from oracle import build_cref
+    import ctypes as C
+    lib = build_cref.load()
+    cfg = small(NG=32, NK=4, NB=3, NBocc=2)
+    S = O.make_system(cfg)
+    D = C.POINTER(C.c_double)
+    h = lib.cref_create(cfg.NG, cfg.NK, cfg.NB, cfg.NBocc, cfg.acell, 1,
+                        S.vion.ctypes.data_as(D), None, None)
+    try:
+        vCG = np.empty(cfg.NG)
+        vCq = np.empty((2 * cfg.NK - 1, cfg.NG))
+        lib.cref_get_tables(h, vCG.ctypes.data_as(D), vCq.ctypes.data_as(D))
+        assert np.max(np.abs(vCG - S.vCG)) < 1e-13
+        u = O.gram_schmidt(S, rand(S, 6))
+        w = rand(S, 7)
+        hw = np.empty_like(w)
+        lib.cref_hpsi(h, u.view(np.float64).ctypes.data_as(D), w.view(np.float64).ctypes.data_as(D),
+                      cfg.NB, C.c_double(0.2), hw.view(np.float64).ctypes.data_as(D))
+        ref = O.ubkwbk_hwbk(S, u, w, 0.2)
+        assert np.max(np.abs(hw - ref)) < 1e-12 * np.max(np.abs(ref))
+        nt = 3
+        A = np.array([0.01, 0.02, 0.03])
+        Aave = np.array([0.005, 0.015, 0.025])
+        uu = u.copy()
+        E, J, N = np.empty(nt), np.empty(nt), np.empty(nt)
+        lib.cref_rk4_run(h, uu.view(np.float64).ctypes.data_as(D), nt, C.c_double(0.004),
+                         A.ctypes.data_as(D), Aave.ctypes.data_as(D), E.ctypes.data_as(D),
+                         J.ctypes.data_as(D), N.ctypes.data_as(D))
+        cfg2 = dataclasses.replace(cfg, dt=0.004)
+        S.cfg = cfg2
+        rt = O.rt_calculation(S, u, nt=nt, A=A, Aave=Aave)
+        assert np.max(np.abs(E - rt.Etot)) < 1e-11 * np.max(np.abs(rt.Etot))
+        assert np.max(np.abs(J - rt.Jtot)) < 1e-11
+        assert np.max(np.abs(uu - rt.ubk)) < 1e-11
+    finally:
+        lib.cref_destroy(h)
