@@ -139,6 +139,11 @@ int mattohf_eps(mattohf_ctx* ctx, double* epsbk, double* epserrorbk);
 
 int mattohf_synchronize(mattohf_ctx* ctx);
 
+/* Diagnostic (no reference counterpart): measured FP64 FMA throughput of
+ * `device` in TFLOP/s (2 flops per DFMA), the roofline denominator of the
+ * FP64-bound kernels. */
+int mattohf_diag_fp64_peak(int device, double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

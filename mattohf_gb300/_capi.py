@@ -34,7 +34,7 @@ EXPORTS = [
     "mattohf_gram_schmidt", "mattohf_hpsi", "mattohf_hpsi_device", "mattohf_fock",
     "mattohf_kinetic", "mattohf_density", "mattohf_observables", "mattohf_rk4_step",
     "mattohf_rk4_run", "mattohf_last_run_timing", "mattohf_gs_run", "mattohf_eps",
-    "mattohf_synchronize",
+    "mattohf_synchronize", "mattohf_diag_fp64_peak",
 ]
 
 
@@ -89,6 +89,7 @@ def load(path: str = LIB_PATH):
         "mattohf_gs_run": ([P, I, I, D, D, D, D, D], I),
         "mattohf_eps": ([P, D, D], I),
         "mattohf_synchronize": ([P], I),
+        "mattohf_diag_fp64_peak": ([I, D], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -30,9 +30,19 @@ __global__ void k_twiddles(double2* tw, int n) {
   }
 }
 
-__global__ void k_zero_int(int* p, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) p[i] = 0;
+// FP64 FMA throughput probe: 8 independent dependency chains per thread.
+__global__ void k_dfma_probe(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+      x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+  }
+  const double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == -12345.0) out[0] = s;
 }
 
 }  // namespace
@@ -937,6 +947,33 @@ int mattohf_gs_run(mattohf_ctx* ctx, int nscf, int ncg, double* Etot_iter, doubl
   CKR(sync_and_flag(ctx));
   if (flag) return fail(ctx, MATTOHF_ERR_NOTCONV, flag == 2 ? "Jacobi eigensolver did not converge"
                                                              : "orthonormalisation met a zero column");
+  return MATTOHF_OK;
+}
+
+int mattohf_diag_fp64_peak(int device, double* tflops) {
+  if (!tflops) return MATTOHF_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return MATTOHF_ERR_CUDA;
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return MATTOHF_ERR_CUDA;
+  double* d = nullptr;
+  if (cudaMalloc(&d, sizeof(double)) != cudaSuccess) return MATTOHF_ERR_ALLOC;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = nsm * 8, threads = 256, iters = 200;
+  k_dfma_probe<<<blocks, threads>>>(d, iters, 1.0000001, 1e-9);
+  cudaEventRecord(e0);
+  k_dfma_probe<<<blocks, threads>>>(d, iters, 1.0000001, 1e-9);
+  cudaEventRecord(e1);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  if (e != cudaSuccess || ms <= 0) return MATTOHF_ERR_CUDA;
+  const double fmas = (double)blocks * threads * iters * 16 * 8;
+  *tflops = 2.0 * fmas / (ms * 1e-3) / 1e12;
   return MATTOHF_OK;
 }
 
