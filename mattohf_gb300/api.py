@@ -139,8 +139,9 @@ class Context:
 
     # -- operator kernels (src/Functions.f90) -----------------------------------
     def ubkwbk_hwbk(self, ubk, wbk, A: float) -> np.ndarray:
+        """h[ubk](A) wbk; passing the same array twice applies h[u] u (symmetric exchange)."""
         u = _c128(ubk, self.shape)
-        w = np.ascontiguousarray(wbk, dtype=np.complex128)
+        w = u if wbk is ubk else np.ascontiguousarray(wbk, dtype=np.complex128)
         nbw = w.shape[1]
         _c128(w, (self.NK, nbw, self.NG))
         out = np.empty_like(w)
@@ -150,7 +151,7 @@ class Context:
 
     def ubkwbk_vFwbk(self, ubk, wbk) -> np.ndarray:
         u = _c128(ubk, self.shape)
-        w = np.ascontiguousarray(wbk, dtype=np.complex128)
+        w = u if wbk is ubk else np.ascontiguousarray(wbk, dtype=np.complex128)
         nbw = w.shape[1]
         out = np.empty_like(w)
         self._check(self.lib.mattohf_fock(self.h, _dp(u.view(np.float64)), _dp(w.view(np.float64)),

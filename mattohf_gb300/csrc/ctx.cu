@@ -68,6 +68,8 @@ struct mattohf_ctx {
   size_t scratch_cap = 0;
   double* d_colbuf = nullptr;
   size_t colbuf_cap = 0;
+  double2* d_sym = nullptr;   // symmetric-exchange partials
+  size_t sym_cap = 0;
   int* d_int = nullptr;  // [0] = step counter, [1] = non-finite flag, [2] = solver flag
   // RT series
   double *d_A = nullptr, *d_Aave = nullptr, *d_sE = nullptr, *d_sJ = nullptr, *d_sN = nullptr;
@@ -202,43 +204,106 @@ int enq_density(mattohf_ctx* ctx, Block u) {
   return MATTOHF_OK;
 }
 
-int enq_fock(mattohf_ctx* ctx, Block u, Block w, int* nchunks_out) {
-  const int ncols = ctx->NK * w.nb;
+// Which exchange partials a combine launch reads.
+struct FockPlan {
+  int nchunks = 1;            // chunked partials per column (bands >= b0)
+  int b0 = 0;                 // first band served by the chunked partials
+  const double2* sym = nullptr;
+  int S = 0, T = 0;
+  bool any = false;           // exchange present at all
+};
+
+int ensure_sym(mattohf_ctx* ctx, size_t need) {
+  if (need <= ctx->sym_cap) return MATTOHF_OK;
+  if (ctx->capturing) return fail(ctx, MATTOHF_ERR_STATE, "sym scratch growth during capture");
+  destroy_graph(ctx);
+  CKR(dalloc(ctx, &ctx->d_sym, need));
+  ctx->sym_cap = need;
+  return MATTOHF_OK;
+}
+
+int timed_begin(mattohf_ctx* ctx) {
+  if (!(ctx->opt_timing && !ctx->capturing)) return MATTOHF_OK;
+  if (ctx->fock_event_used == ctx->fock_events.size()) {
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    ctx->fock_events.push_back({e0, e1});
+  }
+  CK(cudaEventRecord(ctx->fock_events[ctx->fock_event_used].first, ctx->st));
+  return MATTOHF_OK;
+}
+
+int timed_end(mattohf_ctx* ctx) {
+  if (!(ctx->opt_timing && !ctx->capturing)) return MATTOHF_OK;
+  CK(cudaEventRecord(ctx->fock_events[ctx->fock_event_used].second, ctx->st));
+  ctx->fock_event_used++;
+  return MATTOHF_OK;
+}
+
+// Exchange partials of h[u] w.  When w is u itself (all RK4 stages, Ex,
+// Subspace_diag, eps) the occupied rows use the symmetric pair kernel and only
+// the unoccupied rows (if any) take the chunked kernel.
+int enq_fock(mattohf_ctx* ctx, Block u, Block w, FockPlan* plan) {
+  *plan = FockPlan();
+  plan->any = true;
+  const bool same = (w.p == u.p) && (w.kstride == u.kstride) && (w.nb == u.nb);
+  const int NG = ctx->NG;
+  if (same && ctx->opt_sym) {
+    const int S = fock_sym_teams(NG);
+    const int M = ctx->NK * ctx->NBocc;
+    const int T = (M + S - 1) / S;
+    CKR(ensure_sym(ctx, (size_t)T * (T + 1) / 2 * 2 * S * NG));
+    FockSymArgs a;
+    a.u = u;
+    a.nk = ctx->NK;
+    a.nbocc = ctx->NBocc;
+    a.S = S;
+    a.T = T;
+    a.kern = ctx->d_kern;
+    a.tw = ctx->tw;
+    a.scratch = ctx->d_sym;
+    CKR(timed_begin(ctx));
+    CK(launch_fock_sym(NG, a, ctx->st));
+    CKR(timed_end(ctx));
+    plan->sym = ctx->d_sym;
+    plan->S = S;
+    plan->T = T;
+    plan->b0 = ctx->NBocc;
+    if (w.nb == ctx->NBocc) return MATTOHF_OK;
+  }
+  Block wr = w;
+  wr.p = w.p + (size_t)plan->b0 * NG;
+  wr.nb = w.nb - plan->b0;
+  const int ncols = ctx->NK * wr.nb;
   CKR(ensure_scratch(ctx, ncols));
   FockArgs a;
   a.u = u;
-  a.w = w;
+  a.w = wr;
   a.nk = ctx->NK;
   a.nbocc = ctx->NBocc;
   a.kern = ctx->d_kern;
   a.tw = ctx->tw;
   a.scratch = ctx->d_scratch;
   fock_split(ctx, ncols, &a.nchunks, &a.chunk);
-  *nchunks_out = a.nchunks;
-  const bool timed = ctx->opt_timing && !ctx->capturing;
-  if (timed) {
-    if (ctx->fock_event_used == ctx->fock_events.size()) {
-      cudaEvent_t e0, e1;
-      CK(cudaEventCreate(&e0));
-      CK(cudaEventCreate(&e1));
-      ctx->fock_events.push_back({e0, e1});
-    }
-    CK(cudaEventRecord(ctx->fock_events[ctx->fock_event_used].first, ctx->st));
-  }
+  plan->nchunks = a.nchunks;
+  CKR(timed_begin(ctx));
   CK(launch_fock(ctx->NG, a, ncols, ctx->st));
-  if (timed) {
-    CK(cudaEventRecord(ctx->fock_events[ctx->fock_event_used].second, ctx->st));
-    ctx->fock_event_used++;
-  }
+  CKR(timed_end(ctx));
   return MATTOHF_OK;
 }
 
-CombineArgs combine_base(mattohf_ctx* ctx, Block w, AField af, int mode, int nchunks) {
+CombineArgs combine_base(mattohf_ctx* ctx, Block w, AField af, int mode, const FockPlan& fp) {
   CombineArgs a;
   std::memset(&a, 0, sizeof(a));
   a.w = w;
-  a.scratch = (ctx->hf && mode != CM_T) ? ctx->d_scratch : nullptr;
-  a.nchunks = nchunks;
+  const bool ex = ctx->hf && mode != CM_T && fp.any;
+  a.scratch = ex ? ctx->d_scratch : nullptr;
+  a.sym = ex ? fp.sym : nullptr;
+  a.sym_S = fp.S;
+  a.sym_T = fp.T;
+  a.chunk_b0 = fp.b0;
+  a.nchunks = fp.nchunks;
   a.vloc = ctx->d_vloc;
   a.Gx = ctx->d_Gx;
   a.kx = ctx->d_kx;
@@ -257,14 +322,15 @@ CombineArgs combine_base(mattohf_ctx* ctx, Block w, AField af, int mode, int nch
 
 // h[u] w -> out  (mode CM_H), or the exchange / kinetic term alone.
 int enq_hpsi(mattohf_ctx* ctx, Block u, Block w, BlockOut out, AField af, int mode) {
-  int nch = 1;
+  FockPlan fp;
   if (mode == CM_H) CKR(enq_density(ctx, u));
-  if (ctx->hf && mode != CM_T) CKR(enq_fock(ctx, u, w, &nch));
+  if (ctx->hf && mode != CM_T) CKR(enq_fock(ctx, u, w, &fp));
   else if (mode == CM_F) {
     CK(cudaMemsetAsync(out.p, 0, sizeof(double2) * (size_t)ctx->NK * out.kstride, ctx->st));
     return MATTOHF_OK;
   }
-  CombineArgs a = combine_base(ctx, w, af, mode, nch);
+  CKR(ensure_scratch(ctx, ctx->NK * w.nb));
+  CombineArgs a = combine_base(ctx, w, af, mode, fp);
   a.out = out;
   CK(launch_combine(ctx->NG, a, ctx->NK * w.nb, ctx->st));
   return MATTOHF_OK;
@@ -287,14 +353,20 @@ BlockOut blko(double2* p, int ld, int NG, int nb) {
 
 // Observables of `u` at field af (RT:43-47): density scalars, Fock partials,
 // per-column Ekin/Je/<u|F u>, then the ordered reduction.
-int enq_observables(mattohf_ctx* ctx, const double2* u, AField af, bool advance) {
+// With `defer_ex` the exchange energy is left out of Etot (and no Fock apply
+// is made); the next RK4 step's first stage, which applies the exchange
+// operator of the same orbitals, adds it (k_ex_finalize).
+int enq_observables(mattohf_ctx* ctx, const double2* u, AField af, bool advance, bool defer_ex,
+                    FockPlan* plan_out = nullptr) {
   const int NG = ctx->NG, NB = ctx->NB;
   Block ub = blk(u, NB, NG, NB);
   CKR(enq_density(ctx, ub));
-  int nch = 1;
-  if (ctx->hf) CKR(enq_fock(ctx, ub, ub, &nch));
-  else CKR(ensure_scratch(ctx, ctx->NK * NB));
-  CombineArgs a = combine_base(ctx, ub, af, CM_OBS, nch);
+  FockPlan fp;
+  fp.any = false;
+  if (ctx->hf && !defer_ex) CKR(enq_fock(ctx, ub, ub, &fp));
+  CKR(ensure_scratch(ctx, ctx->NK * NB));
+  if (plan_out) *plan_out = fp;
+  CombineArgs a = combine_base(ctx, ub, af, CM_OBS, fp);
   CK(launch_combine(NG, a, ctx->NK * NB, ctx->st));
   ObsReduceArgs r;
   r.colbuf = ctx->d_colbuf;
@@ -307,6 +379,7 @@ int enq_observables(mattohf_ctx* ctx, const double2* u, AField af, bool advance)
   r.vcell = ctx->vcell;
   r.NGd = (double)NG;
   r.hf = ctx->hf;
+  r.defer_ex = defer_ex ? 1 : 0;
   r.out = ctx->d_out;
   r.series_E = advance ? ctx->d_sE : nullptr;
   r.series_J = advance ? ctx->d_sJ : nullptr;
@@ -320,20 +393,43 @@ int enq_observables(mattohf_ctx* ctx, const double2* u, AField af, bool advance)
 
 // One RK4 step (RT:165-170); fields either from host values or from the
 // device series indexed by the device step counter.
-int enq_rk4(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt) {
+ExArgs ex_args(mattohf_ctx* ctx, double* series, int idx, double* out) {
+  ExArgs e;
+  e.colbuf = ctx->d_colbuf;
+  e.nk = ctx->NK;
+  e.nb = ctx->NB;
+  e.nbocc = ctx->NBocc;
+  e.occ = ctx->occ;
+  e.dvcell = ctx->dvcell;
+  e.series_E = series;
+  e.it = ctx->d_int;
+  e.idx = idx;
+  e.out = out;
+  return e;
+}
+
+// One RK4 step (RT:165-170); fields either from host values or from the
+// device series indexed by the device step counter.  With `ex_series` the
+// first stage also completes Etot(it-1) with the exchange energy of the
+// step's input orbitals (the same exchange operator the stage applies).
+int enq_rk4(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt,
+            double* ex_series = nullptr) {
   const int NG = ctx->NG, NB = ctx->NB;
   const int modes[4] = {CM_RK0, CM_RK1, CM_RK2, CM_RK3};
   const AField fs[4] = {f_m, f_ave, f_ave, f_cur};
+  CKR(ensure_scratch(ctx, ctx->NK * NB));
   for (int s = 0; s < 4; ++s) {
     const double2* in = (s == 0) ? ctx->d_u : ctx->d_us;
     Block ub = blk(in, NB, NG, NB);
     CKR(enq_density(ctx, ub));
-    int nch = 1;
-    if (ctx->hf) CKR(enq_fock(ctx, ub, ub, &nch));
-    CombineArgs a = combine_base(ctx, ub, fs[s], modes[s], nch);
+    FockPlan fp;
+    if (ctx->hf) CKR(enq_fock(ctx, ub, ub, &fp));
+    CombineArgs a = combine_base(ctx, ub, fs[s], modes[s], fp);
     a.out = blko(ctx->d_us, NB, NG, NB);
     a.dt = dt;
+    a.ex_cols = (s == 0 && ex_series != nullptr && ctx->hf) ? 1 : 0;
     CK(launch_combine(NG, a, ctx->NK * NB, ctx->st));
+    if (a.ex_cols) CK(launch_ex_finalize(ex_args(ctx, ex_series, -1, nullptr), ctx->st));
   }
   return MATTOHF_OK;
 }
@@ -494,6 +590,8 @@ int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out) {
     if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
     e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
+    e = configure_kernels();
+    if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
   }
   const size_t nu = orb_elems(ctx, ctx->NB);
   if ((rc = dalloc(ctx, &ctx->tw, NG)) || (rc = dalloc(ctx, &ctx->d_Gx, NG)) ||
@@ -532,7 +630,7 @@ int mattohf_destroy(mattohf_ctx* ctx) {
                   ctx->d_k[1], ctx->d_k[2], ctx->d_k[3], ctx->d_a, ctx->d_b, ctx->d_c,
                   ctx->d_scratch, ctx->d_colbuf, ctx->d_int, ctx->d_A, ctx->d_Aave, ctx->d_sE,
                   ctx->d_sJ, ctx->d_sN, ctx->d_work, ctx->d_hwork, ctx->d_M, ctx->d_V, ctx->d_evals,
-                  ctx->d_eps, ctx->d_err};
+                  ctx->d_eps, ctx->d_err, ctx->d_sym};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -646,10 +744,15 @@ static int hpsi_host(mattohf_ctx* ctx, const double* ubk, const double* wbk, int
   const int NG = ctx->NG, NB = ctx->NB;
   const size_t nw = orb_elems(ctx, nbw), nu = orb_elems(ctx, NB);
   CKR(ensure_stage(ctx, std::max(nw, nu)));
+  // h[u] u (the same host array passed twice) keeps u and w in one device
+  // buffer, which selects the symmetric exchange kernel.
+  const bool same = (ubk == wbk) && nbw == NB;
   if (mode != CM_T)
     CK(cudaMemcpyAsync(ctx->d_a, ubk, sizeof(double2) * nu, cudaMemcpyHostToDevice, ctx->st));
-  CK(cudaMemcpyAsync(ctx->d_b, wbk, sizeof(double2) * nw, cudaMemcpyHostToDevice, ctx->st));
-  CKR(enq_hpsi(ctx, blk(ctx->d_a, NB, NG, NB), blk(ctx->d_b, nbw, NG, nbw),
+  if (!same)
+    CK(cudaMemcpyAsync(ctx->d_b, wbk, sizeof(double2) * nw, cudaMemcpyHostToDevice, ctx->st));
+  const double2* wd = same ? ctx->d_a : ctx->d_b;
+  CKR(enq_hpsi(ctx, blk(ctx->d_a, NB, NG, NB), blk(wd, nbw, NG, nbw),
                blko(ctx->d_c, nbw, NG, nbw), aval(A), mode));
   CK(cudaMemcpyAsync(out, ctx->d_c, sizeof(double2) * nw, cudaMemcpyDeviceToHost, ctx->st));
   return sync_and_flag(ctx);
@@ -701,7 +804,7 @@ int mattohf_density(mattohf_ctx* ctx, const double* ubk, double* dns, double* vH
 
 int mattohf_observables(mattohf_ctx* ctx, double A, double* Ecomps, double* Etot, double* Je, double* Nele) {
   CKR(check_ctx(ctx));
-  CKR(enq_observables(ctx, ctx->d_u, aval(A), false));
+  CKR(enq_observables(ctx, ctx->d_u, aval(A), false, false));
   double o[8];
   CK(cudaMemcpyAsync(o, ctx->d_out, sizeof(double) * 7, cudaMemcpyDeviceToHost, ctx->st));
   CKR(sync_and_flag(ctx));
@@ -752,8 +855,8 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
     cudaGraph_t g;
     ctx->capturing = true;
     CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
-    int rc = enq_rk4(ctx, fm, fave, fcur, dt);
-    if (rc == MATTOHF_OK) rc = enq_observables(ctx, ctx->d_u, fcur, true);
+    int rc = enq_rk4(ctx, fm, fave, fcur, dt, ctx->d_sE);
+    if (rc == MATTOHF_OK) rc = enq_observables(ctx, ctx->d_u, fcur, true, true);
     cudaError_t ec = cudaStreamEndCapture(ctx->st, &g);
     ctx->capturing = false;
     if (rc != MATTOHF_OK) return rc;
@@ -774,8 +877,8 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
     if (use_graph) {
       CK(cudaGraphLaunch(ctx->step_exec, ctx->st));
     } else {
-      CKR(enq_rk4(ctx, fm, fave, fcur, dt));
-      CKR(enq_observables(ctx, ctx->d_u, fcur, true));
+      CKR(enq_rk4(ctx, fm, fave, fcur, dt, ctx->d_sE));
+      CKR(enq_observables(ctx, ctx->d_u, fcur, true, true));
     }
     // bounded detection of a blow-up: poll the flag every 256 steps
     if ((it & 255) == 255 && it + 1 < nt) {
@@ -785,6 +888,17 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
         bad_at = it;
         break;
       }
+    }
+  }
+  {
+    // exchange energy of the last step's orbitals (the next stage-1 apply that
+    // would supply it does not happen)
+    const int last = bad_at >= 0 ? bad_at : nt - 1;
+    if (ctx->hf) {
+      FockPlan fp;
+      CKR(enq_observables(ctx, ctx->d_u, aval(0.0), false, false, &fp));
+      (void)fp;
+      CK(launch_ex_finalize(ex_args(ctx, ctx->d_sE, last, nullptr), ctx->st));
     }
   }
   CK(cudaEventRecord(e1, ctx->st));
@@ -885,7 +999,7 @@ int mattohf_gs_run(mattohf_ctx* ctx, int nscf, int ncg, double* Etot_iter, doubl
   std::vector<double> dprev(NG), dnew(NG);
   double o[8];
   // Etotscf(0) and dnsscf(:,1) (GS:26-27)
-  CKR(enq_observables(ctx, ctx->d_u, aval(0.0), false));
+  CKR(enq_observables(ctx, ctx->d_u, aval(0.0), false, false));
   CK(cudaMemcpyAsync(o, ctx->d_out, sizeof(double) * 7, cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaMemcpyAsync(dprev.data(), ctx->d_rho, sizeof(double) * NG, cudaMemcpyDeviceToHost, ctx->st));
   CKR(sync_and_flag(ctx));
@@ -917,12 +1031,10 @@ int mattohf_gs_run(mattohf_ctx* ctx, int nscf, int ncg, double* Etot_iter, doubl
     CKR(enq_rayleigh_ritz(ctx, ctx->d_work, ctx->d_hwork, NB, NB, ctx->d_u));
     // Etot, Je (GS:36-38); the Fock partials of h[u]u are then reused for the
     // Ritz values and residuals (GS:42-43), which apply the same operator.
-    CKR(enq_observables(ctx, ctx->d_u, aval(0.0), false));
+    FockPlan fp;
+    CKR(enq_observables(ctx, ctx->d_u, aval(0.0), false, false, &fp));
     {
-      int nch, ch;
-      fock_split(ctx, NK * NB, &nch, &ch);
-      if (!ctx->hf) nch = 1;
-      CombineArgs a = combine_base(ctx, ub, aval(0.0), CM_H, nch);
+      CombineArgs a = combine_base(ctx, ub, aval(0.0), CM_H, fp);
       a.out = blko(ctx->d_hwork, NB, NG, NB);
       CK(launch_combine(NG, a, NK * NB, ctx->st));
     }

@@ -68,6 +68,22 @@ struct FockArgs {
   int chunk;            // pairs per chunk
 };
 
+// Occupied-pair symmetric exchange (w == u): tiles of S occupied orbitals,
+// one CTA per tile pair (i <= j); partials [tp][2][S][NG] (rows, columns).
+struct FockSymArgs {
+  Block u;
+  int nk, nbocc;
+  int S;                // tile size = teams per CTA
+  int T;                // number of tiles = ceil(NK*nbocc / S)
+  const double* kern;
+  const double2* tw;
+  double2* scratch;
+};
+
+__host__ __device__ __forceinline__ int sym_tp(int i, int j, int T) {
+  return i * T - (i * (i - 1)) / 2 + (j - i);
+}
+
 enum CombineMode : int {
   CM_H = 0,     // out = T_A w + vloc w + F
   CM_RK0 = 1,   // k0 = -i h ; next = u0 + (0.5 dt) k0
@@ -81,6 +97,10 @@ enum CombineMode : int {
 
 struct CombineArgs {
   Block w;                  // columns being processed (the h-apply's wbk)
+  const double2* sym;       // symmetric-exchange partials for occupied columns (or null)
+  int sym_S, sym_T;
+  int chunk_b0;             // first band whose exchange comes from the chunked partials
+  int ex_cols;              // CM_RK0: also store <w|F> per occupied column (deferred Ex)
   BlockOut out;             // h output (CM_H / CM_F / CM_T) or stage input (CM_RK0..2)
   double2* u0;              // RK4 base state [NK][NB][NG] (CM_RK*)
   double2* kbuf[4];         // RK4 stage derivatives [NK][NB][NG]
@@ -106,6 +126,7 @@ struct ObsReduceArgs {
   int nk, nb, nbocc;
   double occ, dvcell, vcell, NGd;
   int hf;
+  int defer_ex;             // 1: Etot excludes Ex (added later by k_ex_finalize)
   double* out;              // [0]=Etot [1]=Ekin [2]=Eion [3]=EH [4]=Ex [5]=Je [6]=Nele
   double* series_E;         // per step (may be null)
   double* series_J;
@@ -118,6 +139,19 @@ struct ObsReduceArgs {
 // Launchers (defined in k_hpsi.cu); all return cudaGetLastError() of the launch.
 cudaError_t launch_density(int NG, const DensArgs& a, cudaStream_t s);
 cudaError_t launch_fock(int NG, const FockArgs& a, int ncols, cudaStream_t s);
+cudaError_t launch_fock_sym(int NG, const FockSymArgs& a, cudaStream_t s);
+int fock_sym_teams(int NG);  // S for this grid size
+cudaError_t configure_kernels();
+struct ExArgs {
+  const double* colbuf;
+  int nk, nb, nbocc;
+  double occ, dvcell;
+  double* series_E;   // Etot series; Ex added to entry it-1 (or `idx` when >= 0)
+  const int* it;
+  int idx;
+  double* out;        // optional: [0] += Ex, [4] = Ex
+};
+cudaError_t launch_ex_finalize(const ExArgs& a, cudaStream_t s);
 cudaError_t launch_combine(int NG, const CombineArgs& a, int ncols, cudaStream_t s);
 cudaError_t launch_obs_reduce(const ObsReduceArgs& a, cudaStream_t s);
 

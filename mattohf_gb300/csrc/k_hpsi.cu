@@ -148,6 +148,135 @@ __global__ void __launch_bounds__(kThreads) k_fock(FockArgs a) {
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Symmetric exchange for w == u over occupied pairs (same F:237-261 sum).
+//
+// For occupied orbitals a=(ka,ba), b=(kb,bb) the pair potentials obey
+//   phi_ba(x_m) = conj(phi_ab(x_m)) + (kern_ba[N/2] - kern_ab[N/2]) conj(R_ab[N/2]) (-1)^m
+// (the soft-Coulomb kernel is even; only the self-aliased Nyquist frequency
+// breaks the conjugate symmetry, R_ab being FFT(u_a conj(u_b))).  One pair of
+// transforms therefore yields both out(a) += phi_ab u_b and
+// out(b) += phi_ba u_a.  A CTA handles a tile pair (i <= j) of S orbitals:
+// team w owns row a = i*S + w (accumulated in registers) and in round r
+// visits b = j*S + (w + r) % S, so within a round every column accumulator
+// (shared memory) has exactly one writer.  Diagonal tiles visit each
+// unordered pair once (rounds 0..S/2).
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_fock_sym(FockSymArgs a) {
+  using TM = Team<N>;
+  constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
+  constexpr int S = (kThreads / 32) * PW;
+  extern __shared__ double2 sm[];
+  double2* tw_s = sm;                  // N
+  double2* bufs = sm + N;              // S * N  (team FFT buffers)
+  double2* cacc = bufs + S * N;        // S * N  (column accumulators)
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tl = lane % T, tw_ = warp * PW + lane / T;
+  const int team_lane0 = (lane / T) * T;
+  double2* buf = bufs + tw_ * N;
+  for (int i = tid; i < N; i += kThreads) tw_s[i] = a.tw[i];
+  for (int i = tid; i < S * N; i += kThreads) cacc[i] = make_double2(0.0, 0.0);
+  // tile pair (ti, tj), ti <= tj, from the linear block index
+  int ti = 0, rem = blockIdx.x;
+  while (rem >= a.T - ti) { rem -= a.T - ti; ++ti; }
+  const int tj = ti + rem;
+  const int M = a.nk * a.nbocc;
+  const int ia = ti * S + tw_;
+  const bool va = ia < M;
+  const int ka = (va ? ia : 0) / a.nbocc, ba = (va ? ia : 0) % a.nbocc;
+  const double2* ucol_a = a.u.p + (size_t)ka * a.u.kstride + (size_t)ba * N;
+  double2 ua[E], racc[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    ua[e] = ucol_a[TM::pos(tl, e)];
+    racc[e] = make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  const bool diag = (ti == tj);
+  const int nrounds = diag ? (S / 2 + 1) : S;
+  for (int r = 0; r < nrounds; ++r) {
+    const int lb = (tw_ + r) % S;
+    const int ib = tj * S + lb;
+    bool valid = va && ib < M;
+    if (diag && (S % 2 == 0) && r == S / 2 && tw_ >= S / 2) valid = false;  // counted by the partner
+    const bool self = diag && r == 0;
+    const int kb = (ib < M ? ib : 0) / a.nbocc, bb = (ib < M ? ib : 0) % a.nbocc;
+    const double2* ucol_b = a.u.p + (size_t)kb * a.u.kstride + (size_t)bb * N;
+    double2 ub[E], x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      ub[e] = ucol_b[TM::pos(tl, e)];
+      x[e] = cmulc(ua[e], ub[e]);
+    }
+    fft_team<N, -1>(x, buf, tw_s, tl);
+    // Nyquist coefficient R_ab[N/2] lives in slot (p=0, r=R0/2) of the team's lane 0
+    const double2 rn_own = x[TM::R0 / 2];
+    const double rnx = __shfl_sync(0xffffffffu, rn_own.x, team_lane0);
+    const double rny = __shfl_sync(0xffffffffu, rn_own.y, team_lane0);
+    const int dab = ka - kb + a.nk - 1, dba = kb - ka + a.nk - 1;
+    const double* kab = a.kern + (size_t)dab * N;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const double v = __ldg(kab + TM::pos(tl, e));
+      x[e] = make_double2(v * x[e].x, v * x[e].y);
+    }
+    fft_team<N, +1>(x, buf, tw_s, tl);
+    if (valid) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) racc[e] = cfma(x[e], ub[e], racc[e]);
+      if (!self) {
+        const double dk = __ldg(a.kern + (size_t)dba * N + N / 2) - __ldg(kab + N / 2);
+        const double cx = dk * rnx, cy = -dk * rny;  // dk * conj(R)
+        double2* col = cacc + lb * N;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          const int q = TM::pos(tl, e);
+          const double sg = (q & 1) ? -1.0 : 1.0;
+          const double2 pba = make_double2(fma(sg, cx, x[e].x), fma(sg, cy, -x[e].y));
+          col[q] = cfma(pba, ua[e], col[q]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // write partials: rows from registers, columns from shared memory
+  double2* dst = a.scratch + (size_t)blockIdx.x * 2 * S * N;
+#pragma unroll
+  for (int e = 0; e < E; ++e) dst[(size_t)tw_ * N + TM::pos(tl, e)] = racc[e];
+  for (int i = tid; i < S * N; i += kThreads) dst[(size_t)S * N + i] = cacc[i];
+}
+
+// Exchange term of output column (ik, ib) at grid point q, summed over the
+// partials in a fixed order.
+__device__ __forceinline__ double2 exchange_at(const CombineArgs& a, int ik, int ib, int q, int N) {
+  if (a.sym != nullptr && ib < a.nbocc) {
+    const int S = a.sym_S, T = a.sym_T;
+    const int o = ik * a.nbocc + ib;
+    const int i = o / S, l = o % S;
+    double2 f = make_double2(0.0, 0.0);
+    for (int j = 0; j < T; ++j) {
+      if (j < i) {
+        f = cadd(f, a.sym[((size_t)sym_tp(j, i, T) * 2 + 1) * S * N + (size_t)l * N + q]);
+      } else if (j == i) {
+        const size_t b = (size_t)sym_tp(i, i, T) * 2 * S * N + (size_t)l * N + q;
+        f = cadd(f, a.sym[b]);
+        f = cadd(f, a.sym[b + (size_t)S * N]);
+      } else {
+        f = cadd(f, a.sym[(size_t)sym_tp(i, j, T) * 2 * S * N + (size_t)l * N + q]);
+      }
+    }
+    return f;
+  }
+  const int nbc = a.w.nb - a.chunk_b0;
+  const int c = ik * nbc + (ib - a.chunk_b0);
+  const double2* src = a.scratch + (size_t)c * a.nchunks * N + q;
+  double2 f = src[0];
+  for (int ch = 1; ch < a.nchunks; ++ch) f = cadd(f, src[(size_t)ch * N]);
+  return f;
+}
+
 // ---------------------------------------------------------------------------
 // Combine: kinetic (F:212-234) + local potential (F:199-203) + Fock partials,
 // then the mode's epilogue (RK4 stages RT:166-170, observables F:94-119,
@@ -196,13 +325,10 @@ __global__ void __launch_bounds__(kThreads) k_combine(CombineArgs a, int ncols) 
     ek = team_sum<T>(ek) / (double)N;
     je = team_sum<T>(je) / (double)N;
     double fr = 0.0, fi = 0.0;
-    if (a.scratch != nullptr && ib < a.nbocc) {
+    if ((a.scratch != nullptr || a.sym != nullptr) && ib < a.nbocc) {
 #pragma unroll
       for (int e = 0; e < E; ++e) {
-        const int q = TM::pos(tl, e);
-        const double2* src = a.scratch + (size_t)c * a.nchunks * N + q;
-        double2 f = src[0];
-        for (int ch = 1; ch < a.nchunks; ++ch) f = cadd(f, src[(size_t)ch * N]);
+        const double2 f = exchange_at(a, ik, ib, TM::pos(tl, e), N);
         fr += wv[e].x * f.x + wv[e].y * f.y;
         fi += wv[e].x * f.y - wv[e].y * f.x;
       }
@@ -225,7 +351,8 @@ __global__ void __launch_bounds__(kThreads) k_combine(CombineArgs a, int ncols) 
     x[e] = make_double2(m * x[e].x / (double)N, m * x[e].y / (double)N);
   }
   fft_team<N, +1>(x, bufs[team], tw_s, tl);
-  if (!valid) return;
+  // deferred exchange energy: <w|F> of occupied columns (stage 1 of an RK4 step)
+  double exr = 0.0, exi = 0.0;
   bool bad = false;
 #pragma unroll
   for (int e = 0; e < E; ++e) {
@@ -239,13 +366,16 @@ __global__ void __launch_bounds__(kThreads) k_combine(CombineArgs a, int ncols) 
         const double v = a.vloc[q];
         h = make_double2(x[e].x + v * wv[e].x, x[e].y + v * wv[e].y);
       }
-      if (a.scratch != nullptr) {
-        const double2* src = a.scratch + (size_t)c * a.nchunks * N + q;
-        double2 f = src[0];
-        for (int ch = 1; ch < a.nchunks; ++ch) f = cadd(f, src[(size_t)ch * N]);
+      if (a.scratch != nullptr || a.sym != nullptr) {
+        const double2 f = exchange_at(a, ik, ib, q, N);
+        if (a.ex_cols) {
+          exr += wv[e].x * f.x + wv[e].y * f.y;
+          exi += wv[e].x * f.y - wv[e].y * f.x;
+        }
         h = cadd(h, f);
       }
     }
+    if (!valid) continue;
     if (a.mode == CM_H || a.mode == CM_F || a.mode == CM_T) {
       a.out.p[(size_t)ik * a.out.kstride + (size_t)ib * N + q] = h;
       bad |= !(isfinite(h.x) && isfinite(h.y));
@@ -275,7 +405,33 @@ __global__ void __launch_bounds__(kThreads) k_combine(CombineArgs a, int ncols) 
     }
     bad |= !(isfinite(nx.x) && isfinite(nx.y));
   }
+  if (a.ex_cols) {
+    exr = team_sum<T>(exr);
+    exi = team_sum<T>(exi);
+    if (valid && tl == 0) {
+      a.colbuf[(size_t)c * 4 + 2] = exr;
+      a.colbuf[(size_t)c * 4 + 3] = exi;
+    }
+  }
   if (bad && a.nonfinite) *a.nonfinite = 1;
+}
+
+// Deferred exchange energy Ex = 0.5 sum_occ occ <u|F u> dvcell (F:165-183),
+// added to the Etot of the step whose orbitals produced F.
+__global__ void k_ex_finalize(ExArgs a) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int idx = a.idx;
+  if (idx < 0) idx = *a.it - 1;
+  if (idx < 0) return;
+  double ex = 0.0;
+  for (int ik = 0; ik < a.nk; ++ik)
+    for (int ib = 0; ib < a.nbocc; ++ib) ex += a.occ * a.colbuf[(size_t)(ik * a.nb + ib) * 4 + 2] * a.dvcell;
+  ex = 0.5 * ex;
+  if (a.series_E) a.series_E[idx] = a.series_E[idx] + ex;
+  if (a.out) {
+    a.out[0] = a.out[0] + ex;
+    a.out[4] = ex;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -290,12 +446,12 @@ __global__ void k_obs_reduce(ObsReduceArgs a) {
       const double* cb = a.colbuf + (size_t)(ik * a.nb + ib) * 4;
       ekin += occ * cb[0] * a.dvcell;
       jre += occ * cb[1];
-      if (ib < a.nbocc) exr += occ * cb[2] * a.dvcell;
+      if (ib < a.nbocc && !a.defer_ex) exr += occ * cb[2] * a.dvcell;
     }
   }
-  const double Ex = a.hf ? 0.5 * exr : 0.0;
+  const double Ex = (a.hf && !a.defer_ex) ? 0.5 * exr : 0.0;
   const double Eion = a.scal[1], EH = a.scal[2], Nele = a.scal[0];
-  const double Etot = ekin + Eion + EH + Ex;
+  const double Etot = a.defer_ex ? (ekin + Eion + EH) : (ekin + Eion + EH + Ex);
   const double Je = -(jre * a.dvcell / a.vcell);
   a.out[0] = Etot;
   a.out[1] = ekin;
@@ -329,6 +485,25 @@ static cudaError_t fock_impl(const FockArgs& a, int ncols, cudaStream_t s) {
 }
 
 template <int N>
+static constexpr int sym_teams() { return (kThreads / 32) * Team<N>::PER_WARP; }
+
+template <int N>
+static size_t sym_smem() { return sizeof(double2) * (size_t)N * (1 + 2 * sym_teams<N>()); }
+
+template <int N>
+static cudaError_t fock_sym_impl(const FockSymArgs& a, cudaStream_t s) {
+  const int tiles = a.T * (a.T + 1) / 2;
+  if (tiles == 0) return cudaSuccess;
+  k_fock_sym<N><<<tiles, kThreads, sym_smem<N>(), s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t configure_impl() {
+  return cudaFuncSetAttribute(k_fock_sym<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sym_smem<N>());
+}
+
+template <int N>
 static cudaError_t combine_impl(const CombineArgs& a, int ncols, cudaStream_t s) {
   constexpr int PER_CTA = (kThreads / 32) * Team<N>::PER_WARP;
   const int blocks = (ncols + PER_CTA - 1) / PER_CTA;
@@ -358,6 +533,41 @@ cudaError_t launch_fock(int NG, const FockArgs& a, int ncols, cudaStream_t s) {
 #define CALL(n) fock_impl<n>(a, ncols, s)
   MATTOHF_DISPATCH(NG, CALL)
 #undef CALL
+}
+
+cudaError_t launch_fock_sym(int NG, const FockSymArgs& a, cudaStream_t s) {
+#define CALL(n) fock_sym_impl<n>(a, s)
+  MATTOHF_DISPATCH(NG, CALL)
+#undef CALL
+}
+
+int fock_sym_teams(int NG) {
+  switch (NG) {
+    case 16: return sym_teams<16>();
+    case 32: return sym_teams<32>();
+    case 64: return sym_teams<64>();
+    case 128: return sym_teams<128>();
+    case 256: return sym_teams<256>();
+    case 512: return sym_teams<512>();
+    default: return 0;
+  }
+}
+
+// Per-device kernel attributes (larger dynamic shared memory); call with the
+// device current.
+cudaError_t configure_kernels() {
+  cudaError_t e;
+  if ((e = configure_impl<16>()) != cudaSuccess) return e;
+  if ((e = configure_impl<32>()) != cudaSuccess) return e;
+  if ((e = configure_impl<64>()) != cudaSuccess) return e;
+  if ((e = configure_impl<128>()) != cudaSuccess) return e;
+  if ((e = configure_impl<256>()) != cudaSuccess) return e;
+  return configure_impl<512>();
+}
+
+cudaError_t launch_ex_finalize(const ExArgs& a, cudaStream_t s) {
+  k_ex_finalize<<<1, 32, 0, s>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_combine(int NG, const CombineArgs& a, int ncols, cudaStream_t s) {

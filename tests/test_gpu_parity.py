@@ -105,6 +105,34 @@ def test_hpsi(name):
         assert rel(got, ref) <= TOL_OP, (A, rel(got, ref))
 
 
+@pytest.mark.parametrize("name", list(CONFIGS))
+@pytest.mark.parametrize("sym", [1, 0])
+def test_hpsi_self(name, sym):
+    """h[u] u (w == u): symmetric occupied-pair exchange vs the oracle, and vs the plain kernel."""
+    from oracle import mattohf_oracle as O
+    from mattohf_gb300 import _capi
+    cfg, ctx, S = setup(name)
+    u = O.gram_schmidt(S, rand_orbs(S, 11))
+    ctx.set_option(_capi.OPT_SYMMETRIC, sym)
+    try:
+        got = ctx.ubkwbk_hwbk(u, u, 0.17)
+        vf = ctx.ubkwbk_vFwbk(u, u)
+    finally:
+        ctx.set_option(_capi.OPT_SYMMETRIC, 1)
+    assert rel(got, O.ubkwbk_hwbk(S, u, u, 0.17)) <= TOL_OP
+    assert rel(vf, O.ubkwbk_vFwbk(S, u, u)) <= TOL_OP
+
+
+def test_sym_nyquist_correction():
+    """Orbitals with a large Nyquist component: the symmetric kernel's Nyquist term matters."""
+    from oracle import mattohf_oracle as O
+    cfg, ctx, S = setup("ng32_nk4")
+    u = rand_orbs(S, 12)
+    u[..., 1::2] *= -1.0                    # push weight to the highest frequencies
+    vf = ctx.ubkwbk_vFwbk(u, u)
+    assert rel(vf, O.ubkwbk_vFwbk(S, u, u)) <= TOL_OP
+
+
 @pytest.mark.parametrize("name", ["ng16_nk3_unocc", "ng64_nk8", "ng256_nk2"])
 def test_fock_kinetic_density(name):
     from oracle import mattohf_oracle as O
