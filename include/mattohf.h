@@ -35,6 +35,7 @@ extern "C" {
 #define MATTOHF_ERR_NOTCONV 5    /* eigensolver / orthonormalisation did not converge */
 #define MATTOHF_ERR_ALLOC 6      /* device allocation failed */
 #define MATTOHF_ERR_STATE 7      /* call not valid in the context's current state */
+#define MATTOHF_ERR_TOO_LARGE 8  /* problem does not fit a fixed-size scratch area */
 
 /* options for mattohf_set_option */
 #define MATTOHF_OPT_GRAPH 1        /* 1: replay RK4 steps from a captured CUDA graph (default 1) */
@@ -143,6 +144,24 @@ int mattohf_synchronize(mattohf_ctx* ctx);
  * `device` in TFLOP/s (2 flops per DFMA), the roofline denominator of the
  * FP64-bound kernels. */
 int mattohf_diag_fp64_peak(int device, double* tflops);
+
+/* Exchange term vFwbk = ubkwbk_vFwbk(ubk, wbk) on caller-owned DEVICE buffers
+ * without allocating any device memory.  No counterpart in the reference: it
+ * exists for callers that cannot call cudaMalloc where they need the exchange
+ * term (a host code with a fixed device arena, a shared memory pool that must
+ * not grow, or a loop that must not take the allocator's locks).
+ *   d_vCq   [(2NK-1)][NG] soft-Coulomb table as returned by mattohf_get_coulomb
+ *   d_ubk   [NK][NB][NG] complex128;  d_wbk, d_vFwbk [NK][nbw][NG] complex128
+ *   stream  cudaStream_t to enqueue on (NULL = default stream); asynchronous.
+ * Scratch comes from one 16 MiB device array inside the library that every GPU
+ * loading the library holds until exit.  The first call on a device looks up
+ * that array's device address (cudaGetSymbolAddress) with the device current,
+ * so make it before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller.  Returns
+ * MATTOHF_ERR_TOO_LARGE when the twiddles, the table and one NK*nbw*NG
+ * complex128 set of partial sums do not fit in 16 MiB. */
+int mattohf_fock_noalloc(int NG, int NK, int NB, int NBocc, int nbw, const double* d_vCq,
+                         const double* d_ubk, const double* d_wbk, double* d_vFwbk, void* stream);
 
 #ifdef __cplusplus
 }

@@ -20,6 +20,7 @@ ERR_TIMEOUT = 4
 ERR_NOTCONV = 5
 ERR_ALLOC = 6
 ERR_STATE = 7
+ERR_TOO_LARGE = 8
 
 OPT_GRAPH = 1
 OPT_FOCK_CHUNKS = 2
@@ -34,7 +35,7 @@ EXPORTS = [
     "mattohf_gram_schmidt", "mattohf_hpsi", "mattohf_hpsi_device", "mattohf_fock",
     "mattohf_kinetic", "mattohf_density", "mattohf_observables", "mattohf_rk4_step",
     "mattohf_rk4_run", "mattohf_last_run_timing", "mattohf_gs_run", "mattohf_eps",
-    "mattohf_synchronize", "mattohf_diag_fp64_peak",
+    "mattohf_synchronize", "mattohf_diag_fp64_peak", "mattohf_fock_noalloc",
 ]
 
 
@@ -90,6 +91,7 @@ def load(path: str = LIB_PATH):
         "mattohf_eps": ([P, D, D], I),
         "mattohf_synchronize": ([P], I),
         "mattohf_diag_fp64_peak": ([I, D], I),
+        "mattohf_fock_noalloc": ([I, I, I, I, I, P, P, P, P, P], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -532,6 +532,7 @@ const char* mattohf_status_string(int s) {
     case MATTOHF_ERR_NOTCONV: return "not converged";
     case MATTOHF_ERR_ALLOC: return "device allocation failed";
     case MATTOHF_ERR_STATE: return "invalid state";
+    case MATTOHF_ERR_TOO_LARGE: return "problem exceeds the fixed scratch size";
     default: return "unknown status";
   }
 }
