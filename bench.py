@@ -46,6 +46,18 @@ def fock_flops_per_apply(NG, NK, NB, NBocc):
     return P * (10 * NG * L + 16 * NG)
 
 
+def fock_sym_flops_per_apply(NG, NK, NBocc):
+    """Executed algorithmic FLOPs of the symmetric exchange (w == u, NB == NBocc).
+
+    M = NK*NBocc occupied orbitals; M(M+1)/2 unordered pairs each take two
+    FFTs (5 N log2 N) plus 16 N pointwise; the M(M-1)/2 off-diagonal pairs add
+    the second accumulation (8 N).
+    """
+    L = int(np.log2(NG))
+    M = NK * NBocc
+    return M * (M + 1) // 2 * (10 * NG * L + 16 * NG) + M * (M - 1) // 2 * 8 * NG
+
+
 def dist_info():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -230,28 +242,22 @@ def run_gpu(args, dist):
     u0 = initial_state(ctx)
     K, W = args.steps, args.warmup
     A, Aave = fields(cfg, W + K)
-    # --- warm-up (graph capture happens here)
-    ctx.set_orbitals(u0)
-    ctx.rk4_run(A[:W], Aave[:W], cfg.dt)
-    # --- timed region: K steps, each its own graph replay bracketed by events,
-    #     with an L2 flush (a 512 MiB write) between steps outside the events.
+    # --- timed region: one mattohf_rk4_run of K steps (graph replay); the
+    #     library brackets every step with CUDA events on its stream and writes
+    #     512 MiB (> L2) between steps, outside the events.
     import ctypes as C
-    import torch
-    torch.cuda.set_device(dev)
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
-    step_ms = []
+    ctx.set_option(_capi.OPT_L2_FLUSH, 512 << 20)
+    ctx.set_orbitals(u0)
+    ctx.rk4_run(A[:W], Aave[:W], cfg.dt)          # warm-up incl. graph capture
     dist.barrier()
-    torch.cuda.synchronize()
+    ctx.synchronize()
     with ClockSampler(dev) as clk:
-        for i in range(K):
-            flush.fill_(float(i))
-            torch.cuda.synchronize()
-            ctx.rk4_run(A[W + i:W + i + 1], Aave[W + i:W + i + 1], cfg.dt)
-            run_ms, _, _ = ctx.last_run_timing()
-            step_ms.append(run_ms)
-    torch.cuda.synchronize()
+        ctx.rk4_run(A[W:W + K], Aave[W:W + K], cfg.dt)
+    ctx.synchronize()
     dist.barrier()
-    total_ms = dist.max(float(np.sum(step_ms)))
+    run_ms, _, _ = ctx.last_run_timing()
+    ctx.set_option(_capi.OPT_L2_FLUSH, 0)
+    total_ms = dist.max(run_ms)
     ms_per_step = total_ms / K
     value = dist.ws * K / (total_ms * 1e-3)
     clocks = clk.summary()
@@ -262,7 +268,7 @@ def run_gpu(args, dist):
     ctx.rk4_run(A[:2], Aave[:2], cfg.dt)
     _, fock_ms, nf = ctx.last_run_timing()
     ctx.set_option(_capi.OPT_KERNEL_TIMING, 0)
-    flops = fock_flops_per_apply(cfg.NG, cfg.NK, cfg.NB, cfg.NBocc)
+    flops = fock_sym_flops_per_apply(cfg.NG, cfg.NK, cfg.NBocc)
     achieved = flops / (fock_ms / nf * 1e-3) / 1e12
     peak = C.c_double()
     lib.mattohf_diag_fp64_peak(dev, C.byref(peak))
@@ -275,7 +281,7 @@ def run_gpu(args, dist):
     # --- end to end through the public C ABI with host buffers
     Ke = K
     ue = np.ascontiguousarray(u0)
-    torch.cuda.synchronize()
+    ctx.synchronize()
     t0 = time.perf_counter()
     ctx.set_orbitals(ue)
     E, J, N = ctx.rk4_run(A[W:W + Ke], Aave[W:W + Ke], cfg.dt)
@@ -309,11 +315,132 @@ def run_gpu(args, dist):
                          "frac": achieved / peak.value if peak.value else None,
                          "traffic": prof_traffic, "kernel": "k_fock",
                          "flops_per_launch": flops, "launch_ms": fock_ms / nf,
-                         "peak_source": "measured DFMA throughput on this GPU (mattohf_diag_fp64_peak)"},
+                         "peak_source": "measured DFMA throughput on this GPU (mattohf_diag_fp64_peak)",
+                         "flops_model": "symmetric exchange: M(M+1)/2 pairs x (10 N log2 N + 16 N) + M(M-1)/2 x 8 N, M = NK*NBocc"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * K, "clocks": clocks}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
+
+
+ENSEMBLE_DT = 1.5e-3
+ADJ_DT = 2.5e-3
+
+
+def run_ensemble(args):
+    """Batched ensemble of independent runs vs the same runs one at a time.
+
+    256 runs, seed 1: NK in {8,16,32,64}, Nocc = NB in {1..4}, NG = 128,
+    a in U[8,14], A0 log-uniform in [0.005, 0.2], w in U[0.03, 0.1], T = 200;
+    one ion (Z=2, alpha=1) at a/2; dt = 1.5e-3 (the configured 0.02 is
+    RK4-unstable at NG = 128).  Initial state: Gaussian guess + Gram-Schmidt.
+    """
+    import math
+    from mattohf_gb300 import Batch, RunConfig, define_afield
+    import dataclasses
+    rng = np.random.default_rng(1)
+    R = args.runs
+    nks = rng.choice([8, 16, 32, 64], size=R)
+    noc = rng.integers(1, 5, size=R)
+    acell = rng.uniform(8.0, 14.0, size=R)
+    A0 = np.exp(rng.uniform(math.log(0.005), math.log(0.2), size=R))
+    w = rng.uniform(0.03, 0.1, size=R)
+    cfgs = [RunConfig.from_pulse(float(A0[r]), float(w[r]), 200.0, acell=float(acell[r]), NG=128,
+                                 NK=int(nks[r]), NB=int(noc[r]), NBocc=int(noc[r]), Zeff=[2.0],
+                                 alpha=[1.0], Rion=[0.5], Kion=[1], dt=ENSEMBLE_DT) for r in range(R)]
+    K, W = args.steps, args.warmup
+    t0 = time.perf_counter()
+    b = Batch(cfgs)
+    setup_s = time.perf_counter() - t0
+    A = np.empty((R, W + K))
+    for r, c in enumerate(cfgs):
+        A[r] = define_afield(dataclasses.replace(c, NT=W + K))[1]
+    Aave = np.concatenate([0.5 * A[:, :1], 0.5 * (A[:, 1:] + A[:, :-1])], axis=1)
+    u0 = []
+    for r in range(R):
+        b[r].Init_wf()
+        b[r].Gram_Schmidt()
+        u0.append(b[r].get_orbitals())
+    b.rk4_run(A[:, :W], Aave[:, :W], ENSEMBLE_DT)
+    b.rk4_run(A[:, W:], Aave[:, W:], ENSEMBLE_DT)
+    t_batch = b.last_run_ms()
+    # the same runs one at a time through each member's own (graph-replayed) path
+    t_plain = 0.0
+    for r in range(R):
+        m = b[r]
+        m.set_orbitals(u0[r])
+        m.rk4_run(A[r, :W], Aave[r, :W], ENSEMBLE_DT)
+        m.rk4_run(A[r, W:], Aave[r, W:], ENSEMBLE_DT)
+        t_plain += m.last_run_timing()[0]
+    kb = float(sum(c.NK * c.NB for c in cfgs))
+    line = {"metric": "TDHF RK4 steps/s (ensemble aggregate)", "value": R * K / (t_batch * 1e-3),
+            "unit": "run-steps/s", "n_gpus": 1, "steps": K, "warmup": W, "higher_is_better": True,
+            "plain_value": R * K / (t_plain * 1e-3), "batched_over_plain": t_plain / t_batch,
+            "kpoint_orbital_steps_per_s": kb * K / (t_batch * 1e-3), "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{R} runs, NK in {{8,16,32,64}}, Nocc in {{1..4}}, NG=128, a in [8,14], "
+                                   f"dt={ENSEMBLE_DT}", "setup_s": setup_s}}
+    print(json.dumps(line), flush=True)
+    b.close()
+
+
+def run_adjoint(args):
+    """Adjoint gradient / forward time on the differentiation workload.
+
+    a = 10, one ion (Z=2) at a/2, NK = 16, Nocc = NB = 2, NG = 128, 4000 steps
+    at dt = 2.5e-3 (the configured 0.025 is RK4-unstable here); control = the
+    A0 = 0.05, w = 0.057, T = 100 pulse plus N(0, 1e-3) noise (seed 2);
+    checkpoints every 100 steps; objective = absorbed energy.  Checked by
+    central differences (h = 1e-6) on 32 random samples.
+    """
+    from mattohf_gb300 import Context, RunConfig, define_afield, aave_from_samples
+    import dataclasses
+    nt = args.adj_steps
+    cfg = RunConfig.from_pulse(0.05, 0.057, 100.0, acell=10.0, NG=128, NK=16, NB=2, NBocc=2, Zeff=[2.0],
+                               alpha=[1.0], Rion=[0.5], Kion=[1], dt=ADJ_DT, NT=nt)
+    rng = np.random.default_rng(2)
+    A = define_afield(cfg)[1] + 1e-3 * rng.standard_normal(nt)
+    Aave = aave_from_samples(A)
+    with Context(cfg) as ctx:
+        ctx.Init_wf()
+        ctx.Gram_Schmidt()
+        ctx.GS_calculation(5, 4)
+        u0 = ctx.get_orbitals()
+        E0 = ctx.observables(0.0)["Etot"]
+        # forward: the plain RT loop with per-step observables
+        ctx.rk4_run(A[:50], Aave[:50], cfg.dt)       # warm-up and graph capture
+        ctx.set_orbitals(u0)
+        ctx.rk4_run(A, Aave, cfg.dt)
+        t_fwd = ctx.last_run_timing()[0]
+        ctx.set_orbitals(u0)
+        ctx.adjoint(A[:50], cfg.dt, "energy", ckpt_every=10)   # warm-up
+        ctx.set_orbitals(u0)
+        L, g, gv = ctx.adjoint(A, cfg.dt, "energy", ckpt_every=100)
+        _, t_adj = ctx.adjoint_timing()
+
+        def obj(Ax):
+            ctx.set_orbitals(u0)
+            E, _, _ = ctx.rk4_run(Ax, aave_from_samples(Ax), cfg.dt)
+            return E[-1] - E0
+
+        h = 1e-6
+        gs, fds = [], []
+        for n in rng.choice(nt, size=args.fd_samples, replace=False):
+            Ap, Am = A.copy(), A.copy()
+            Ap[n] += h
+            Am[n] -= h
+            fds.append((obj(Ap) - obj(Am)) / (2 * h))
+            gs.append(g[n])
+        gs, fds = np.array(gs), np.array(fds)
+        worst = float(np.max(np.abs(gs - fds)) / np.max(np.abs(fds)))
+        worst_each = float(np.max(np.abs(gs - fds) / np.abs(fds)))
+    line = {"metric": "adjoint-gradient/forward time ratio", "value": t_adj / t_fwd, "unit": "ratio",
+            "higher_is_better": False, "forward_ms": t_fwd, "adjoint_ms": t_adj, "steps": nt,
+            "objective": L, "fd_rel_err": worst, "fd_max_rel_err_per_sample": worst_each,
+            "fd_samples": args.fd_samples, "fd_h": 1e-6, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "a=10, NK=16, Nocc=2, NG=128, pulse+N(0,1e-3), checkpoints every 100",
+                       "dt": cfg.dt}}
+    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -324,6 +451,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="plain", choices=["plain", "ensemble", "adjoint"])
+    ap.add_argument("--runs", type=int, default=256)
+    ap.add_argument("--adj-steps", type=int, default=4000)
+    ap.add_argument("--fd-samples", type=int, default=32)
     ap.add_argument("--profile-case", action="store_true",
                     help="small profiling case: 3 applies of h[u]u on the workload (no timing)")
     args = ap.parse_args()
@@ -339,7 +470,15 @@ def main():
         return
     dist = Dist()
     try:
-        if args.impl == "reference":
+        if args.workload == "ensemble":
+            from mattohf_gb300 import build
+            build.build()
+            run_ensemble(args)
+        elif args.workload == "adjoint":
+            from mattohf_gb300 import build
+            build.build()
+            run_adjoint(args)
+        elif args.impl == "reference":
             run_reference(args, dist)
         else:
             from mattohf_gb300 import build

@@ -42,6 +42,8 @@ extern "C" {
 #define MATTOHF_OPT_FOCK_CHUNKS 2  /* pair chunks per Fock output column; 0 = automatic */
 #define MATTOHF_OPT_KERNEL_TIMING 3 /* 1: bracket every Fock launch with CUDA events (no graph) */
 #define MATTOHF_OPT_SYMMETRIC 4    /* 1: use the occupied-pair Hermitian symmetry when w == u (default 1) */
+#define MATTOHF_OPT_L2_FLUSH 5     /* >0: bytes written between RK4 steps of mattohf_rk4_run, which then
+                                      reports the summed per-step device time (benchmarking) */
 
 typedef struct mattohf_ctx mattohf_ctx;
 
@@ -80,6 +82,9 @@ int mattohf_get_grids(mattohf_ctx* ctx, double* rx, double* Gx, double* kx, doub
 /* Coulomb tables: vCG[NG] (I:143-146) and vCq[(2NK-1)][NG] = k_vCk(Gx+kx(kr)-kx(kc))
  * indexed by kr-kc+NK-1 (the distinct columns of vCGkk, I:130-137). */
 int mattohf_get_coulomb(mattohf_ctx* ctx, double* vCG, double* vCq);
+/* k_vCk (src/Functions.f90:33-52) of this cell at n arbitrary arguments q (the
+ * debug table vk.out of src/Initialization.f90:149-155 uses q = Gx + kx). */
+int mattohf_vck(mattohf_ctx* ctx, const double* q, int n, double* out);
 /* Ion potential vion[NG]; set replaces it. */
 int mattohf_get_vion(mattohf_ctx* ctx, double* vion);
 int mattohf_set_vion(mattohf_ctx* ctx, const double* vion);
@@ -122,7 +127,8 @@ int mattohf_rk4_step(mattohf_ctx* ctx, double Aave, double A, double dt);
  * state overflows. */
 int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const double* Aave,
                     double* Etot, double* Je, double* Nele);
-/* Device time of the last mattohf_rk4_run in milliseconds, and (with
+/* Device time of the last mattohf_rk4_run in milliseconds (with
+ * MATTOHF_OPT_L2_FLUSH: the sum of the per-step times, flushes excluded), and (with
  * MATTOHF_OPT_KERNEL_TIMING) the summed device time and launch count of the
  * Fock pair kernel inside it. */
 int mattohf_last_run_timing(mattohf_ctx* ctx, double* run_ms, double* fock_ms, int* fock_launches);
@@ -139,6 +145,46 @@ int mattohf_gs_run(mattohf_ctx* ctx, int nscf, int ncg, double* Etot_iter, doubl
 int mattohf_eps(mattohf_ctx* ctx, double* epsbk, double* epserrorbk);
 
 int mattohf_synchronize(mattohf_ctx* ctx);
+
+/* FourierTr / WindowFourierTr (src/RT_calculation.f90:246-351) on the GPU:
+ * for omega_i = i/nomega*omegaM (i = 1..nomega), out[i-1][7] =
+ * {omega, Re JF, Im JF, Re EF, Im EF, Re AF, Im AF} with
+ * JF = sum_t e^{i omega t} filter (J - J0) dt, EF, AF likewise for E, A.
+ * The caller supplies the filter (polynomial or envelope window). */
+int mattohf_fourier(int device, int nt, const double* time, const double* J, double J0, const double* E,
+                    const double* A, const double* filter, int nomega, double omegaM, double dt,
+                    double* out);
+
+/* ---- Adjoint gradient (no reference counterpart).  From the device orbitals
+ * u0, runs nt RK4 steps with A[n] (Aave from A as in RT:227-230, stage
+ * fields as in RT:165) and returns the objective
+ *   objective 0: absorbed energy Etot(u_nt, A[nt-1]) - Etot(u0, 0)
+ *   objective 1: final current Je(u_nt, A[nt-1])
+ * with its gradient dLdA[nt] with respect to every field sample and
+ * dLdvion[NG] with respect to the ion potential on the grid (either output
+ * may be NULL).  Backward RK4 adjoint with checkpoints every ckpt_every
+ * steps (0: about sqrt(nt)) and recomputation between checkpoints.  Requires
+ * NB == NBocc.  Leaves the orbitals at u_nt. */
+int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double dt, const double* A, int ckpt_every,
+                    double* L, double* dLdA, double* dLdvion);
+/* Device times of the last mattohf_adjoint: the forward pass alone and the whole gradient. */
+int mattohf_adjoint_timing(mattohf_ctx* ctx, double* forward_ms, double* total_ms);
+
+/* ---- Batched ensemble (no reference counterpart: the reference runs one
+ * system per process).  nruns independent runs with uneven NK, NB(=NBocc),
+ * acell, ions and fields on one GPU, all with the same NG and device.  Each
+ * member is an ordinary context (mattohf_batch_run) for set/get of orbitals,
+ * Init_wf, Gram_Schmidt or a ground state; mattohf_batch_rk4_run then
+ * advances all of them together, one graph replay per RK4 step.
+ * A, Aave, Etot, Je, Nele are [nruns][nt]; dt is [nruns]. */
+typedef struct mattohf_batch mattohf_batch;
+int mattohf_batch_create(int nruns, const mattohf_config* cfgs, mattohf_batch** out);
+int mattohf_batch_destroy(mattohf_batch* b);
+const char* mattohf_batch_last_error(const mattohf_batch* b);
+mattohf_ctx* mattohf_batch_run(mattohf_batch* b, int run);
+int mattohf_batch_rk4_run(mattohf_batch* b, int nt, const double* dt, const double* A,
+                          const double* Aave, double* Etot, double* Je, double* Nele);
+int mattohf_batch_last_run_ms(mattohf_batch* b, double* ms);
 
 /* Diagnostic (no reference counterpart): measured FP64 FMA throughput of
  * `device` in TFLOP/s (2 flops per DFMA), the roofline denominator of the

@@ -26,6 +26,7 @@ OPT_GRAPH = 1
 OPT_FOCK_CHUNKS = 2
 OPT_KERNEL_TIMING = 3
 OPT_SYMMETRIC = 4
+OPT_L2_FLUSH = 5
 
 # every symbol include/mattohf.h declares
 EXPORTS = [
@@ -36,6 +37,9 @@ EXPORTS = [
     "mattohf_kinetic", "mattohf_density", "mattohf_observables", "mattohf_rk4_step",
     "mattohf_rk4_run", "mattohf_last_run_timing", "mattohf_gs_run", "mattohf_eps",
     "mattohf_synchronize", "mattohf_diag_fp64_peak", "mattohf_fock_noalloc",
+    "mattohf_batch_create", "mattohf_batch_destroy", "mattohf_batch_last_error", "mattohf_batch_run",
+    "mattohf_batch_rk4_run", "mattohf_batch_last_run_ms", "mattohf_adjoint", "mattohf_adjoint_timing",
+    "mattohf_fourier", "mattohf_vck",
 ]
 
 
@@ -92,6 +96,16 @@ def load(path: str = LIB_PATH):
         "mattohf_synchronize": ([P], I),
         "mattohf_diag_fp64_peak": ([I, D], I),
         "mattohf_fock_noalloc": ([I, I, I, I, I, P, P, P, P, P], I),
+        "mattohf_batch_create": ([I, C.POINTER(mattohf_config), C.POINTER(P)], I),
+        "mattohf_batch_destroy": ([P], I),
+        "mattohf_batch_last_error": ([P], C.c_char_p),
+        "mattohf_batch_run": ([P, I], P),
+        "mattohf_batch_rk4_run": ([P, I, D, D, D, D, D, D], I),
+        "mattohf_batch_last_run_ms": ([P, D], I),
+        "mattohf_adjoint": ([P, I, I, C.c_double, D, I, D, D, D], I),
+        "mattohf_adjoint_timing": ([P, D, D], I),
+        "mattohf_vck": ([P, D, I, D], I),
+        "mattohf_fourier": ([I, I, D, D, C.c_double, D, D, D, I, C.c_double, C.c_double, D], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -108,6 +108,13 @@ class Context:
         self._check(self.lib.mattohf_get_coulomb(self.h, _dp(vCG), _dp(vCq)))
         return vCG, vCq
 
+    def vck(self, q) -> np.ndarray:
+        """k_vCk(q) of this cell (src/Functions.f90:33-52) at arbitrary arguments."""
+        q = np.ascontiguousarray(q, dtype=np.float64).ravel()
+        out = np.empty_like(q)
+        self._check(self.lib.mattohf_vck(self.h, _dp(q), q.size, _dp(out)))
+        return out
+
     @property
     def vion(self) -> np.ndarray:
         v = np.empty(self.NG)
@@ -213,6 +220,26 @@ class Context:
         self._check(self.lib.mattohf_last_run_timing(self.h, C.byref(r), C.byref(f), C.byref(n)))
         return r.value, f.value, n.value
 
+    # -- adjoint gradient (extension) -------------------------------------------
+    def adjoint(self, A, dt: float, objective: str = "energy", ckpt_every: int = 0):
+        """(L, dL/dA[n], dL/dvion[x]) of the absorbed energy or final current.
+
+        Propagates the device orbitals nt = len(A) RK4 steps (they end at u_nt).
+        """
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        obj = {"energy": 0, "current": 1}[objective]
+        L = C.c_double()
+        g = np.empty(A.size)
+        gv = np.empty(self.NG)
+        self._check(self.lib.mattohf_adjoint(self.h, obj, A.size, float(dt), _dp(A), int(ckpt_every),
+                                             C.byref(L), _dp(g), _dp(gv)))
+        return L.value, g, gv
+
+    def adjoint_timing(self):
+        f, t = C.c_double(), C.c_double()
+        self._check(self.lib.mattohf_adjoint_timing(self.h, C.byref(f), C.byref(t)))
+        return f.value, t.value
+
     # -- ground state (src/GS_calculation.f90) -----------------------------------
     def GS_calculation(self, nscf: int, ncg: int) -> Dict[str, np.ndarray]:
         Et = np.empty(nscf + 1)
@@ -226,3 +253,95 @@ class Context:
 
     def synchronize(self):
         self._check(self.lib.mattohf_synchronize(self.h))
+
+
+class _Member(Context):
+    """A run owned by a Batch: an ordinary context that the batch destroys."""
+
+    def __init__(self, lib, handle, cfg):  # noqa: D401 - no mattohf_create here
+        self.lib = lib
+        self.cfg = cfg
+        self.NG, self.NK, self.NB, self.NBocc = cfg.NG, cfg.NK, cfg.NB, cfg.NBocc
+        self.h = C.c_void_p(handle)
+        self._owned = False
+
+    def close(self):
+        self.h = None  # destroyed with the batch
+
+
+class Batch:
+    """Many independent runs advanced together (``mattohf_batch``).
+
+    All runs share NG and have NB == NBocc; NK, acell, ions, dt and the
+    vector potential differ per run.  ``batch[r]`` is run r's context.
+    """
+
+    def __init__(self, cfgs, device: int = 0):
+        self.lib = _capi.load()
+        self.cfgs = list(cfgs)
+        keep = []
+        arr = (_capi.mattohf_config * len(self.cfgs))()
+        for c, cfg in zip(arr, self.cfgs):
+            z = np.ascontiguousarray(cfg.Zeff, dtype=np.float64)
+            al = np.ascontiguousarray(cfg.alpha, dtype=np.float64)
+            R = np.ascontiguousarray(cfg.Rion, dtype=np.float64)
+            K = np.ascontiguousarray(cfg.Kion, dtype=np.int32)
+            keep.append((z, al, R, K))
+            c.NG, c.NK, c.NB, c.NBocc = cfg.NG, cfg.NK, cfg.NB, cfg.NBocc
+            c.acell = cfg.acell
+            c.functional_hf = 1 if cfg.functional.strip() == "HF" else 0
+            c.device = device
+            c.nspecies, c.Zeff, c.alpha = z.size, _dp(z), _dp(al)
+            c.nion, c.Rion, c.Kion = R.size, _dp(R), K.ctypes.data_as(C.POINTER(C.c_int))
+        h = C.c_void_p()
+        st = self.lib.mattohf_batch_create(len(self.cfgs), arr, C.byref(h))
+        if st != _capi.OK:
+            raise MattohfError(st, self.lib.mattohf_status_string(st).decode())
+        self.h = h
+        self.members = [_Member(self.lib, self.lib.mattohf_batch_run(h, r), cfg)
+                        for r, cfg in enumerate(self.cfgs)]
+
+    def __len__(self):
+        return len(self.members)
+
+    def __getitem__(self, r) -> Context:
+        return self.members[r]
+
+    def _check(self, st):
+        if st != _capi.OK:
+            raise MattohfError(st, self.lib.mattohf_batch_last_error(self.h).decode())
+
+    def rk4_run(self, A, Aave, dt):
+        """A, Aave: (nruns, nt); dt: scalar or (nruns,).  Returns (Etot, Je, Nele), each (nruns, nt)."""
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        Aave = np.ascontiguousarray(Aave, dtype=np.float64)
+        R, nt = A.shape
+        dts = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, dtype=np.float64), (R,)))
+        E, J, N = np.empty((R, nt)), np.empty((R, nt)), np.empty((R, nt))
+        self._check(self.lib.mattohf_batch_rk4_run(self.h, nt, _dp(dts), _dp(A), _dp(Aave), _dp(E), _dp(J),
+                                                    _dp(N)))
+        return E, J, N
+
+    def last_run_ms(self) -> float:
+        ms = C.c_double()
+        self._check(self.lib.mattohf_batch_last_run_ms(self.h, C.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            for m in self.members:
+                m.h = None
+            self.lib.mattohf_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <functional>
 
 using namespace mattohf;
 
@@ -58,6 +59,7 @@ struct mattohf_ctx {
   double2* tw = nullptr;
   double *d_Gx = nullptr, *d_kx = nullptr, *d_vCG = nullptr, *d_vcq = nullptr, *d_kern = nullptr;
   double *d_vion = nullptr, *d_vloc = nullptr, *d_rho = nullptr, *d_scal = nullptr, *d_out = nullptr;
+  double* d_dpart = nullptr;  // [kDensChunks][NG] density partials
   // state
   double2 *d_u = nullptr, *d_us = nullptr, *d_k[4] = {nullptr, nullptr, nullptr, nullptr};
   // staging for host-array entry points
@@ -68,8 +70,9 @@ struct mattohf_ctx {
   size_t scratch_cap = 0;
   double* d_colbuf = nullptr;
   size_t colbuf_cap = 0;
-  double2* d_sym = nullptr;   // symmetric-exchange partials
+  double2* d_sym = nullptr;   // symmetric-exchange tile partials
   size_t sym_cap = 0;
+  double2* d_symF = nullptr;  // reduced symmetric exchange [NK*NBocc][NG]
   int* d_int = nullptr;  // [0] = step counter, [1] = non-finite flag, [2] = solver flag
   // RT series
   double *d_A = nullptr, *d_Aave = nullptr, *d_sE = nullptr, *d_sJ = nullptr, *d_sN = nullptr;
@@ -81,6 +84,18 @@ struct mattohf_ctx {
   double *d_eps = nullptr, *d_err = nullptr;
   // options
   int opt_graph = 1, opt_chunks = 0, opt_timing = 0, opt_sym = 1;
+  long long opt_flush = 0;            // bytes written between timed RK4 steps (0 = no flush)
+  void* d_flush = nullptr;
+  size_t flush_cap = 0;
+  std::vector<cudaEvent_t> step_events;
+  // adjoint work
+  double2 *d_ckpt = nullptr, *d_store = nullptr, *d_lam = nullptr, *d_lamu = nullptr, *d_vbuf = nullptr,
+          *d_Fa = nullptr, *d_uN = nullptr, *d_u0 = nullptr;
+  double2* d_lamk[4] = {nullptr, nullptr, nullptr, nullptr};
+  double *d_psi = nullptr, *d_sig = nullptr, *d_gcol = nullptr, *d_gstage = nullptr, *d_gvion = nullptr,
+         *d_vloc_adj = nullptr, *d_dpart2 = nullptr;
+  int* d_adj_int = nullptr;  // [0] step n, [1] segment start
+  double last_adj_ms = 0, last_adj_fwd_ms = 0;
   // graph of one RK4 step
   cudaGraphExec_t step_exec = nullptr;
   double step_dt = 0;
@@ -200,6 +215,9 @@ int enq_density(mattohf_ctx* ctx, Block u) {
   a.vloc = ctx->d_vloc;
   a.scal = ctx->d_scal;
   a.nk = ctx->NK;
+  a.part = ctx->d_dpart;
+  a.mu = nullptr;
+  a.gvion = nullptr;
   CK(launch_density(ctx->NG, a, ctx->st));
   return MATTOHF_OK;
 }
@@ -241,6 +259,18 @@ int timed_end(mattohf_ctx* ctx) {
   return MATTOHF_OK;
 }
 
+// Every buffer the RK4 step's exchange applies need, allocated up front so a
+// graph capture never has to grow one.
+int ensure_fock_buffers(mattohf_ctx* ctx) {
+  CKR(ensure_scratch(ctx, ctx->NK * ctx->NB));
+  const int M = ctx->NK * ctx->NBocc;
+  const int S = choose_sym_tile(ctx->NG, M);
+  const int T = (M + S - 1) / S;
+  CKR(ensure_sym(ctx, (size_t)T * (T + 1) / 2 * 2 * S * ctx->NG));
+  if (!ctx->d_symF) CKR(dalloc(ctx, &ctx->d_symF, (size_t)M * ctx->NG));
+  return MATTOHF_OK;
+}
+
 // Exchange partials of h[u] w.  When w is u itself (all RK4 stages, Ex,
 // Subspace_diag, eps) the occupied rows use the symmetric pair kernel and only
 // the unoccupied rows (if any) take the chunked kernel.
@@ -250,10 +280,11 @@ int enq_fock(mattohf_ctx* ctx, Block u, Block w, FockPlan* plan) {
   const bool same = (w.p == u.p) && (w.kstride == u.kstride) && (w.nb == u.nb);
   const int NG = ctx->NG;
   if (same && ctx->opt_sym) {
-    const int S = fock_sym_teams(NG);
     const int M = ctx->NK * ctx->NBocc;
+    const int S = choose_sym_tile(NG, M);
     const int T = (M + S - 1) / S;
     CKR(ensure_sym(ctx, (size_t)T * (T + 1) / 2 * 2 * S * NG));
+    if (!ctx->d_symF) CKR(dalloc(ctx, &ctx->d_symF, (size_t)M * NG));
     FockSymArgs a;
     a.u = u;
     a.nk = ctx->NK;
@@ -263,10 +294,11 @@ int enq_fock(mattohf_ctx* ctx, Block u, Block w, FockPlan* plan) {
     a.kern = ctx->d_kern;
     a.tw = ctx->tw;
     a.scratch = ctx->d_sym;
+    a.F = ctx->d_symF;
     CKR(timed_begin(ctx));
     CK(launch_fock_sym(NG, a, ctx->st));
     CKR(timed_end(ctx));
-    plan->sym = ctx->d_sym;
+    plan->sym = ctx->d_symF;
     plan->S = S;
     plan->T = T;
     plan->b0 = ctx->NBocc;
@@ -592,6 +624,7 @@ int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out) {
     e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
     e = configure_kernels();
+    if (e == cudaSuccess) e = configure_adjoint_kernels();
     if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
   }
   const size_t nu = orb_elems(ctx, ctx->NB);
@@ -600,7 +633,7 @@ int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out) {
       (rc = dalloc(ctx, &ctx->d_vloc, NG)) || (rc = dalloc(ctx, &ctx->d_rho, NG)) ||
       (rc = dalloc(ctx, &ctx->d_scal, 8)) || (rc = dalloc(ctx, &ctx->d_out, 8)) ||
       (rc = dalloc(ctx, &ctx->d_u, nu)) || (rc = dalloc(ctx, &ctx->d_us, nu)) ||
-      (rc = dalloc(ctx, &ctx->d_int, 8)))
+      (rc = dalloc(ctx, &ctx->d_int, 8)) || (rc = dalloc(ctx, &ctx->d_dpart, (size_t)kDensChunks * NG)))
     return bail(rc);
   for (int s = 0; s < 4; ++s)
     if ((rc = dalloc(ctx, &ctx->d_k[s], nu))) return bail(rc);
@@ -622,6 +655,16 @@ int mattohf_destroy(mattohf_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   destroy_graph(ctx);
+  {
+    void* adj[] = {ctx->d_ckpt, ctx->d_store, ctx->d_lam, ctx->d_lamu, ctx->d_vbuf, ctx->d_Fa, ctx->d_uN,
+                   ctx->d_u0, ctx->d_lamk[0], ctx->d_lamk[1], ctx->d_lamk[2], ctx->d_lamk[3], ctx->d_psi,
+                   ctx->d_sig, ctx->d_gcol, ctx->d_gstage, ctx->d_gvion, ctx->d_vloc_adj, ctx->d_dpart2,
+                   ctx->d_adj_int};
+    for (void* p : adj)
+      if (p) cudaFree(p);
+  }
+  for (auto ev : ctx->step_events) cudaEventDestroy(ev);
+  if (ctx->d_flush) cudaFree(ctx->d_flush);
   for (auto& ev : ctx->fock_events) {
     cudaEventDestroy(ev.first);
     cudaEventDestroy(ev.second);
@@ -631,7 +674,7 @@ int mattohf_destroy(mattohf_ctx* ctx) {
                   ctx->d_k[1], ctx->d_k[2], ctx->d_k[3], ctx->d_a, ctx->d_b, ctx->d_c,
                   ctx->d_scratch, ctx->d_colbuf, ctx->d_int, ctx->d_A, ctx->d_Aave, ctx->d_sE,
                   ctx->d_sJ, ctx->d_sN, ctx->d_work, ctx->d_hwork, ctx->d_M, ctx->d_V, ctx->d_evals,
-                  ctx->d_eps, ctx->d_err, ctx->d_sym};
+                  ctx->d_eps, ctx->d_err, ctx->d_sym, ctx->d_symF, ctx->d_dpart};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -649,6 +692,10 @@ int mattohf_set_option(mattohf_ctx* ctx, int option, long long value) {
       break;
     case MATTOHF_OPT_KERNEL_TIMING: ctx->opt_timing = value ? 1 : 0; break;
     case MATTOHF_OPT_SYMMETRIC: ctx->opt_sym = value ? 1 : 0; break;
+    case MATTOHF_OPT_L2_FLUSH:
+      if (value < 0 || value > (4LL << 30)) return fail(ctx, MATTOHF_ERR_ARG, "flush bytes out of range");
+      ctx->opt_flush = value;
+      break;
     default: return fail(ctx, MATTOHF_ERR_ARG, "unknown option");
   }
   destroy_graph(ctx);
@@ -675,6 +722,22 @@ int mattohf_get_coulomb(mattohf_ctx* ctx, double* vCG, double* vCq) {
     CK(cudaMemcpyAsync(vCq, ctx->d_vcq, sizeof(double) * ctx->NG * (2 * ctx->NK - 1),
                        cudaMemcpyDeviceToHost, ctx->st));
   return sync_and_flag(ctx);
+}
+
+int mattohf_vck(mattohf_ctx* ctx, const double* q, int n, double* out) {
+  CKR(check_ctx(ctx));
+  if (n < 0 || (n > 0 && (!q || !out))) return fail(ctx, MATTOHF_ERR_ARG, "bad vck arguments");
+  if (n == 0) return MATTOHF_OK;
+  double* d = nullptr;
+  CKR(dalloc(ctx, &d, 2 * (size_t)n));
+  int rc = MATTOHF_OK;
+  if (cudaMemcpyAsync(d, q, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->st) != cudaSuccess ||
+      launch_vck_table(ctx->NG, ctx->NK, ctx->acell, d, n, d + n, ctx->st) != cudaSuccess ||
+      cudaMemcpyAsync(out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->st) != cudaSuccess ||
+      cudaStreamSynchronize(ctx->st) != cudaSuccess)
+    rc = fail(ctx, MATTOHF_ERR_CUDA, "k_vCk evaluation failed");
+  cudaFree(d);
+  return rc;
 }
 
 int mattohf_get_vion(mattohf_ctx* ctx, double* vion) {
@@ -838,7 +901,7 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
   if (nt < 0 || (nt > 0 && (!A || !Aave))) return fail(ctx, MATTOHF_ERR_ARG, "bad rk4_run arguments");
   if (nt == 0) return MATTOHF_OK;
   CKR(ensure_series(ctx, nt));
-  CKR(ensure_scratch(ctx, ctx->NK * ctx->NB));
+  CKR(ensure_fock_buffers(ctx));
   CK(cudaMemcpyAsync(ctx->d_A, A, sizeof(double) * nt, cudaMemcpyHostToDevice, ctx->st));
   CK(cudaMemcpyAsync(ctx->d_Aave, Aave, sizeof(double) * nt, cudaMemcpyHostToDevice, ctx->st));
   CK(cudaMemsetAsync(ctx->d_int, 0, 2 * sizeof(int), ctx->st));
@@ -868,6 +931,23 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
     ctx->step_dt = dt;
   }
   ctx->fock_event_used = 0;
+  // Optional per-step timing with an L2 flush between steps: each step (and
+  // the closing exchange apply) is bracketed by its own events and the flush
+  // runs outside them.
+  const bool stepwise = ctx->opt_flush > 0;
+  if (stepwise) {
+    if ((size_t)ctx->opt_flush > ctx->flush_cap) {
+      if (ctx->d_flush) cudaFree(ctx->d_flush);
+      ctx->d_flush = nullptr;
+      CK(cudaMalloc(&ctx->d_flush, (size_t)ctx->opt_flush));
+      ctx->flush_cap = (size_t)ctx->opt_flush;
+    }
+    while (ctx->step_events.size() < 2 * (size_t)(nt + 1)) {
+      cudaEvent_t ev;
+      CK(cudaEventCreate(&ev));
+      ctx->step_events.push_back(ev);
+    }
+  }
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -875,12 +955,17 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
   int flag = 0;
   int bad_at = -1;
   for (int it = 0; it < nt; ++it) {
+    if (stepwise) {
+      CK(cudaMemsetAsync(ctx->d_flush, it & 0xff, (size_t)ctx->opt_flush, ctx->st));
+      CK(cudaEventRecord(ctx->step_events[2 * it], ctx->st));
+    }
     if (use_graph) {
       CK(cudaGraphLaunch(ctx->step_exec, ctx->st));
     } else {
       CKR(enq_rk4(ctx, fm, fave, fcur, dt, ctx->d_sE));
       CKR(enq_observables(ctx, ctx->d_u, fcur, true, true));
     }
+    if (stepwise) CK(cudaEventRecord(ctx->step_events[2 * it + 1], ctx->st));
     // bounded detection of a blow-up: poll the flag every 256 steps
     if ((it & 255) == 255 && it + 1 < nt) {
       CK(cudaMemcpyAsync(&flag, ctx->d_int + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
@@ -895,6 +980,10 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
     // exchange energy of the last step's orbitals (the next stage-1 apply that
     // would supply it does not happen)
     const int last = bad_at >= 0 ? bad_at : nt - 1;
+    if (stepwise) {
+      CK(cudaMemsetAsync(ctx->d_flush, 0x5a, (size_t)ctx->opt_flush, ctx->st));
+      CK(cudaEventRecord(ctx->step_events[2 * nt], ctx->st));
+    }
     if (ctx->hf) {
       FockPlan fp;
       CKR(enq_observables(ctx, ctx->d_u, aval(0.0), false, false, &fp));
@@ -904,8 +993,22 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
   }
   CK(cudaEventRecord(e1, ctx->st));
   CK(cudaEventSynchronize(e1));
+  cudaEvent_t e1_copy = e1;
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, e0, e1));
+  if (stepwise) {
+    const int ndone_steps = bad_at >= 0 ? bad_at + 1 : nt;
+    double sum = 0.0;
+    for (int it = 0; it < ndone_steps; ++it) {
+      float f = 0;
+      CK(cudaEventElapsedTime(&f, ctx->step_events[2 * it], ctx->step_events[2 * it + 1]));
+      sum += f;
+    }
+    float f = 0;
+    CK(cudaEventElapsedTime(&f, ctx->step_events[2 * nt], e1_copy));
+    sum += f;
+    ms = (float)sum;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   ctx->last_run_ms = ms;
@@ -1093,6 +1196,644 @@ int mattohf_diag_fp64_peak(int device, double* tflops) {
 int mattohf_synchronize(mattohf_ctx* ctx) {
   CKR(check_ctx(ctx));
   return sync_and_flag(ctx);
+}
+
+}  // extern "C"
+
+
+// ===========================================================================
+// Adjoint of the RK4 real-time loop (no counterpart in the reference).
+// ===========================================================================
+namespace {
+
+// Recompute one forward step from d_u, storing its four stage inputs in the
+// segment store at slot (it - seg0)*4 + s.
+int enq_recompute_step(mattohf_ctx* ctx, AField fm, AField fave, AField fcur, double dt, size_t elems) {
+  const int NG = ctx->NG, NB = ctx->NB;
+  const int modes[4] = {CM_RK0, CM_RK1, CM_RK2, CM_RK3};
+  const AField fs[4] = {fm, fave, fave, fcur};
+  int* it = ctx->d_int;
+  int* seg0 = ctx->d_adj_int + 1;
+  CK(launch_stage_copy(nullptr, ctx->d_u, ctx->d_store, it, seg0, 0, elems, 1, ctx->st));
+  for (int s = 0; s < 4; ++s) {
+    const double2* in = (s == 0) ? ctx->d_u : ctx->d_us;
+    Block ub = blk(in, NB, NG, NB);
+    CKR(enq_density(ctx, ub));
+    FockPlan fp;
+    if (ctx->hf) CKR(enq_fock(ctx, ub, ub, &fp));
+    CombineArgs a = combine_base(ctx, ub, fs[s], modes[s], fp);
+    a.out = blko(ctx->d_us, NB, NG, NB);
+    a.dt = dt;
+    CK(launch_combine(NG, a, ctx->NK * NB, ctx->st));
+    if (s < 3) CK(launch_stage_copy(nullptr, ctx->d_us, ctx->d_store, it, seg0, s + 1, elems, 1, ctx->st));
+  }
+  CK(launch_counter_add(it, 1, ctx->st));
+  return MATTOHF_OK;
+}
+
+// One backward RK4 step at n = d_adj_int[0] (RT:165-170 reversed).
+int enq_adjoint_step(mattohf_ctx* ctx, double dt, size_t elems) {
+  const int NG = ctx->NG, NB = ctx->NB, NK = ctx->NK;
+  int* n = ctx->d_adj_int;
+  int* seg0 = ctx->d_adj_int + 1;
+  CK(launch_adj_init(ctx->d_lam, ctx->d_lamu, ctx->d_lamk, dt, elems, ctx->st));
+  const double cst[3] = {0.5 * dt, 0.5 * dt, dt};
+  const int amodes[4] = {AM, AAVE, AAVE, ACUR};
+  const int M = NK * ctx->NBocc;
+  const int S = choose_sym_tile(NG, M);
+  const int T = (M + S - 1) / S;
+  for (int s = 3; s >= 0; --s) {
+    CK(launch_stage_copy(ctx->d_vbuf, nullptr, ctx->d_store, n, seg0, s, elems, 0, ctx->st));
+    Block vb = blk(ctx->d_vbuf, NB, NG, NB);
+    CKR(enq_density(ctx, vb));  // vloc = vH[rho(v)] + vion
+    // sigma = sum Im(conj(mu) v) -> psi = vH[sigma]; accumulate the vion gradient
+    DensArgs d;
+    d.u = vb;
+    d.nbocc = ctx->NBocc;
+    d.occ = ctx->occ;
+    d.vCG = ctx->d_vCG;
+    d.vion = ctx->d_vion;
+    d.tw = ctx->tw;
+    d.dvcell = ctx->dvcell;
+    d.rho = ctx->d_sig;
+    d.vloc = ctx->d_psi;
+    d.scal = ctx->d_scal + 4;
+    d.nk = NK;
+    d.part = ctx->d_dpart2;
+    d.mu = ctx->d_lamk[s];
+    d.gvion = ctx->d_gvion;
+    CK(launch_density(NG, d, ctx->st));
+    if (ctx->hf) {
+      AdjFockArgs f;
+      f.v = ctx->d_vbuf;
+      f.mu = ctx->d_lamk[s];
+      f.kstride = NB * NG;
+      f.nk = NK;
+      f.nbocc = ctx->NBocc;
+      f.S = S;
+      f.T = T;
+      f.kern = ctx->d_kern;
+      f.tw = ctx->tw;
+      f.scratch = ctx->d_sym;
+      CKR(timed_begin(ctx));
+      CK(launch_fock_adj(NG, f, ctx->st));
+      CK(launch_sym_reduce(ctx->d_sym, S, T, M, NG, ctx->d_Fa, ctx->st));
+      CKR(timed_end(ctx));
+    }
+    AdjCombineArgs c;
+    c.mu = ctx->d_lamk[s];
+    c.v = ctx->d_vbuf;
+    c.Fa = ctx->d_Fa;
+    c.psi = ctx->d_psi;
+    c.vloc = ctx->d_vloc;
+    c.Gx = ctx->d_Gx;
+    c.kx = ctx->d_kx;
+    c.tw = ctx->tw;
+    c.af.mode = amodes[s];
+    c.af.val = 0.0;
+    c.af.A = ctx->d_A;
+    c.af.Aave = ctx->d_Aave;
+    c.af.it = n;
+    c.nb = NB;
+    c.occ = ctx->occ;
+    c.lam_u = ctx->d_lamu;
+    c.lam_prev = s > 0 ? ctx->d_lamk[s - 1] : nullptr;
+    c.cprev = s > 0 ? cst[s - 1] : 0.0;
+    c.gcol = ctx->d_gcol;
+    c.gstage = ctx->d_gstage;
+    c.n = n;
+    c.slot = s;
+    CK(launch_adj_combine(NG, c, NK * NB, ctx->st));
+  }
+  CK(cudaMemcpyAsync(ctx->d_lam, ctx->d_lamu, sizeof(double2) * elems, cudaMemcpyDeviceToDevice, ctx->st));
+  CK(launch_counter_add(n, -1, ctx->st));
+  return MATTOHF_OK;
+}
+
+int capture(mattohf_ctx* ctx, cudaGraphExec_t* exec, const std::function<int()>& body) {
+  cudaGraph_t g;
+  ctx->capturing = true;
+  CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+  const int rc = body();
+  const cudaError_t ec = cudaStreamEndCapture(ctx->st, &g);
+  ctx->capturing = false;
+  if (rc != MATTOHF_OK) return rc;
+  CK(ec);
+  const cudaError_t ei = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  CK(ei);
+  return MATTOHF_OK;
+}
+
+}  // namespace
+
+extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double dt, const double* A,
+                               int ckpt_every, double* L, double* dLdA, double* dLdvion) {
+  CKR(check_ctx(ctx));
+  if (objective != 0 && objective != 1) return fail(ctx, MATTOHF_ERR_ARG, "objective must be 0 (energy) or 1 (current)");
+  if (nt < 1 || !A || !(dt > 0.0)) return fail(ctx, MATTOHF_ERR_ARG, "bad adjoint arguments");
+  if (ctx->NB != ctx->NBocc) return fail(ctx, MATTOHF_ERR_ARG, "the adjoint needs all bands occupied (NB == NBocc)");
+  const int NG = ctx->NG, NB = ctx->NB, NK = ctx->NK;
+  const size_t elems = orb_elems(ctx, NB);
+  // checkpoint interval: default sqrt(nt), at most what fits the budget of device memory left
+  int C = ckpt_every > 0 ? ckpt_every : std::max(1, (int)std::lround(std::sqrt((double)nt)));
+  C = std::min(C, nt);
+  const int nseg = (nt + C - 1) / C;
+  size_t freeb = 0, totalb = 0;
+  CK(cudaMemGetInfo(&freeb, &totalb));
+  const size_t need = sizeof(double2) * elems * ((size_t)nseg + 4 * (size_t)C + 10);
+  if (need > freeb) return fail(ctx, MATTOHF_ERR_ALLOC, "checkpoint storage exceeds free device memory; lower ckpt_every");
+  CKR(ensure_series(ctx, nt));
+  CKR(ensure_scratch(ctx, NK * NB));
+  const int M = NK * ctx->NBocc;
+  const int S = choose_sym_tile(NG, M);
+  const int T = (M + S - 1) / S;
+  CKR(ensure_sym(ctx, (size_t)T * (T + 1) / 2 * 2 * S * NG));
+  if (!ctx->d_symF) CKR(dalloc(ctx, &ctx->d_symF, (size_t)M * NG));
+  destroy_graph(ctx);
+  CKR(dalloc(ctx, &ctx->d_ckpt, elems * nseg));
+  CKR(dalloc(ctx, &ctx->d_store, elems * 4 * C));
+  double2** bufs[] = {&ctx->d_lam, &ctx->d_lamu, &ctx->d_vbuf, &ctx->d_Fa, &ctx->d_uN, &ctx->d_u0,
+                      &ctx->d_lamk[0], &ctx->d_lamk[1], &ctx->d_lamk[2], &ctx->d_lamk[3]};
+  for (double2** b : bufs) CKR(dalloc(ctx, b, elems));
+  CKR(dalloc(ctx, &ctx->d_psi, NG));
+  CKR(dalloc(ctx, &ctx->d_sig, NG));
+  CKR(dalloc(ctx, &ctx->d_vloc_adj, NG));
+  CKR(dalloc(ctx, &ctx->d_gvion, NG));
+  CKR(dalloc(ctx, &ctx->d_dpart2, (size_t)kDensChunks * NG));
+  CKR(dalloc(ctx, &ctx->d_gcol, (size_t)NK * NB));
+  CKR(dalloc(ctx, &ctx->d_gstage, (size_t)nt * 4));
+  CKR(dalloc(ctx, &ctx->d_adj_int, 4));
+  // fields (RT:227-230)
+  std::vector<double> Ah(A, A + nt), Aave(nt);
+  Aave[0] = 0.5 * (Ah[0] + 0.0);
+  for (int i = 1; i < nt; ++i) Aave[i] = 0.5 * (Ah[i] + Ah[i - 1]);
+  CK(cudaMemcpyAsync(ctx->d_A, Ah.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->d_Aave, Aave.data(), sizeof(double) * nt, cudaMemcpyHostToDevice, ctx->st));
+  AField fm, fave, fcur;
+  fm.A = fave.A = fcur.A = ctx->d_A;
+  fm.Aave = fave.Aave = fcur.Aave = ctx->d_Aave;
+  fm.it = fave.it = fcur.it = ctx->d_int;
+  fm.val = fave.val = fcur.val = 0.0;
+  fm.mode = AM;
+  fave.mode = AAVE;
+  fcur.mode = ACUR;
+
+  cudaEvent_t e0, e1, e2;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventCreate(&e2));
+  CK(cudaEventRecord(e0, ctx->st));
+  // ---- objective at t = 0 and the forward pass with checkpoints
+  double o0[8];
+  std::vector<double> rho0(NG), rhoN(NG);
+  CKR(enq_observables(ctx, ctx->d_u, aval(0.0), false, false));
+  CK(cudaMemcpyAsync(o0, ctx->d_out, sizeof(double) * 7, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(rho0.data(), ctx->d_rho, sizeof(double) * NG, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(ctx->d_u0, ctx->d_u, sizeof(double2) * elems, cudaMemcpyDeviceToDevice, ctx->st));
+  CK(cudaMemsetAsync(ctx->d_int, 0, 2 * sizeof(int), ctx->st));
+  cudaGraphExec_t gfwd = nullptr, grec = nullptr, gadj = nullptr;
+  auto cleanup = [&]() {
+    if (gfwd) cudaGraphExecDestroy(gfwd);
+    if (grec) cudaGraphExecDestroy(grec);
+    if (gadj) cudaGraphExecDestroy(gadj);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+  };
+  int rc = capture(ctx, &gfwd, [&]() {
+    CK(launch_checkpoint(ctx->d_ckpt, ctx->d_u, ctx->d_int, C, elems, ctx->st));
+    CKR(enq_rk4(ctx, fm, fave, fcur, dt, nullptr));
+    CK(launch_counter_add(ctx->d_int, 1, ctx->st));
+    return MATTOHF_OK;
+  });
+  if (rc == MATTOHF_OK)
+    rc = capture(ctx, &grec, [&]() { return enq_recompute_step(ctx, fm, fave, fcur, dt, elems); });
+  if (rc == MATTOHF_OK) rc = capture(ctx, &gadj, [&]() { return enq_adjoint_step(ctx, dt, elems); });
+  if (rc != MATTOHF_OK) {
+    cleanup();
+    return rc;
+  }
+  for (int it = 0; it < nt; ++it) CK(cudaGraphLaunch(gfwd, ctx->st));
+  CK(cudaEventRecord(e1, ctx->st));
+  // ---- objective at t = T and its gradient
+  const double Afin = Ah[nt - 1];
+  double oN[8];
+  CKR(enq_observables(ctx, ctx->d_u, aval(Afin), false, false));
+  CK(cudaMemcpyAsync(oN, ctx->d_out, sizeof(double) * 7, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(rhoN.data(), ctx->d_rho, sizeof(double) * NG, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(ctx->d_uN, ctx->d_u, sizeof(double2) * elems, cudaMemcpyDeviceToDevice, ctx->st));
+  Block ub = blk(ctx->d_u, NB, NG, NB);
+  if (objective == 0) {
+    // dE = <2 occ dvcell h[u] u, du>
+    CKR(enq_hpsi(ctx, ub, ub, blko(ctx->d_lam, NB, NG, NB), aval(Afin), CM_H));
+    CK(launch_scale2(ctx->d_lam, 2.0 * ctx->occ * ctx->dvcell, elems, ctx->st));
+  } else {
+    // dJ = <-2 occ (dvcell/vcell) P_A u, du>
+    CK(launch_velocity(NG, ctx->d_u, ctx->d_lam, ctx->tw, ctx->d_Gx, ctx->d_kx, NB, Afin,
+                       -2.0 * ctx->occ * ctx->dvcell / ctx->vcell, NK * NB, ctx->st));
+  }
+  CK(cudaMemsetAsync(ctx->d_gvion, 0, sizeof(double) * NG, ctx->st));
+  CK(cudaMemsetAsync(ctx->d_gstage, 0, sizeof(double) * 4 * nt, ctx->st));
+  // ---- backward over segments: recompute stage inputs, then reverse them
+  for (int seg = nseg - 1; seg >= 0; --seg) {
+    const int s0 = seg * C, len = std::min(C, nt - s0);
+    const int hv[2] = {s0 + len - 1, s0};
+    CK(cudaMemcpyAsync(ctx->d_u, ctx->d_ckpt + (size_t)seg * elems, sizeof(double2) * elems,
+                       cudaMemcpyDeviceToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->d_int, &s0, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->d_adj_int, hv, 2 * sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+    for (int j = 0; j < len; ++j) CK(cudaGraphLaunch(grec, ctx->st));
+    for (int j = 0; j < len; ++j) CK(cudaGraphLaunch(gadj, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));  // host values above are stack-resident
+  }
+  CK(cudaEventRecord(e2, ctx->st));
+  std::vector<double> gst((size_t)nt * 4), gv(NG);
+  CK(cudaMemcpyAsync(gst.data(), ctx->d_gstage, sizeof(double) * 4 * nt, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(gv.data(), ctx->d_gvion, sizeof(double) * NG, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(ctx->d_u, ctx->d_uN, sizeof(double2) * elems, cudaMemcpyDeviceToDevice, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  float fwd_ms = 0, tot_ms = 0;
+  cudaEventElapsedTime(&fwd_ms, e0, e1);
+  cudaEventElapsedTime(&tot_ms, e0, e2);
+  ctx->last_adj_fwd_ms = fwd_ms;
+  ctx->last_adj_ms = tot_ms;
+  cleanup();
+  // ---- chain rule: stage fields (2 Aave - A, Aave, Aave, A) -> samples A[n]
+  std::vector<double> gA(nt, 0.0), gAave(nt, 0.0);
+  for (int i = 0; i < nt; ++i) {
+    const double* g = &gst[(size_t)i * 4];
+    gAave[i] += g[1] + g[2] + 2.0 * g[0];
+    gA[i] += g[3] - g[0];
+  }
+  gA[nt - 1] += objective == 0 ? -oN[5] * ctx->vcell : -oN[6] / ctx->vcell;
+  for (int i = 0; i < nt; ++i) {
+    gA[i] += 0.5 * gAave[i];
+    if (i + 1 < nt) gA[i] += 0.5 * gAave[i + 1];
+  }
+  if (L) *L = objective == 0 ? oN[0] - o0[0] : oN[5];
+  if (dLdA) std::copy(gA.begin(), gA.end(), dLdA);
+  if (dLdvion) {
+    for (int g = 0; g < NG; ++g)
+      dLdvion[g] = gv[g] + (objective == 0 ? (rhoN[g] - rho0[g]) * ctx->dvcell : 0.0);
+  }
+  return MATTOHF_OK;
+}
+
+extern "C" int mattohf_adjoint_timing(mattohf_ctx* ctx, double* forward_ms, double* total_ms) {
+  if (!ctx) return MATTOHF_ERR_ARG;
+  if (forward_ms) *forward_ms = ctx->last_adj_fwd_ms;
+  if (total_ms) *total_ms = ctx->last_adj_ms;
+  return MATTOHF_OK;
+}
+
+// ===========================================================================
+// Batched ensemble: many independent runs (uneven NK, NB, acell, fields)
+// advanced together.  Each run keeps its own mattohf_ctx (tables, orbitals,
+// stage buffers, series); per step the batch launches each phase once for
+// all runs — density, symmetric exchange over the union of all runs' tile
+// pairs, combine over the union of all columns — from argument arrays in
+// device memory, and the step is captured once in a CUDA graph.
+// ===========================================================================
+struct mattohf_batch {
+  int R = 0, NG = 0, device = 0;
+  std::vector<mattohf_ctx*> runs;
+  cudaStream_t st = nullptr;
+  int* d_int = nullptr;  // [0] step counter, [1] non-finite flag
+  static constexpr int kVariants = 6;  // stages 0..3, observables, observables with exchange
+  DensArgs* d_dens[kVariants] = {};
+  FockSymArgs* d_fsym[kVariants] = {};
+  CombineArgs* d_comb[kVariants] = {};
+  ObsReduceArgs* d_obs = nullptr;
+  ExArgs* d_ex = nullptr;
+  ExArgs* d_exf = nullptr;
+  int *d_tile_pre = nullptr, *d_elem_pre = nullptr, *d_cta_pre = nullptr;
+  int total_tiles = 0, total_elems = 0, total_ctas = 0;
+  cudaGraphExec_t exec = nullptr;
+  int built_nt = -1;
+  std::vector<double> dts;
+  double last_ms = 0;
+  std::string err;
+};
+
+namespace {
+
+int bfail(mattohf_batch* b, int code, const std::string& m) {
+  if (b) b->err = m;
+  return code;
+}
+
+#define BCK(call)                                                                          \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return bfail(b, MATTOHF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+int bupload(mattohf_batch* b, T** d, const std::vector<T>& h) {
+  if (*d) cudaFree(*d);
+  *d = nullptr;
+  if (cudaMalloc((void**)d, sizeof(T) * std::max<size_t>(1, h.size())) != cudaSuccess)
+    return bfail(b, MATTOHF_ERR_ALLOC, "batch argument allocation failed");
+  BCK(cudaMemcpyAsync(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, b->st));
+  return MATTOHF_OK;
+}
+
+// (Re)build every per-run argument array for runs of `nt` steps.
+int batch_prepare(mattohf_batch* b, int nt) {
+  if (b->built_nt >= nt && b->exec) return MATTOHF_OK;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  const int R = b->R, NG = b->NG;
+  std::vector<DensArgs> dens[mattohf_batch::kVariants];
+  std::vector<FockSymArgs> fsym[mattohf_batch::kVariants];
+  std::vector<CombineArgs> comb[mattohf_batch::kVariants];
+  std::vector<ObsReduceArgs> obs(R);
+  std::vector<ExArgs> ex(R), exf(R);
+  std::vector<int> tile_pre(R + 1, 0), elem_pre(R + 1, 0), cta_pre(R + 1, 0);
+  const int cpc = combine_cols_per_cta(NG);
+  const int S = fock_sym_teams(NG);
+  for (int r = 0; r < R; ++r) {
+    mattohf_ctx* ctx = b->runs[r];
+    int rc;
+    if ((rc = ensure_series(ctx, nt)) || (rc = ensure_scratch(ctx, ctx->NK * ctx->NB)))
+      return bfail(b, rc, ctx->err);
+    const int M = ctx->NK * ctx->NBocc;
+    const int T = (M + S - 1) / S;
+    if ((rc = ensure_sym(ctx, (size_t)T * (T + 1) / 2 * 2 * S * NG))) return bfail(b, rc, ctx->err);
+    if (!ctx->d_symF && (rc = dalloc(ctx, &ctx->d_symF, (size_t)M * NG))) return bfail(b, rc, ctx->err);
+    tile_pre[r + 1] = tile_pre[r] + T * (T + 1) / 2;
+    elem_pre[r + 1] = elem_pre[r] + M * NG;
+    cta_pre[r + 1] = cta_pre[r] + (ctx->NK * ctx->NB + cpc - 1) / cpc;
+    AField fld[4];
+    for (int i = 0; i < 4; ++i) {
+      fld[i].A = ctx->d_A;
+      fld[i].Aave = ctx->d_Aave;
+      fld[i].it = b->d_int;
+      fld[i].val = 0.0;
+    }
+    fld[0].mode = AM;
+    fld[1].mode = AAVE;
+    fld[2].mode = AAVE;
+    fld[3].mode = ACUR;
+    const int modes[4] = {CM_RK0, CM_RK1, CM_RK2, CM_RK3};
+    for (int v = 0; v < mattohf_batch::kVariants; ++v) {
+      const double2* uin = (v >= 1 && v <= 3) ? ctx->d_us : ctx->d_u;
+      Block ub = blk(uin, ctx->NB, NG, ctx->NB);
+      DensArgs d;
+      d.u = ub;
+      d.nbocc = ctx->NBocc;
+      d.occ = ctx->occ;
+      d.vCG = ctx->d_vCG;
+      d.vion = ctx->d_vion;
+      d.tw = ctx->tw;
+      d.dvcell = ctx->dvcell;
+      d.rho = ctx->d_rho;
+      d.vloc = ctx->d_vloc;
+      d.scal = ctx->d_scal;
+      d.nk = ctx->NK;
+      d.part = ctx->d_dpart;
+      d.mu = nullptr;
+      d.gvion = nullptr;
+      dens[v].push_back(d);
+      FockSymArgs f;
+      f.u = ub;
+      f.nk = ctx->NK;
+      f.nbocc = ctx->NBocc;
+      f.S = S;
+      f.T = T;
+      f.kern = ctx->d_kern;
+      f.tw = ctx->tw;
+      f.scratch = ctx->d_sym;
+      f.F = ctx->d_symF;
+      fsym[v].push_back(f);
+      FockPlan fp;
+      fp.any = (v != 4);
+      fp.sym = ctx->d_symF;
+      fp.S = S;
+      fp.T = T;
+      fp.b0 = ctx->NBocc;
+      const AField af = v < 4 ? fld[v] : fld[3];
+      CombineArgs c = combine_base(ctx, ub, af, v < 4 ? modes[v] : CM_OBS, fp);
+      if (v == 4) {
+        c.sym = nullptr;
+        c.scratch = nullptr;
+      }
+      if (v == 5) c.af = aval(0.0);
+      c.out = blko(ctx->d_us, ctx->NB, NG, ctx->NB);
+      c.dt = b->dts[r];
+      c.ex_cols = (v == 0 && ctx->hf) ? 1 : 0;
+      c.nonfinite = b->d_int + 1;
+      comb[v].push_back(c);
+    }
+    ObsReduceArgs o;
+    o.colbuf = ctx->d_colbuf;
+    o.scal = ctx->d_scal;
+    o.nk = ctx->NK;
+    o.nb = ctx->NB;
+    o.nbocc = ctx->NBocc;
+    o.occ = ctx->occ;
+    o.dvcell = ctx->dvcell;
+    o.vcell = ctx->vcell;
+    o.NGd = (double)NG;
+    o.hf = ctx->hf;
+    o.defer_ex = 1;
+    o.out = ctx->d_out;
+    o.series_E = ctx->d_sE;
+    o.series_J = ctx->d_sJ;
+    o.series_N = ctx->d_sN;
+    o.it = b->d_int;
+    o.advance = 2;
+    o.nonfinite = b->d_int + 1;
+    obs[r] = o;
+    ex[r] = ex_args(ctx, ctx->d_sE, -1, nullptr);
+    ex[r].it = b->d_int;
+    exf[r] = ex_args(ctx, ctx->d_sE, nt - 1, nullptr);
+    exf[r].it = b->d_int;
+  }
+  int rc;
+  for (int v = 0; v < mattohf_batch::kVariants; ++v) {
+    if ((rc = bupload(b, &b->d_dens[v], dens[v])) || (rc = bupload(b, &b->d_fsym[v], fsym[v])) ||
+        (rc = bupload(b, &b->d_comb[v], comb[v])))
+      return rc;
+  }
+  if ((rc = bupload(b, &b->d_obs, obs)) || (rc = bupload(b, &b->d_ex, ex)) || (rc = bupload(b, &b->d_exf, exf)) ||
+      (rc = bupload(b, &b->d_tile_pre, tile_pre)) || (rc = bupload(b, &b->d_elem_pre, elem_pre)) ||
+      (rc = bupload(b, &b->d_cta_pre, cta_pre)))
+    return rc;
+  b->total_tiles = tile_pre[R];
+  b->total_elems = elem_pre[R];
+  b->total_ctas = cta_pre[R];
+  BCK(cudaStreamSynchronize(b->st));
+  // capture one step for all runs
+  cudaGraph_t g;
+  BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int s = 0; s < 4 && e == cudaSuccess; ++s) {
+    e = launch_density_batch(NG, b->d_dens[s], R, b->st);
+    if (e == cudaSuccess)
+      e = launch_fock_sym_batch(NG, b->d_fsym[s], b->d_tile_pre, R, b->total_tiles, b->d_elem_pre,
+                                b->total_elems, b->st);
+    if (e == cudaSuccess) e = launch_combine_batch(NG, b->d_comb[s], b->d_cta_pre, R, b->total_ctas, b->st);
+    if (e == cudaSuccess && s == 0) e = launch_ex_finalize_batch(b->d_ex, R, b->st);
+  }
+  if (e == cudaSuccess) e = launch_density_batch(NG, b->d_dens[4], R, b->st);
+  if (e == cudaSuccess) e = launch_combine_batch(NG, b->d_comb[4], b->d_cta_pre, R, b->total_ctas, b->st);
+  if (e == cudaSuccess) e = launch_obs_reduce_batch(b->d_obs, R, b->st);
+  if (e == cudaSuccess) e = launch_step_advance(b->d_int, b->st);
+  cudaError_t ec = cudaStreamEndCapture(b->st, &g);
+  BCK(e);
+  BCK(ec);
+  cudaError_t ei = cudaGraphInstantiate(&b->exec, g, 0);
+  cudaGraphDestroy(g);
+  BCK(ei);
+  b->built_nt = nt;
+  return MATTOHF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mattohf_batch_create(int nruns, const mattohf_config* cfgs, mattohf_batch** out) {
+  if (!out || !cfgs || nruns < 1) return MATTOHF_ERR_ARG;
+  *out = nullptr;
+  for (int r = 0; r < nruns; ++r) {
+    if (cfgs[r].NG != cfgs[0].NG || cfgs[r].device != cfgs[0].device) return MATTOHF_ERR_ARG;
+    if (cfgs[r].NB != cfgs[r].NBocc) return MATTOHF_ERR_ARG;  // all bands occupied (symmetric exchange)
+  }
+  mattohf_batch* b = new mattohf_batch();
+  b->R = nruns;
+  b->NG = cfgs[0].NG;
+  b->device = cfgs[0].device;
+  b->dts.assign(nruns, 0.0);
+  for (int r = 0; r < nruns; ++r) {
+    mattohf_ctx* c = nullptr;
+    const int rc = mattohf_create(&cfgs[r], &c);
+    if (rc != MATTOHF_OK) {
+      mattohf_batch_destroy(b);
+      return rc;
+    }
+    b->runs.push_back(c);
+  }
+  if (cudaSetDevice(b->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&b->d_int, 4 * sizeof(int)) != cudaSuccess ||
+      cudaMemset(b->d_int, 0, 4 * sizeof(int)) != cudaSuccess) {
+    mattohf_batch_destroy(b);
+    return MATTOHF_ERR_CUDA;
+  }
+  *out = b;
+  return MATTOHF_OK;
+}
+
+int mattohf_batch_destroy(mattohf_batch* b) {
+  if (!b) return MATTOHF_OK;
+  cudaSetDevice(b->device);
+  if (b->st) cudaStreamSynchronize(b->st);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (int v = 0; v < mattohf_batch::kVariants; ++v) {
+    cudaFree(b->d_dens[v]);
+    cudaFree(b->d_fsym[v]);
+    cudaFree(b->d_comb[v]);
+  }
+  void* ptrs[] = {b->d_obs, b->d_ex, b->d_exf, b->d_tile_pre, b->d_elem_pre, b->d_cta_pre, b->d_int};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (auto* c : b->runs) mattohf_destroy(c);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+  return MATTOHF_OK;
+}
+
+const char* mattohf_batch_last_error(const mattohf_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+mattohf_ctx* mattohf_batch_run(mattohf_batch* b, int run) {
+  if (!b || run < 0 || run >= b->R) return nullptr;
+  return b->runs[run];
+}
+
+int mattohf_batch_rk4_run(mattohf_batch* b, int nt, const double* dt, const double* A, const double* Aave,
+                          double* Etot, double* Je, double* Nele) {
+  if (!b || nt < 0 || (nt > 0 && (!dt || !A || !Aave))) return MATTOHF_ERR_ARG;
+  if (nt == 0) return MATTOHF_OK;
+  BCK(cudaSetDevice(b->device));
+  bool dt_changed = false;
+  for (int r = 0; r < b->R; ++r) {
+    if (!(dt[r] > 0.0) || !std::isfinite(dt[r])) return bfail(b, MATTOHF_ERR_ARG, "dt must be positive");
+    if (b->dts[r] != dt[r]) dt_changed = true;
+    b->dts[r] = dt[r];
+  }
+  if (dt_changed || b->built_nt < nt) {
+    b->built_nt = -1;
+    int rc = batch_prepare(b, nt);
+    if (rc != MATTOHF_OK) return rc;
+  } else {
+    // the final-exchange arguments depend on nt
+    std::vector<ExArgs> exf(b->R);
+    for (int r = 0; r < b->R; ++r) {
+      exf[r] = ex_args(b->runs[r], b->runs[r]->d_sE, nt - 1, nullptr);
+      exf[r].it = b->d_int;
+    }
+    BCK(cudaMemcpyAsync(b->d_exf, exf.data(), sizeof(ExArgs) * b->R, cudaMemcpyHostToDevice, b->st));
+  }
+  // every run's orbitals were set on its own stream
+  for (auto* c : b->runs) BCK(cudaStreamSynchronize(c->st));
+  for (int r = 0; r < b->R; ++r) {
+    mattohf_ctx* c = b->runs[r];
+    BCK(cudaMemcpyAsync(c->d_A, A + (size_t)r * nt, sizeof(double) * nt, cudaMemcpyHostToDevice, b->st));
+    BCK(cudaMemcpyAsync(c->d_Aave, Aave + (size_t)r * nt, sizeof(double) * nt, cudaMemcpyHostToDevice, b->st));
+  }
+  BCK(cudaMemsetAsync(b->d_int, 0, 2 * sizeof(int), b->st));
+  cudaEvent_t e0, e1;
+  BCK(cudaEventCreate(&e0));
+  BCK(cudaEventCreate(&e1));
+  BCK(cudaEventRecord(e0, b->st));
+  int flag = 0, bad_at = -1;
+  for (int it = 0; it < nt; ++it) {
+    BCK(cudaGraphLaunch(b->exec, b->st));
+    if ((it & 255) == 255 && it + 1 < nt) {
+      BCK(cudaMemcpyAsync(&flag, b->d_int + 1, sizeof(int), cudaMemcpyDeviceToHost, b->st));
+      BCK(cudaStreamSynchronize(b->st));
+      if (flag) {
+        bad_at = it;
+        break;
+      }
+    }
+  }
+  // exchange energy of the last step's orbitals
+  const int NG = b->NG;
+  BCK(launch_density_batch(NG, b->d_dens[5], b->R, b->st));
+  BCK(launch_fock_sym_batch(NG, b->d_fsym[5], b->d_tile_pre, b->R, b->total_tiles, b->d_elem_pre, b->total_elems, b->st));
+  BCK(launch_combine_batch(NG, b->d_comb[5], b->d_cta_pre, b->R, b->total_ctas, b->st));
+  BCK(launch_ex_finalize_batch(b->d_exf, b->R, b->st));
+  BCK(cudaEventRecord(e1, b->st));
+  BCK(cudaEventSynchronize(e1));
+  float ms = 0;
+  BCK(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->last_ms = ms;
+  const int ndone = bad_at >= 0 ? bad_at + 1 : nt;
+  for (int r = 0; r < b->R; ++r) {
+    mattohf_ctx* c = b->runs[r];
+    if (Etot) BCK(cudaMemcpyAsync(Etot + (size_t)r * nt, c->d_sE, sizeof(double) * ndone, cudaMemcpyDeviceToHost, b->st));
+    if (Je) BCK(cudaMemcpyAsync(Je + (size_t)r * nt, c->d_sJ, sizeof(double) * ndone, cudaMemcpyDeviceToHost, b->st));
+    if (Nele) BCK(cudaMemcpyAsync(Nele + (size_t)r * nt, c->d_sN, sizeof(double) * ndone, cudaMemcpyDeviceToHost, b->st));
+  }
+  BCK(cudaMemcpyAsync(&flag, b->d_int + 1, sizeof(int), cudaMemcpyDeviceToHost, b->st));
+  BCK(cudaStreamSynchronize(b->st));
+  if (flag) return bfail(b, MATTOHF_ERR_NONFINITE, "non-finite state in the ensemble");
+  return MATTOHF_OK;
+}
+
+int mattohf_batch_last_run_ms(mattohf_batch* b, double* ms) {
+  if (!b || !ms) return MATTOHF_ERR_ARG;
+  *ms = b->last_ms;
+  return MATTOHF_OK;
 }
 
 }  // extern "C"

@@ -6,6 +6,7 @@
 namespace mattohf {
 
 constexpr int kThreads = 128;  // threads per CTA for the column/pair kernels (4 warps)
+constexpr int kDensChunks = 32; // column chunks of the two-stage density reduction
 
 // How a kernel obtains the vector potential of the current launch.
 //   AVAL : use `A_val` directly
@@ -55,6 +56,12 @@ struct DensArgs {
   double* vloc;       // NG out: vH + vion
   double* scal;       // out: [0]=Nele, [1]=Eion, [2]=EH
   int nk;
+  double* part;       // scratch [kDensChunks][NG] partial densities
+  // adjoint mode (mu != null): accumulate sigma = sum_cols Im(conj(mu) u)
+  // instead of the density, write vH[sigma] to vloc (no vion), and add
+  // sigma to gvion (if non-null)
+  const double2* mu;
+  double* gvion;
 };
 
 struct FockArgs {
@@ -78,6 +85,7 @@ struct FockSymArgs {
   const double* kern;
   const double2* tw;
   double2* scratch;
+  double2* F;           // reduced exchange term of the occupied orbitals [NK*nbocc][NG]
 };
 
 __host__ __device__ __forceinline__ int sym_tp(int i, int j, int T) {
@@ -97,7 +105,7 @@ enum CombineMode : int {
 
 struct CombineArgs {
   Block w;                  // columns being processed (the h-apply's wbk)
-  const double2* sym;       // symmetric-exchange partials for occupied columns (or null)
+  const double2* sym;       // reduced symmetric exchange [NK*nbocc][NG] for occupied columns (or null)
   int sym_S, sym_T;
   int chunk_b0;             // first band whose exchange comes from the chunked partials
   int ex_cols;              // CM_RK0: also store <w|F> per occupied column (deferred Ex)
@@ -131,8 +139,8 @@ struct ObsReduceArgs {
   double* series_E;         // per step (may be null)
   double* series_J;
   double* series_N;
-  int* it;                  // step counter, incremented when `advance`
-  int advance;
+  int* it;                  // step counter
+  int advance;              // 0: no series; 1: write series[it] and increment it; 2: write only
   int* nonfinite;
 };
 
@@ -140,7 +148,9 @@ struct ObsReduceArgs {
 cudaError_t launch_density(int NG, const DensArgs& a, cudaStream_t s);
 cudaError_t launch_fock(int NG, const FockArgs& a, int ncols, cudaStream_t s);
 cudaError_t launch_fock_sym(int NG, const FockSymArgs& a, cudaStream_t s);
-int fock_sym_teams(int NG);  // S for this grid size
+int fock_sym_teams(int NG);  // teams of a full symmetric-exchange CTA (largest tile size)
+int choose_sym_tile(int NG, int M);  // tile size for a single run of M occupied orbitals
+cudaError_t sym_launch_params(int NG, int S, int* threads, size_t* smem);
 cudaError_t configure_kernels();
 struct ExArgs {
   const double* colbuf;
@@ -154,6 +164,64 @@ struct ExArgs {
 cudaError_t launch_ex_finalize(const ExArgs& a, cudaStream_t s);
 cudaError_t launch_combine(int NG, const CombineArgs& a, int ncols, cudaStream_t s);
 cudaError_t launch_obs_reduce(const ObsReduceArgs& a, cudaStream_t s);
+
+// Batched launchers: per-run argument structs live in device memory; work
+// items map to runs through exclusive prefix arrays (pre[0] = 0, pre[nruns] = total).
+cudaError_t launch_density_batch(int NG, const DensArgs* d_args, int nruns, cudaStream_t s);
+cudaError_t launch_fock_sym_batch(int NG, const FockSymArgs* d_args, const int* d_tile_pre, int nruns,
+                                  int total_tiles, const int* d_elem_pre, int total_elems,
+                                  cudaStream_t s);
+int combine_cols_per_cta(int NG);
+cudaError_t launch_combine_batch(int NG, const CombineArgs* d_args, const int* d_cta_pre, int nruns,
+                                 int total_ctas, cudaStream_t s);
+cudaError_t launch_obs_reduce_batch(const ObsReduceArgs* d_args, int nruns, cudaStream_t s);
+cudaError_t launch_ex_finalize_batch(const ExArgs* d_args, int nruns, cudaStream_t s);
+cudaError_t launch_step_advance(int* it, cudaStream_t s);
+
+// ---- adjoint (k_adjoint.cu) ----
+struct AdjFockArgs {
+  const double2* v;     // stage input [NK][NB][NG]
+  const double2* mu;    // adjoint of the stage derivative, same layout
+  int kstride;          // NB * NG
+  int nk, nbocc, S, T;
+  const double* kern;
+  const double2* tw;
+  double2* scratch;     // tile partials, as FockSymArgs
+};
+struct AdjCombineArgs {
+  const double2* mu;
+  const double2* v;
+  const double2* Fa;    // reduced exchange part of J^T mu (includes the factor i)
+  const double* psi;    // vH[sigma]
+  const double* vloc;   // vH[rho(v)] + vion
+  const double* Gx;
+  const double* kx;
+  const double2* tw;
+  AField af;
+  int nb;
+  double occ;
+  double2* lam_u;       // += J^T mu
+  double2* lam_prev;    // += cprev * J^T mu (previous stage's adjoint), or null
+  double cprev;
+  double* gcol;         // per-column field-gradient partials
+  double* gstage;       // [nt][4] stage-field gradients
+  const int* n;         // current step
+  int slot;             // stage index 0..3
+};
+cudaError_t launch_fock_adj(int NG, const AdjFockArgs& a, cudaStream_t s);
+cudaError_t configure_adjoint_kernels();
+cudaError_t launch_sym_reduce(const double2* part, int S, int T, int M, int N, double2* F, cudaStream_t s);
+cudaError_t launch_adj_combine(int NG, const AdjCombineArgs& a, int ncols, cudaStream_t s);
+cudaError_t launch_adj_init(const double2* lam, double2* lam_u, double2* const* lamk, double dt, size_t n,
+                            cudaStream_t s);
+cudaError_t launch_stage_copy(double2* dst, const double2* src, double2* store, const int* n, const int* seg0,
+                              int slot, size_t elems, int to_store, cudaStream_t s);
+cudaError_t launch_checkpoint(double2* ckpt, const double2* u, const int* it, int every, size_t elems,
+                              cudaStream_t s);
+cudaError_t launch_counter_add(int* p, int d, cudaStream_t s);
+cudaError_t launch_velocity(int NG, const double2* u, double2* out, const double2* tw, const double* Gx,
+                            const double* kx, int nb, double A, double scale, int ncols, cudaStream_t s);
+cudaError_t launch_scale2(double2* x, double sc, size_t n, cudaStream_t s);
 
 // Tables (k_table.cu)
 cudaError_t launch_vck_table(int NG, int NK, double acell, const double* d_q, int nq,

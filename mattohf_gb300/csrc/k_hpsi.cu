@@ -13,8 +13,43 @@ namespace mattohf {
 // ---------------------------------------------------------------------------
 // Density (F:55-71) and Hartree potential (F:147-162), one CTA.
 // ---------------------------------------------------------------------------
+// Stage 1: partial densities over a contiguous range of columns (one CTA per
+// chunk, thread per grid point); the FP64 work is spread over many SMs.
+__device__ __forceinline__ void dens_partial_body(const DensArgs& a, int N, int chunk) {
+  const int ncol = a.nk * a.u.nb;
+  const int per = (ncol + kDensChunks - 1) / kDensChunks;
+  const int c0 = chunk * per, c1 = min(ncol, c0 + per);
+  for (int ig = threadIdx.x; ig < N; ig += blockDim.x) {
+    double s = 0.0;
+    if (a.mu == nullptr) {
+      for (int c = c0; c < c1; ++c) {   // ik outer, ib inner within the chunk (reference order)
+        const int ik = c / a.u.nb, ib = c % a.u.nb;
+        const double occ = ib < a.nbocc ? a.occ : 0.0;
+        const double2 z = a.u.p[(size_t)ik * a.u.kstride + (size_t)ib * N + ig];
+        s += fma(occ * z.x, z.x, (occ * z.y) * z.y);
+      }
+    } else {
+      for (int c = c0; c < c1; ++c) {   // adjoint source: Im(conj(mu) u)
+        const int ik = c / a.u.nb, ib = c % a.u.nb;
+        const size_t o = (size_t)ik * a.u.kstride + (size_t)ib * N + ig;
+        const double2 z = a.u.p[o], m = a.mu[o];
+        s += fma(m.x, z.y, -(m.y * z.x));
+      }
+    }
+    a.part[(size_t)chunk * N + ig] = s;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_dens_partial(DensArgs a, int N) { dens_partial_body(a, N, blockIdx.x); }
+
+__global__ void __launch_bounds__(256) k_dens_partial_batch(const DensArgs* __restrict__ args, int N) {
+  dens_partial_body(args[blockIdx.y], N, blockIdx.x);
+}
+
+// Stage 2 (one CTA): rho = ordered sum of the chunk partials, then the
+// Hartree potential (F:147-162), vloc = vH + vion and the density scalars.
 template <int N>
-__global__ void __launch_bounds__(256) k_density(DensArgs a) {
+__device__ __forceinline__ void density_body(const DensArgs& a) {
   using TM = Team<N>;
   __shared__ double rho_s[N];
   __shared__ double vh_s[N];
@@ -22,17 +57,9 @@ __global__ void __launch_bounds__(256) k_density(DensArgs a) {
   __shared__ double2 buf_s[TM::PER_WARP][N];
   const int tid = threadIdx.x;
   for (int i = tid; i < N; i += blockDim.x) tw_s[i] = a.tw[i];
-  // rho(ig) = sum_ik sum_ib occ*|u|^2, ik outer, ib inner (reference order)
   for (int ig = tid; ig < N; ig += blockDim.x) {
-    double s = 0.0;
-    for (int ik = 0; ik < a.nk; ++ik) {
-      const double2* col = a.u.p + (size_t)ik * a.u.kstride + ig;
-      for (int ib = 0; ib < a.u.nb; ++ib) {
-        const double occ = ib < a.nbocc ? a.occ : 0.0;
-        const double2 z = col[(size_t)ib * N];
-        s += fma(occ * z.x, z.x, (occ * z.y) * z.y);
-      }
-    }
+    double s = a.part[ig];
+    for (int ch = 1; ch < kDensChunks; ++ch) s += a.part[(size_t)ch * N + ig];
     rho_s[ig] = s;
     a.rho[ig] = s;
   }
@@ -55,6 +82,13 @@ __global__ void __launch_bounds__(256) k_density(DensArgs a) {
     }
   }
   __syncthreads();
+  if (a.mu != nullptr) {
+    for (int ig = tid; ig < N; ig += blockDim.x) {
+      a.vloc[ig] = vh_s[ig];
+      if (a.gvion) a.gvion[ig] += rho_s[ig];
+    }
+    return;
+  }
   for (int ig = tid; ig < N; ig += blockDim.x) a.vloc[ig] = vh_s[ig] + a.vion[ig];
   if (tid == 0) {
     // sequential sums, as the Fortran SUM intrinsic evaluates them
@@ -68,6 +102,27 @@ __global__ void __launch_bounds__(256) k_density(DensArgs a) {
     a.scal[1] = si * a.dvcell;
     a.scal[2] = 0.5 * sh * a.dvcell;
   }
+}
+
+template <int N>
+__global__ void __launch_bounds__(512) k_density(DensArgs a) { density_body<N>(a); }
+
+
+// one CTA per run
+template <int N>
+__global__ void __launch_bounds__(512) k_density_batch(const DensArgs* __restrict__ args) {
+  density_body<N>(args[blockIdx.x]);
+}
+
+// run owning work item `i` given exclusive prefix sums pre[0..nruns] (pre[0] = 0)
+__device__ __forceinline__ int find_run(const int* __restrict__ pre, int nruns, int i) {
+  int lo = 0, hi = nruns - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pre[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
 }
 
 // ---------------------------------------------------------------------------
@@ -164,27 +219,28 @@ __global__ void __launch_bounds__(kThreads) k_fock(FockArgs a) {
 // unordered pair once (rounds 0..S/2).
 // ---------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(kThreads) k_fock_sym(FockSymArgs a) {
+__device__ __forceinline__ void fock_sym_body(const FockSymArgs& a, const int tile) {
   using TM = Team<N>;
   constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
-  constexpr int S = (kThreads / 32) * PW;
+  const int S = a.S;                          // tile size (runtime, <= teams per CTA)
+  const int nteam = (blockDim.x >> 5) * PW;    // teams in this CTA (>= S)
   extern __shared__ double2 sm[];
   double2* tw_s = sm;                  // N
-  double2* bufs = sm + N;              // S * N  (team FFT buffers)
-  double2* cacc = bufs + S * N;        // S * N  (column accumulators)
+  double2* bufs = sm + N;              // nteam * N  (team FFT buffers)
+  double2* cacc = bufs + nteam * N;    // S * N  (column accumulators)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tl = lane % T, tw_ = warp * PW + lane / T;
   const int team_lane0 = (lane / T) * T;
   double2* buf = bufs + tw_ * N;
-  for (int i = tid; i < N; i += kThreads) tw_s[i] = a.tw[i];
-  for (int i = tid; i < S * N; i += kThreads) cacc[i] = make_double2(0.0, 0.0);
+  for (int i = tid; i < N; i += blockDim.x) tw_s[i] = a.tw[i];
+  for (int i = tid; i < S * N; i += blockDim.x) cacc[i] = make_double2(0.0, 0.0);
   // tile pair (ti, tj), ti <= tj, from the linear block index
-  int ti = 0, rem = blockIdx.x;
+  int ti = 0, rem = tile;
   while (rem >= a.T - ti) { rem -= a.T - ti; ++ti; }
   const int tj = ti + rem;
   const int M = a.nk * a.nbocc;
   const int ia = ti * S + tw_;
-  const bool va = ia < M;
+  const bool va = tw_ < S && ia < M;
   const int ka = (va ? ia : 0) / a.nbocc, ba = (va ? ia : 0) % a.nbocc;
   const double2* ucol_a = a.u.p + (size_t)ka * a.u.kstride + (size_t)ba * N;
   double2 ua[E], racc[E];
@@ -242,33 +298,63 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym(FockSymArgs a) {
     __syncthreads();
   }
   // write partials: rows from registers, columns from shared memory
-  double2* dst = a.scratch + (size_t)blockIdx.x * 2 * S * N;
+  double2* dst = a.scratch + (size_t)tile * 2 * S * N;
+  if (tw_ < S) {
 #pragma unroll
-  for (int e = 0; e < E; ++e) dst[(size_t)tw_ * N + TM::pos(tl, e)] = racc[e];
-  for (int i = tid; i < S * N; i += kThreads) dst[(size_t)S * N + i] = cacc[i];
+    for (int e = 0; e < E; ++e) dst[(size_t)tw_ * N + TM::pos(tl, e)] = racc[e];
+  }
+  for (int i = tid; i < S * N; i += blockDim.x) dst[(size_t)S * N + i] = cacc[i];
+}
+
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_fock_sym(FockSymArgs a) { fock_sym_body<N>(a, blockIdx.x); }
+
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_fock_sym_batch(const FockSymArgs* __restrict__ args,
+                                                           const int* __restrict__ pre, int nruns) {
+  const int r = find_run(pre, nruns, blockIdx.x);
+  fock_sym_body<N>(args[r], blockIdx.x - pre[r]);
+}
+
+// Sum the tile-pair partials of every occupied output into F[o][q] (fixed
+// order over tiles: column partials of earlier tiles, the diagonal tile's row
+// and column partials, row partials of later tiles).
+__device__ __forceinline__ void sym_reduce_body(const double2* __restrict__ part, int S, int T, int M,
+                                                int N, double2* __restrict__ F, int idx) {
+  if (idx >= M * N) return;
+  const int o = idx / N, q = idx % N;
+  const int i = o / S, l = o % S;
+  const size_t SN = (size_t)S * N;
+  double2 f = make_double2(0.0, 0.0);
+  for (int j = 0; j < i; ++j) f = cadd(f, part[(size_t)sym_tp(j, i, T) * 2 * SN + SN + (size_t)l * N + q]);
+  {
+    const size_t b = (size_t)sym_tp(i, i, T) * 2 * SN + (size_t)l * N + q;
+    f = cadd(f, part[b]);
+    f = cadd(f, part[b + SN]);
+  }
+  for (int j = i + 1; j < T; ++j) f = cadd(f, part[(size_t)sym_tp(i, j, T) * 2 * SN + (size_t)l * N + q]);
+  F[idx] = f;
+}
+
+__global__ void k_sym_reduce(const double2* __restrict__ part, int S, int T, int M, int N,
+                             double2* __restrict__ F) {
+  sym_reduce_body(part, S, T, M, N, F, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// element prefix: pre[r] = sum over earlier runs of M_r * N
+__global__ void k_sym_reduce_batch(const FockSymArgs* __restrict__ args, const int* __restrict__ pre,
+                                   int nruns, int N) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= pre[nruns]) return;
+  const int r = find_run(pre, nruns, idx);
+  const FockSymArgs& a = args[r];
+  sym_reduce_body(a.scratch, a.S, a.T, a.nk * a.nbocc, N, a.F, idx - pre[r]);
 }
 
 // Exchange term of output column (ik, ib) at grid point q, summed over the
 // partials in a fixed order.
 __device__ __forceinline__ double2 exchange_at(const CombineArgs& a, int ik, int ib, int q, int N) {
-  if (a.sym != nullptr && ib < a.nbocc) {
-    const int S = a.sym_S, T = a.sym_T;
-    const int o = ik * a.nbocc + ib;
-    const int i = o / S, l = o % S;
-    double2 f = make_double2(0.0, 0.0);
-    for (int j = 0; j < T; ++j) {
-      if (j < i) {
-        f = cadd(f, a.sym[((size_t)sym_tp(j, i, T) * 2 + 1) * S * N + (size_t)l * N + q]);
-      } else if (j == i) {
-        const size_t b = (size_t)sym_tp(i, i, T) * 2 * S * N + (size_t)l * N + q;
-        f = cadd(f, a.sym[b]);
-        f = cadd(f, a.sym[b + (size_t)S * N]);
-      } else {
-        f = cadd(f, a.sym[(size_t)sym_tp(i, j, T) * 2 * S * N + (size_t)l * N + q]);
-      }
-    }
-    return f;
-  }
+  if (a.sym != nullptr && ib < a.nbocc) return a.sym[(size_t)(ik * a.nbocc + ib) * N + q];
   const int nbc = a.w.nb - a.chunk_b0;
   const int c = ik * nbc + (ib - a.chunk_b0);
   const double2* src = a.scratch + (size_t)c * a.nchunks * N + q;
@@ -283,7 +369,7 @@ __device__ __forceinline__ double2 exchange_at(const CombineArgs& a, int ik, int
 // F:165-183, F:289-318).  One team per output column.
 // ---------------------------------------------------------------------------
 template <int N>
-__global__ void __launch_bounds__(kThreads) k_combine(CombineArgs a, int ncols) {
+__device__ __forceinline__ void combine_body(const CombineArgs& a, const int ncols, const int cta) {
   using TM = Team<N>;
   constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
   constexpr int NTEAM = (kThreads / 32) * PW;
@@ -295,7 +381,7 @@ __global__ void __launch_bounds__(kThreads) k_combine(CombineArgs a, int ncols) 
   __syncthreads();
   const double A = afield_value(a.af);
   // warp-uniform: whole warps go idle together
-  const int col0 = (blockIdx.x * (kThreads / 32) + warp) * PW;
+  const int col0 = (cta * (kThreads / 32) + warp) * PW;
   if (col0 >= ncols) return;
   const int col = col0 + lane / T;
   const bool valid = col < ncols;
@@ -416,10 +502,23 @@ __global__ void __launch_bounds__(kThreads) k_combine(CombineArgs a, int ncols) 
   if (bad && a.nonfinite) *a.nonfinite = 1;
 }
 
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_combine(CombineArgs a, int ncols) {
+  combine_body<N>(a, ncols, blockIdx.x);
+}
+
+// CTA prefix: pre[r] = sum over earlier runs of ceil(ncols_r / columns per CTA)
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_combine_batch(const CombineArgs* __restrict__ args,
+                                                          const int* __restrict__ pre, int nruns) {
+  const int r = find_run(pre, nruns, blockIdx.x);
+  const CombineArgs& a = args[r];
+  combine_body<N>(a, a.nk * a.w.nb, blockIdx.x - pre[r]);
+}
+
 // Deferred exchange energy Ex = 0.5 sum_occ occ <u|F u> dvcell (F:165-183),
 // added to the Etot of the step whose orbitals produced F.
-__global__ void k_ex_finalize(ExArgs a) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ void ex_finalize_body(const ExArgs& a) {
   int idx = a.idx;
   if (idx < 0) idx = *a.it - 1;
   if (idx < 0) return;
@@ -434,11 +533,19 @@ __global__ void k_ex_finalize(ExArgs a) {
   }
 }
 
+__global__ void k_ex_finalize(ExArgs a) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) ex_finalize_body(a);
+}
+
+__global__ void k_ex_finalize_batch(const ExArgs* __restrict__ args, int nruns) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nruns) ex_finalize_body(args[r]);
+}
+
 // ---------------------------------------------------------------------------
 // Observable reduction (F:74-91, F:165-183, F:289-318) in reference order.
 // ---------------------------------------------------------------------------
-__global__ void k_obs_reduce(ObsReduceArgs a) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ void obs_reduce_body(const ObsReduceArgs& a) {
   double ekin = 0.0, jre = 0.0, exr = 0.0;
   for (int ik = 0; ik < a.nk; ++ik) {
     for (int ib = 0; ib < a.nb; ++ib) {
@@ -466,8 +573,22 @@ __global__ void k_obs_reduce(ObsReduceArgs a) {
     if (a.series_J) a.series_J[it] = Je;
     if (a.series_N) a.series_N[it] = Nele;
     if (!(isfinite(Etot) && isfinite(Je) && isfinite(Nele)) && a.nonfinite) *a.nonfinite = 1;
-    *a.it = it + 1;
+    if (a.advance == 1) *a.it = it + 1;
   }
+}
+
+__global__ void k_obs_reduce(ObsReduceArgs a) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) obs_reduce_body(a);
+}
+
+// one thread per run; the step counter is advanced by k_step_advance afterwards
+__global__ void k_obs_reduce_batch(const ObsReduceArgs* __restrict__ args, int nruns) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nruns) obs_reduce_body(args[r]);
+}
+
+__global__ void k_step_advance(int* it) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *it = *it + 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -490,11 +611,27 @@ static constexpr int sym_teams() { return (kThreads / 32) * Team<N>::PER_WARP; }
 template <int N>
 static size_t sym_smem() { return sizeof(double2) * (size_t)N * (1 + 2 * sym_teams<N>()); }
 
+// threads and dynamic shared memory of a symmetric-exchange CTA with tile size S
+template <int N>
+static void sym_launch_shape(int S, int* threads, size_t* smem) {
+  constexpr int PW = Team<N>::PER_WARP;
+  const int warps = (S + PW - 1) / PW;
+  *threads = 32 * warps;
+  *smem = sizeof(double2) * (size_t)N * (1 + warps * PW + S);
+}
+
 template <int N>
 static cudaError_t fock_sym_impl(const FockSymArgs& a, cudaStream_t s) {
   const int tiles = a.T * (a.T + 1) / 2;
   if (tiles == 0) return cudaSuccess;
-  k_fock_sym<N><<<tiles, kThreads, sym_smem<N>(), s>>>(a);
+  int threads;
+  size_t smem;
+  sym_launch_shape<N>(a.S, &threads, &smem);
+  k_fock_sym<N><<<tiles, threads, smem, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int M = a.nk * a.nbocc;
+  k_sym_reduce<<<(M * N + 255) / 256, 256, 0, s>>>(a.scratch, a.S, a.T, M, N, a.F);
   return cudaGetLastError();
 }
 
@@ -524,7 +661,10 @@ static cudaError_t combine_impl(const CombineArgs& a, int ncols, cudaStream_t s)
   }
 
 cudaError_t launch_density(int NG, const DensArgs& a, cudaStream_t s) {
-#define CALL(n) (k_density<n><<<1, 256, 0, s>>>(a), cudaGetLastError())
+  k_dens_partial<<<kDensChunks, 256, 0, s>>>(a, NG);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+#define CALL(n) (k_density<n><<<1, (n) < 64 ? 64 : (n), 0, s>>>(a), cudaGetLastError())
   MATTOHF_DISPATCH(NG, CALL)
 #undef CALL
 }
@@ -539,6 +679,32 @@ cudaError_t launch_fock_sym(int NG, const FockSymArgs& a, cudaStream_t s) {
 #define CALL(n) fock_sym_impl<n>(a, s)
   MATTOHF_DISPATCH(NG, CALL)
 #undef CALL
+}
+
+// Largest tile size (a power of two up to the teams of a full CTA) that still
+// yields enough tile pairs to occupy every SM several times; small systems
+// fall back to small tiles so their few pairs spread over many SMs.
+int choose_sym_tile(int NG, int M) {
+  int S = fock_sym_teams(NG);
+  while (S > 1) {
+    const int T = (M + S - 1) / S;
+    if (T * (T + 1) / 2 >= 4 * 152) break;
+    S >>= 1;
+  }
+  return S;
+}
+
+cudaError_t sym_launch_params(int NG, int S, int* threads, size_t* smem) {
+  switch (NG) {
+    case 16: sym_launch_shape<16>(S, threads, smem); break;
+    case 32: sym_launch_shape<32>(S, threads, smem); break;
+    case 64: sym_launch_shape<64>(S, threads, smem); break;
+    case 128: sym_launch_shape<128>(S, threads, smem); break;
+    case 256: sym_launch_shape<256>(S, threads, smem); break;
+    case 512: sym_launch_shape<512>(S, threads, smem); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaSuccess;
 }
 
 int fock_sym_teams(int NG) {
@@ -574,6 +740,76 @@ cudaError_t launch_combine(int NG, const CombineArgs& a, int ncols, cudaStream_t
 #define CALL(n) combine_impl<n>(a, ncols, s)
   MATTOHF_DISPATCH(NG, CALL)
 #undef CALL
+}
+
+// ---- batched launchers (many independent runs per launch) ----
+cudaError_t launch_density_batch(int NG, const DensArgs* d_args, int nruns, cudaStream_t s) {
+  k_dens_partial_batch<<<dim3(kDensChunks, nruns), 256, 0, s>>>(d_args, NG);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+#define CALL(n) (k_density_batch<n><<<nruns, (n) < 64 ? 64 : (n), 0, s>>>(d_args), cudaGetLastError())
+  MATTOHF_DISPATCH(NG, CALL)
+#undef CALL
+}
+
+template <int N>
+static cudaError_t fock_sym_batch_impl(const FockSymArgs* d_args, const int* d_tile_pre, int nruns,
+                                       int total_tiles, const int* d_elem_pre, int total_elems,
+                                       cudaStream_t s) {
+  if (total_tiles <= 0) return cudaSuccess;
+  k_fock_sym_batch<N><<<total_tiles, kThreads, sym_smem<N>(), s>>>(d_args, d_tile_pre, nruns);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_sym_reduce_batch<<<(total_elems + 255) / 256, 256, 0, s>>>(d_args, d_elem_pre, nruns, N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fock_sym_batch(int NG, const FockSymArgs* d_args, const int* d_tile_pre, int nruns,
+                                  int total_tiles, const int* d_elem_pre, int total_elems,
+                                  cudaStream_t s) {
+#define CALL(n) fock_sym_batch_impl<n>(d_args, d_tile_pre, nruns, total_tiles, d_elem_pre, total_elems, s)
+  MATTOHF_DISPATCH(NG, CALL)
+#undef CALL
+}
+
+int combine_cols_per_cta(int NG) {
+  switch (NG) {
+    case 16: return (kThreads / 32) * Team<16>::PER_WARP;
+    case 32: return (kThreads / 32) * Team<32>::PER_WARP;
+    case 64: return (kThreads / 32) * Team<64>::PER_WARP;
+    case 128: return (kThreads / 32) * Team<128>::PER_WARP;
+    case 256: return (kThreads / 32) * Team<256>::PER_WARP;
+    case 512: return (kThreads / 32) * Team<512>::PER_WARP;
+    default: return 0;
+  }
+}
+
+cudaError_t launch_combine_batch(int NG, const CombineArgs* d_args, const int* d_cta_pre, int nruns,
+                                 int total_ctas, cudaStream_t s) {
+  if (total_ctas <= 0) return cudaSuccess;
+#define CALL(n) (k_combine_batch<n><<<total_ctas, kThreads, 0, s>>>(d_args, d_cta_pre, nruns), cudaGetLastError())
+  MATTOHF_DISPATCH(NG, CALL)
+#undef CALL
+}
+
+cudaError_t launch_obs_reduce_batch(const ObsReduceArgs* d_args, int nruns, cudaStream_t s) {
+  k_obs_reduce_batch<<<(nruns + 127) / 128, 128, 0, s>>>(d_args, nruns);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ex_finalize_batch(const ExArgs* d_args, int nruns, cudaStream_t s) {
+  k_ex_finalize_batch<<<(nruns + 127) / 128, 128, 0, s>>>(d_args, nruns);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step_advance(int* it, cudaStream_t s) {
+  k_step_advance<<<1, 32, 0, s>>>(it);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sym_reduce(const double2* part, int S, int T, int M, int N, double2* F, cudaStream_t s) {
+  k_sym_reduce<<<(M * N + 255) / 256, 256, 0, s>>>(part, S, T, M, N, F);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_obs_reduce(const ObsReduceArgs& a, cudaStream_t s) {

@@ -10,7 +10,7 @@ tests, golden vectors or fixtures, and it cannot be compiled here (no Fortran
 compiler, no FFTW, no system LAPACK).  The restatement is therefore pinned by
 physics known-answer tests instead (free-particle eigenvalues, the 2*K0(|q|)
 limit of the soft-Coulomb transform, Hermiticity, particle number, gauge
-covariance, RK4 order) which live in ``tests/test_oracle_physics.py``.
+covariance, RK4 order) which live in ``tests/test_oracle.py``.
 
 Third-party arithmetic the reference links but does not vendor:
   * FFTW3 (unpinned OS build, ``src/make.inc:7``): ``dfftw_plan_dft_1d`` with
@@ -782,3 +782,136 @@ def window_fourier_tr(cfg: Config, time, Jtot, Jtotm1, E, A):
     EF = (eiwt * (filt * E)[None, :]).sum(axis=1) * cfg.dt
     AF = (eiwt * (filt * A)[None, :]).sum(axis=1) * cfg.dt
     return omega, JF, EF, AF
+
+
+# ---------------------------------------------------------------------------
+# Adjoint of the RK4 real-time loop (extension: no counterpart in the reference)
+# ---------------------------------------------------------------------------
+# Real inner product <a, b>_R = Re sum conj(a) b over all orbital entries.
+# f(v, a) = -i h[v](a) v is the RK4 right-hand side (RT:166-169).  The
+# adjoint needs J_f(v)^T mu for that real inner product.
+
+def _pair_potential(S: System, ki: int, kj: int, rho: np.ndarray) -> np.ndarray:
+    """Phi_ij[rho] = IFFT(-vCGkk(:,ki,kj)/NG * FFT(rho/NK)) as in F:250-253."""
+    v = S.vCGkk[ki * S.NK + kj]
+    g = fftf(rho / float(S.NK))
+    return fftb(-v * g / float(S.NG))
+
+
+def velocity(S: System, u: np.ndarray, A: float) -> np.ndarray:
+    """P_A u = IFFT((G+k+A) FFT(u)/NG) per column (the operator inside ubk_Je, F:306-310)."""
+    GkA = S.Gx[None, :] + S.kx[:, None] + A            # (NK, NG)
+    return fftb(GkA[:, None, :] * fftf(u) / float(S.NG))
+
+
+def hf_vjp(S: System, v: np.ndarray, mu: np.ndarray, A: float) -> np.ndarray:
+    """J^T mu of f(v) = -i h[v](A) v (all bands occupied, NB == NBocc)."""
+    assert S.NB == S.NBocc
+    NK, NB = S.NK, S.NB
+    # kinetic + local + exchange operator at fixed v: (-i h)^T = i h
+    out = 1j * ubkwbk_hwbk(S, v, mu, A)
+    # Hartree: delta vH from delta rho = 2 occ Re(conj(v) dv)
+    sig = np.sum(np.imag(np.conj(mu) * v), axis=(0, 1))
+    psi = dns_vH(S, sig)
+    out += 2.0 * S.occbk[:, :, None] * psi[None, None, :] * v
+    if S.hf:
+        # exchange operator's dependence on v:
+        #   out_i += i sum_j conj(phi_ji) mu_j,  phi_ji = Phi_ji[v_j conj(v_i)]
+        #   out_i += -i sum_j v_j Phi_ij[v_i conj(mu_j)]
+        for ki in range(NK):
+            for bi in range(NB):
+                acc = np.zeros(S.NG, dtype=np.complex128)
+                for kj in range(NK):
+                    for bj in range(NB):
+                        phi_ji = _pair_potential(S, kj, ki, v[kj, bj] * np.conj(v[ki, bi]))
+                        acc += 1j * np.conj(phi_ji) * mu[kj, bj]
+                        acc += -1j * v[kj, bj] * _pair_potential(S, ki, kj, v[ki, bi] * np.conj(mu[kj, bj]))
+                out[ki, bi] += acc
+    return out
+
+
+def _field_grad(S: System, lam_k: np.ndarray, v: np.ndarray, a: float) -> float:
+    """<lam_k, d f/d a>_R with d f / d a = -i P_a v."""
+    return float(np.real(np.sum(np.conj(lam_k) * (-1j) * velocity(S, v, a))))
+
+
+def objective_grad_u(S: System, u: np.ndarray, A: float, objective: str) -> np.ndarray:
+    """Gradient g of the objective w.r.t. u (dL = <g, du>_R)."""
+    if objective == "energy":
+        return 2.0 * S.occbk[:, :, None] * S.dvcell * ubkwbk_hwbk(S, u, u, A)
+    if objective == "current":
+        return -2.0 * S.occbk[:, :, None] * (S.dvcell / S.vcell) * velocity(S, u, A)
+    raise ValueError(objective)
+
+
+def objective_value(S: System, u: np.ndarray, A: float, objective: str, u0: np.ndarray) -> float:
+    if objective == "energy":
+        return ubk_Etot(S, u, A) - ubk_Etot(S, u0, 0.0)
+    return ubk_Je(S, u, A)
+
+
+def objective_dA(S: System, u: np.ndarray, A: float, objective: str) -> float:
+    """Explicit derivative of the objective w.r.t. the final field sample."""
+    if objective == "energy":
+        return -ubk_Je(S, u, A) * S.vcell
+    return -float(np.sum(ubk_dns(S, u)) * S.dvcell) / S.vcell
+
+
+def rt_adjoint(S: System, u0: np.ndarray, A: np.ndarray, dt: float, objective: str = "energy"):
+    """Objective, its gradient w.r.t. every field sample A[n] and w.r.t. vion(x).
+
+    Forward: the RK4 loop of RT:38-42 with Aave[n] = (A[n]+A[n-1])/2, A[-1]=0
+    (RT:227-230), stage fields 2 Aave - A, Aave, Aave, A (RT:165-169).
+    Objective: absorbed energy Etot(u_N, A[N-1]) - Etot(u_0, 0), or the final
+    current Je(u_N, A[N-1]).  Backward: discrete adjoint of every RK4 stage.
+    """
+    A = np.asarray(A, dtype=np.float64)
+    N = A.size
+    Aave = np.empty(N)
+    Aave[0] = 0.5 * (A[0] + 0.0)
+    Aave[1:] = 0.5 * (A[1:] + A[:-1])
+    c = [0.5 * dt, 0.5 * dt, dt]
+    states = [u0.copy()]
+    u = u0.copy()
+    for n in range(N):
+        u = rk4_step(S, u, Aave[n], A[n], dt)
+        states.append(u)
+    L = objective_value(S, u, A[-1], objective, u0)
+    lam = objective_grad_u(S, u, A[-1], objective)
+    gA = np.zeros(N)
+    gA[-1] += objective_dA(S, u, A[-1], objective)
+    gAave = np.zeros(N)
+    gvion = np.zeros(S.NG)
+    if objective == "energy":   # Eion = sum vion rho dvcell at both ends
+        gvion += (ubk_dns(S, u) - ubk_dns(S, u0)) * S.dvcell
+    for n in range(N - 1, -1, -1):
+        un = states[n]
+        Am = 2.0 * Aave[n] - A[n]
+        a = [Am, Aave[n], Aave[n], A[n]]
+        # recompute the stage inputs
+        h = lambda w, f: -1j * ubkwbk_hwbk(S, w, w, f)
+        us = [un]
+        k1 = h(un, a[0])
+        us.append(un + c[0] * k1)
+        k2 = h(us[1], a[1])
+        us.append(un + c[1] * k2)
+        k3 = h(us[2], a[2])
+        us.append(un + c[2] * k3)
+        lam_k = [dt / 6.0 * lam, dt / 3.0 * lam, dt / 3.0 * lam, dt / 6.0 * lam]
+        lam_u = lam.copy()
+        ga = [0.0] * 4
+        for s in range(3, -1, -1):
+            ga[s] = _field_grad(S, lam_k[s], us[s], a[s])
+            gvion += np.sum(np.imag(np.conj(lam_k[s]) * us[s]), axis=(0, 1))
+            lu = hf_vjp(S, us[s], lam_k[s], a[s])
+            lam_u = lam_u + lu
+            if s > 0:
+                lam_k[s - 1] = lam_k[s - 1] + c[s - 1] * lu
+        lam = lam_u
+        # stage fields -> (Aave[n], A[n]) : Am = 2 Aave - A
+        gAave[n] += ga[1] + ga[2] + 2.0 * ga[0]
+        gA[n] += ga[3] - ga[0]
+    # Aave[n] = (A[n] + A[n-1]) / 2
+    gA += 0.5 * gAave
+    gA[:-1] += 0.5 * gAave[1:]
+    return L, gA, gvion

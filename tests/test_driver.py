@@ -1,0 +1,127 @@
+"""Drop-in driver: input parsing, Fortran output formats (CPU) and an end-to-end run (GPU)."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+INPUT = """sys_name
+  'tiny'
+
+acell
+  6.0d0
+
+NB
+  2
+NBocc
+  2
+NG
+  16
+  128
+NK
+  2
+
+Nscf
+  2
+NCG
+  2
+dt
+  0.005
+NT
+  8
+Nomega
+  50
+omegaM
+  2.0
+field_option
+  'LP'
+omegac
+  1.55
+Tpulse
+  0.05
+E0
+  20.0
+nenvelope
+  2
+atoms
+  1             : Nspecies
+  2             : Zeff
+  1.0d0         : alpha
+  1             : Nion
+  0.5d0  1      : Rion, Kion
+"""
+
+
+def test_read_input_first_value_and_atoms(tmp_path):
+    from mattohf_gb300 import read_input
+    from oracle import mattohf_oracle as O
+    p = tmp_path / "input.dat"
+    p.write_text(INPUT)
+    cfg = read_input(str(p))
+    assert (cfg.NG, cfg.NK, cfg.NB, cfg.NBocc, cfg.NT) == (16, 2, 2, 2, 8)   # first value only
+    assert cfg.sys_name == "tiny" and cfg.field_option == "LP"
+    assert cfg.Zeff == [2.0] and cfg.Rion == [0.5] and cfg.Kion == [1]
+    o = O.read_input(str(p))
+    for k in ("acell", "NG", "NK", "NB", "NBocc", "Nscf", "NCG", "dt", "NT", "Nomega", "omegaM",
+              "omegac", "Tpulse", "E0", "nenvelope", "Zeff", "alpha", "Rion", "Kion", "sys_name"):
+        assert getattr(cfg, k) == getattr(o, k), k
+
+
+def test_fortran_e_format():
+    from mattohf_gb300.driver import fortran_e
+    assert fortran_e(1.0) == "  0.100000000000E+01"
+    assert fortran_e(-0.00123456789012345) == " -0.123456789012E-02"
+    assert fortran_e(0.0) == "  0.000000000000E+00"
+    assert fortran_e(9.9999999999999e5) == "  0.100000000000E+07"
+    assert fortran_e(1.5e123) == "  0.150000000000+124"
+    assert fortran_e(2.5, e=3) == " 0.250000000000E+001"
+
+
+def test_define_afield_matches_oracle():
+    from mattohf_gb300 import RunConfig, define_afield
+    from oracle import mattohf_oracle as O
+    import dataclasses
+    cfg = RunConfig(NT=300, dt=0.05, field_option="LP", omegac=1.55, Tpulse=5.0, E0=2.0, nenvelope=4,
+                    phiCEP=0.3)
+    t, A, Aave, E = define_afield(cfg)
+    ot, oA, oAave, oE, _ = O.define_afield(O.Config(**{f.name: getattr(cfg, f.name) for f in dataclasses.fields(O.Config)}))
+    assert np.array_equal(A, oA) and np.array_equal(Aave, oAave) and np.array_equal(E, oE)
+
+
+@pytest.mark.gpu
+def test_driver_end_to_end(tmp_path, built_lib):
+    from mattohf_gb300 import read_input
+    from mattohf_gb300.driver import run
+    p = tmp_path / "input.dat"
+    p.write_text(INPUT)
+    cfg = read_input(str(p))
+    res = run(cfg, out_dir=str(tmp_path), log=lambda *a: None)
+    for f in ("potential.out", "vk.out", "tiny_GSinfo.out", "tiny_DoS.out", "tiny_band.out",
+              "tiny_EtotNJEAt.out", "tiny_JEAF.out", "tiny_JEAF_window.out"):
+        assert os.path.exists(tmp_path / f), f
+    rows = [l for l in open(tmp_path / "tiny_EtotNJEAt.out") if not l.startswith("#")]
+    assert len(rows) == cfg.NT and len(rows[0]) == 8 * 20 + 1
+    vals = np.array([[float(l[i * 20:(i + 1) * 20].replace("E", "e")) for i in range(8)] for l in rows])
+    assert np.allclose(vals[:, 1], res["Etot"], rtol=1e-11, atol=0)
+
+
+@pytest.mark.gpu
+def test_fourier_matches_oracle(built_lib):
+    from mattohf_gb300 import RunConfig
+    from mattohf_gb300.driver import fourier
+    from oracle import mattohf_oracle as O
+    import dataclasses
+    cfg = RunConfig(dt=0.1, NT=400, Nomega=64, omegaM=3.0, field_option="LP", Tpulse=5.0)
+    rng = np.random.default_rng(0)
+    t = cfg.dt * np.arange(cfg.NT)
+    J, E, A = rng.standard_normal((3, cfg.NT))
+    oc = O.Config(**{f.name: getattr(cfg, f.name) for f in dataclasses.fields(O.Config)})
+    w, JF, EF, AF, _, _ = O.fourier_tr(oc, t, J, 0.3, E, A)
+    ft = fourier(cfg, t, J, 0.3, E, A, window=False)
+    assert np.allclose(ft[:, 0], w, rtol=1e-15)
+    for col, ref in ((1, JF), (3, EF), (5, AF)):
+        assert np.max(np.abs(ft[:, col] + 1j * ft[:, col + 1] - ref)) <= 1e-12 * np.max(np.abs(ref))
+    w2, JF2, _, _ = O.window_fourier_tr(oc, t, J, 0.3, E, A)
+    fw = fourier(cfg, t, J, 0.3, E, A, window=True)
+    assert np.max(np.abs(fw[:, 1] + 1j * fw[:, 2] - JF2)) <= 1e-12 * np.max(np.abs(JF2))

@@ -1,0 +1,62 @@
+"""Adjoint gradient on the GPU vs the oracle's discrete adjoint and vs finite differences."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfg(**kw):
+    from mattohf_gb300 import RunConfig
+    base = dict(acell=8.0, NG=32, NK=4, NB=2, NBocc=2, Zeff=[2.0], alpha=[1.0], Rion=[0.5], Kion=[1])
+    base.update(kw)
+    return RunConfig(**base)
+
+
+@pytest.mark.parametrize("objective", ["energy", "current"])
+@pytest.mark.parametrize("ckpt", [0, 2])
+def test_adjoint_matches_oracle(built_lib, objective, ckpt):
+    from mattohf_gb300 import Context
+    from oracle import mattohf_oracle as O
+    from conftest import to_oracle_config
+    cfg = _cfg()
+    S = O.make_system(to_oracle_config(cfg))
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    rng = np.random.default_rng(4)
+    A = 0.05 * rng.standard_normal(5)
+    dt = 0.004
+    Lr, gr, gvr = O.rt_adjoint(S, u0, A, dt, objective)
+    with Context(cfg) as ctx:
+        ctx.set_orbitals(u0)
+        L, g, gv = ctx.adjoint(A, dt, objective, ckpt_every=ckpt)
+    assert abs(L - Lr) <= 1e-10 * max(1.0, abs(Lr))
+    assert np.max(np.abs(g - gr)) <= 1e-9 * np.max(np.abs(gr))
+    assert np.max(np.abs(gv - gvr)) <= 1e-9 * np.max(np.abs(gvr))
+
+
+def test_adjoint_finite_differences_gpu(built_lib):
+    """Central differences (h = 1e-6) of the GPU objective on random samples agree to 1e-6."""
+    from mattohf_gb300 import Context
+    cfg = _cfg(NG=64, NK=4, NB=2, NBocc=2, acell=10.0)
+    rng = np.random.default_rng(5)
+    nt = 24
+    A = 0.05 * np.sin(0.3 * np.arange(nt)) + 1e-3 * rng.standard_normal(nt)
+    dt = 0.004
+    with Context(cfg) as ctx:
+        ctx.Init_wf()
+        ctx.Gram_Schmidt()
+        u0 = ctx.get_orbitals()
+        L, g, _ = ctx.adjoint(A, dt, "energy", ckpt_every=5)
+
+        def obj(Ax):
+            ctx.set_orbitals(u0)
+            return ctx.adjoint(Ax, dt, "energy", ckpt_every=nt)[0]
+
+        h = 1e-6
+        for n in rng.choice(nt, size=6, replace=False):
+            Ap, Am = A.copy(), A.copy()
+            Ap[n] += h
+            Am[n] -= h
+            fd = (obj(Ap) - obj(Am)) / (2 * h)
+            assert abs(g[n] - fd) <= 1e-6 * np.max(np.abs(g)) + 2e-10, (n, g[n], fd)

@@ -1,0 +1,67 @@
+"""Batched ensemble vs the same runs advanced one at a time (needs a GB300)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfgs():
+    from mattohf_gb300 import RunConfig
+    out = []
+    rng = np.random.default_rng(1)
+    for nk, nb in [(2, 1), (4, 2), (8, 3), (4, 4), (2, 2)]:
+        a = float(rng.uniform(8.0, 14.0))
+        out.append(RunConfig(acell=a, NG=64, NK=nk, NB=nb, NBocc=nb, Zeff=[2.0], alpha=[1.0],
+                             Rion=[0.5], Kion=[1]))
+    return out
+
+
+def test_batch_matches_single_runs(built_lib):
+    from mattohf_gb300 import Batch, Context
+    cfgs = _cfgs()
+    nt = 4
+    rng = np.random.default_rng(2)
+    A = 0.02 * rng.standard_normal((len(cfgs), nt))
+    Aave = np.concatenate([0.5 * A[:, :1], 0.5 * (A[:, 1:] + A[:, :-1])], axis=1)
+    dts = np.array([0.004, 0.003, 0.002, 0.004, 0.005])
+    with Batch(cfgs) as b:
+        u0 = []
+        for r in range(len(cfgs)):
+            b[r].Init_wf()
+            b[r].Gram_Schmidt()
+            u0.append(b[r].get_orbitals())
+        E, J, N = b.rk4_run(A, Aave, dts)
+        ub = [b[r].get_orbitals() for r in range(len(cfgs))]
+    for r, cfg in enumerate(cfgs):
+        with Context(cfg) as c:
+            c.set_orbitals(u0[r])
+            e, j, n = c.rk4_run(A[r], Aave[r], dts[r])
+            us = c.get_orbitals()
+        assert np.array_equal(e, E[r]), r
+        assert np.array_equal(j, J[r]), r
+        assert np.array_equal(n, N[r]), r
+        assert np.array_equal(us, ub[r]), r
+
+
+def test_batch_against_oracle(built_lib):
+    """One member of a mixed batch against the oracle's RT loop."""
+    from mattohf_gb300 import Batch
+    from oracle import mattohf_oracle as O
+    from conftest import to_oracle_config
+    cfgs = _cfgs()
+    nt = 3
+    A = np.tile(np.array([0.01, 0.02, 0.015]), (len(cfgs), 1))
+    Aave = np.concatenate([0.5 * A[:, :1], 0.5 * (A[:, 1:] + A[:, :-1])], axis=1)
+    with Batch(cfgs) as b:
+        for r in range(len(cfgs)):
+            b[r].Init_wf()
+            b[r].Gram_Schmidt()
+        u2 = b[2].get_orbitals()
+        E, J, N = b.rk4_run(A, Aave, 0.003)
+    import dataclasses
+    S = O.make_system(to_oracle_config(dataclasses.replace(cfgs[2], dt=0.003)))
+    ref = O.rt_calculation(S, u2, nt=nt, A=A[2], Aave=Aave[2])
+    assert np.max(np.abs(E[2] - ref.Etot)) <= 1e-10 * np.max(np.abs(ref.Etot))
+    assert np.max(np.abs(J[2] - ref.Jtot)) <= 1e-10

@@ -141,7 +141,7 @@ def test_fock_kinetic_density(name):
     w = rand_orbs(S, 4, nb=S.NB + 1)  # a Krylov-like block with another band count
     assert rel(ctx.ubkwbk_vFwbk(u, w), O.ubkwbk_vFwbk(S, u, w)) <= TOL_OP
     assert rel(ctx.ubk_tubk(w, -0.2), O.ubk_tubk(S, w, -0.2)) <= TOL_OP
-    assert rel(ctx.ubk_dns(u), O.ubk_dns(S, u)) <= 1e-14
+    assert rel(ctx.ubk_dns(u), O.ubk_dns(S, u)) <= 1e-13
     assert rel(ctx.dns_vH_of(u), O.dns_vH(S, O.ubk_dns(S, u))) <= TOL_OP
 
 

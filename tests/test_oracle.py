@@ -176,3 +176,32 @@ def test_c_port_matches_numpy_oracle():
         assert np.max(np.abs(uu - rt.ubk)) < 1e-11
     finally:
         lib.cref_destroy(h)
+
+
+@pytest.mark.parametrize("objective", ["energy", "current"])
+def test_oracle_adjoint_matches_finite_differences(objective):
+    """Discrete RK4 adjoint of the oracle vs central differences (h = 1e-6)."""
+    cfg = small(NG=16, NK=2, NB=2, NBocc=2, acell=6.0)
+    S = O.make_system(cfg)
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    rng = np.random.default_rng(3)
+    A = 0.05 * rng.standard_normal(4)
+    dt = 0.01
+    L, g, gv = O.rt_adjoint(S, u0, A, dt, objective)
+    h = 1e-6
+    for n in range(A.size):
+        Ap, Am = A.copy(), A.copy()
+        Ap[n] += h
+        Am[n] -= h
+        fd = (O.rt_adjoint(S, u0, Ap, dt, objective)[0] - O.rt_adjoint(S, u0, Am, dt, objective)[0]) / (2 * h)
+        assert abs(g[n] - fd) <= 1e-6 * np.max(np.abs(g)) + 1e-12
+    # ion potential on the grid
+    for x in (0, 5):
+        vp = S.vion.copy()
+        S.vion = vp.copy(); S.vion[x] += h
+        Lp = O.rt_adjoint(S, u0, A, dt, objective)[0]
+        S.vion = vp.copy(); S.vion[x] -= h
+        Lm = O.rt_adjoint(S, u0, A, dt, objective)[0]
+        S.vion = vp
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(gv[x] - fd) <= 1e-5 * np.max(np.abs(gv)) + 1e-9  # FD round-off ~ 1e-16*|E|/h
