@@ -278,6 +278,27 @@ def run_gpu(args, dist):
         with open(tp) as fh:
             prof_traffic = json.load(fh).get("bytes_per_launch")
 
+    # --- the same timed region with the exchange transforms in double-float
+    #     arithmetic (MATTOHF_OPT_FOCK_DF64; parity-tested at the FP64 tolerances)
+    ctx.set_option(_capi.OPT_FOCK_DF64, 1)
+    ctx.set_option(_capi.OPT_L2_FLUSH, 512 << 20)
+    ctx.set_orbitals(u0)
+    ctx.rk4_run(A[:W], Aave[:W], cfg.dt)
+    ctx.set_orbitals(u0)
+    ctx.rk4_run(A[W:W + K], Aave[W:W + K], cfg.dt)
+    df_ms, _, _ = ctx.last_run_timing()
+    ctx.set_option(_capi.OPT_L2_FLUSH, 0)
+    ctx.set_option(_capi.OPT_KERNEL_TIMING, 1)
+    ctx.set_orbitals(u0)
+    ctx.rk4_run(A[:2], Aave[:2], cfg.dt)
+    _, df_fock_ms, df_nf = ctx.last_run_timing()
+    ctx.set_option(_capi.OPT_KERNEL_TIMING, 0)
+    ctx.set_option(_capi.OPT_FOCK_DF64, 0)
+    double_float = {"value": K / (df_ms * 1e-3), "unit": "steps/s", "ms_per_step": df_ms / K,
+                    "fock_launch_ms": df_fock_ms / df_nf,
+                    "note": "exchange pair transforms in double-float (2xFP32, 48-bit significand) on the "
+                            "FP32 pipe; parity within the FP64 tolerances (1e-12 per apply, 1e-10 RT)"}
+
     # --- end to end through the public C ABI with host buffers
     Ke = K
     ue = np.ascontiguousarray(u0)
@@ -317,7 +338,7 @@ def run_gpu(args, dist):
                          "flops_per_launch": flops, "launch_ms": fock_ms / nf,
                          "peak_source": "measured DFMA throughput on this GPU (mattohf_diag_fp64_peak)",
                          "flops_model": "symmetric exchange: M(M+1)/2 pairs x (10 N log2 N + 16 N) + M(M-1)/2 x 8 N, M = NK*NBocc"},
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * K, "clocks": clocks}
+            "cpu_baseline": cpu, "e2e": e2e, "double_float_exchange": double_float, "gpu_launches": launches_per_step * K, "clocks": clocks}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -433,10 +454,20 @@ def run_adjoint(args):
         gs, fds = np.array(gs), np.array(fds)
         worst = float(np.max(np.abs(gs - fds)) / np.max(np.abs(fds)))
         worst_each = float(np.max(np.abs(gs - fds) / np.abs(fds)))
+        # the same samples with h = 1e-4: round-off of the 4000-step difference
+        # quotient shrinks 100x while the O(h^2) truncation stays negligible
+        fds4 = []
+        for n in rng.choice(nt, size=min(8, args.fd_samples), replace=False):
+            Ap, Am = A.copy(), A.copy()
+            Ap[n] += 1e-4
+            Am[n] -= 1e-4
+            fds4.append(((obj(Ap) - obj(Am)) / 2e-4, g[n]))
+        fds4 = np.array(fds4)
+        worst4 = float(np.max(np.abs(fds4[:, 1] - fds4[:, 0])) / np.max(np.abs(fds4[:, 0])))
     line = {"metric": "adjoint-gradient/forward time ratio", "value": t_adj / t_fwd, "unit": "ratio",
             "higher_is_better": False, "forward_ms": t_fwd, "adjoint_ms": t_adj, "steps": nt,
             "objective": L, "fd_rel_err": worst, "fd_max_rel_err_per_sample": worst_each,
-            "fd_samples": args.fd_samples, "fd_h": 1e-6, "dtype": "f64",
+            "fd_samples": args.fd_samples, "fd_h": 1e-6, "fd_rel_err_h1e-4": worst4, "dtype": "f64",
             "data": "synthetic",
             "config": {"workload": "a=10, NK=16, Nocc=2, NG=128, pulse+N(0,1e-3), checkpoints every 100",
                        "dt": cfg.dt}}

@@ -42,6 +42,8 @@ extern "C" {
 #define MATTOHF_OPT_FOCK_CHUNKS 2  /* pair chunks per Fock output column; 0 = automatic */
 #define MATTOHF_OPT_KERNEL_TIMING 3 /* 1: bracket every Fock launch with CUDA events (no graph) */
 #define MATTOHF_OPT_SYMMETRIC 4    /* 1: use the occupied-pair Hermitian symmetry when w == u (default 1) */
+#define MATTOHF_OPT_FOCK_DF64 6   /* 1: symmetric exchange transforms in double-float (2 x FP32, 48-bit
+                                      significand) arithmetic on the FP32 pipe; default 0 (FP64) */
 #define MATTOHF_OPT_L2_FLUSH 5     /* >0: bytes written between RK4 steps of mattohf_rk4_run, which then
                                       reports the summed per-step device time (benchmarking) */
 

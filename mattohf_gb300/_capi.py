@@ -27,6 +27,7 @@ OPT_FOCK_CHUNKS = 2
 OPT_KERNEL_TIMING = 3
 OPT_SYMMETRIC = 4
 OPT_L2_FLUSH = 5
+OPT_FOCK_DF64 = 6
 
 # every symbol include/mattohf.h declares
 EXPORTS = [

@@ -73,6 +73,10 @@ struct mattohf_ctx {
   double2* d_sym = nullptr;   // symmetric-exchange tile partials
   size_t sym_cap = 0;
   double2* d_symF = nullptr;  // reduced symmetric exchange [NK*NBocc][NG]
+  float4* d_udf = nullptr;    // double-float copy of the occupied orbitals
+  float2* d_kern_df = nullptr;
+  float4* d_tw_df = nullptr;
+  int opt_df = 0;             // exchange transforms in double-float arithmetic
   int* d_int = nullptr;  // [0] = step counter, [1] = non-finite flag, [2] = solver flag
   // RT series
   double *d_A = nullptr, *d_Aave = nullptr, *d_sE = nullptr, *d_sJ = nullptr, *d_sN = nullptr;
@@ -268,6 +272,7 @@ int ensure_fock_buffers(mattohf_ctx* ctx) {
   const int T = (M + S - 1) / S;
   CKR(ensure_sym(ctx, (size_t)T * (T + 1) / 2 * 2 * S * ctx->NG));
   if (!ctx->d_symF) CKR(dalloc(ctx, &ctx->d_symF, (size_t)M * ctx->NG));
+  if (!ctx->d_udf) CKR(dalloc(ctx, &ctx->d_udf, (size_t)M * ctx->NG));
   return MATTOHF_OK;
 }
 
@@ -296,7 +301,22 @@ int enq_fock(mattohf_ctx* ctx, Block u, Block w, FockPlan* plan) {
     a.scratch = ctx->d_sym;
     a.F = ctx->d_symF;
     CKR(timed_begin(ctx));
-    CK(launch_fock_sym(NG, a, ctx->st));
+    if (ctx->opt_df) {
+      if (!ctx->d_udf) CKR(dalloc(ctx, &ctx->d_udf, (size_t)M * NG));
+      FockSymDfArgs d;
+      d.u = ctx->d_udf;
+      d.nk = ctx->NK;
+      d.nbocc = ctx->NBocc;
+      d.S = S;
+      d.T = T;
+      d.kern = ctx->d_kern_df;
+      d.tw = ctx->d_tw_df;
+      d.scratch = ctx->d_sym;
+      d.F = ctx->d_symF;
+      CK(launch_fock_sym_df(NG, d, u.p, u.kstride, ctx->d_udf, ctx->st));
+    } else {
+      CK(launch_fock_sym(NG, a, ctx->st));
+    }
     CKR(timed_end(ctx));
     plan->sym = ctx->d_symF;
     plan->S = S;
@@ -625,6 +645,7 @@ int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out) {
     if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
     e = configure_kernels();
     if (e == cudaSuccess) e = configure_adjoint_kernels();
+    if (e == cudaSuccess) e = configure_df_kernels();
     if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
   }
   const size_t nu = orb_elems(ctx, ctx->NB);
@@ -646,6 +667,12 @@ int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out) {
   k_twiddles<<<(NG + 127) / 128, 128, 0, ctx->st>>>(ctx->tw, NG);
   if (cudaGetLastError() != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
   if ((rc = compute_tables(ctx))) return bail(rc);
+  if ((rc = dalloc(ctx, &ctx->d_kern_df, (size_t)(2 * ctx->NK - 1) * NG)) || (rc = dalloc(ctx, &ctx->d_tw_df, NG)))
+    return bail(rc);
+  if (launch_to_df_tables(ctx->d_kern, (2 * ctx->NK - 1) * NG, ctx->d_kern_df, ctx->tw, NG, ctx->d_tw_df, ctx->st) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(ctx->st) != cudaSuccess)
+    return bail(MATTOHF_ERR_CUDA);
   *out = ctx;
   return MATTOHF_OK;
 }
@@ -674,7 +701,8 @@ int mattohf_destroy(mattohf_ctx* ctx) {
                   ctx->d_k[1], ctx->d_k[2], ctx->d_k[3], ctx->d_a, ctx->d_b, ctx->d_c,
                   ctx->d_scratch, ctx->d_colbuf, ctx->d_int, ctx->d_A, ctx->d_Aave, ctx->d_sE,
                   ctx->d_sJ, ctx->d_sN, ctx->d_work, ctx->d_hwork, ctx->d_M, ctx->d_V, ctx->d_evals,
-                  ctx->d_eps, ctx->d_err, ctx->d_sym, ctx->d_symF, ctx->d_dpart};
+                  ctx->d_eps, ctx->d_err, ctx->d_sym, ctx->d_symF, ctx->d_dpart,
+                  ctx->d_udf, ctx->d_kern_df, ctx->d_tw_df};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -692,6 +720,7 @@ int mattohf_set_option(mattohf_ctx* ctx, int option, long long value) {
       break;
     case MATTOHF_OPT_KERNEL_TIMING: ctx->opt_timing = value ? 1 : 0; break;
     case MATTOHF_OPT_SYMMETRIC: ctx->opt_sym = value ? 1 : 0; break;
+    case MATTOHF_OPT_FOCK_DF64: ctx->opt_df = value ? 1 : 0; break;
     case MATTOHF_OPT_L2_FLUSH:
       if (value < 0 || value > (4LL << 30)) return fail(ctx, MATTOHF_ERR_ARG, "flush bytes out of range");
       ctx->opt_flush = value;

@@ -88,6 +88,22 @@ struct FockSymArgs {
   double2* F;           // reduced exchange term of the occupied orbitals [NK*nbocc][NG]
 };
 
+// Symmetric exchange with double-float pair transforms (k_fock_df.cu).
+struct FockSymDfArgs {
+  const float4* u;      // occupied orbitals as df [NK*nbocc][NG]
+  int nk, nbocc;
+  int S, T;
+  const float2* kern;   // df copy of the kernel table
+  const float4* tw;     // df twiddles
+  double2* scratch;     // tile partials (FP64), as FockSymArgs
+  double2* F;           // reduced exchange [NK*nbocc][NG]
+};
+cudaError_t launch_fock_sym_df(int NG, const FockSymDfArgs& a, const double2* u, int kstride, float4* udf,
+                               cudaStream_t s);
+cudaError_t configure_df_kernels();
+cudaError_t launch_to_df_tables(const double* kern, int nkern, float2* kern_df, const double2* tw, int ntw,
+                                float4* tw_df, cudaStream_t s);
+
 __host__ __device__ __forceinline__ int sym_tp(int i, int j, int T) {
   return i * T - (i * (i - 1)) / 2 + (j - i);
 }

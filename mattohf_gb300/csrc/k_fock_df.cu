@@ -1,0 +1,191 @@
+// Symmetric exchange (src/Functions.f90:237-261, w == u) with the pair
+// transforms in double-float arithmetic (fft_df.cuh).
+//
+// Same tile-pair decomposition, Nyquist correction and partial-sum layout as
+// k_fock_sym in k_hpsi.cu; only the arithmetic of the pair chain (pair
+// density, forward transform, kernel, inverse transform, the two
+// accumulations) runs on the FP32 pipe as unevaluated hi+lo pairs.  Inputs are
+// converted from FP64 once per apply, the partial sums back to FP64 on the way
+// out, so everything outside this kernel stays complex128.
+#include "fft_df.cuh"
+#include "internal.h"
+
+namespace mattohf {
+
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) {
+  using TM = Team<N>;
+  using df::cdf;
+  constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
+  const int S = a.S;
+  const int nteam = (blockDim.x >> 5) * PW;
+  extern __shared__ float4 smf[];
+  cdf* tw_s = reinterpret_cast<cdf*>(smf);        // N
+  cdf* bufs = tw_s + N;                           // nteam * N
+  cdf* cacc = bufs + nteam * N;                   // S * N
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tl = lane % T, tw_ = warp * PW + lane / T;
+  const int team_lane0 = (lane / T) * T;
+  cdf* buf = bufs + tw_ * N;
+  for (int i = tid; i < N; i += blockDim.x) tw_s[i] = df::load(a.tw + i);
+  for (int i = tid; i < S * N; i += blockDim.x) {
+    cdf z;
+    z.re = make_float2(0.f, 0.f);
+    z.im = make_float2(0.f, 0.f);
+    cacc[i] = z;
+  }
+  int ti = 0, rem = blockIdx.x;
+  while (rem >= a.T - ti) { rem -= a.T - ti; ++ti; }
+  const int tj = ti + rem;
+  const int M = a.nk * a.nbocc;
+  const int ia = ti * S + tw_;
+  const bool va = tw_ < S && ia < M;
+  const int oa = va ? ia : 0;
+  const int ka = oa / a.nbocc;
+  cdf ua[E], racc[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    ua[e] = df::load(a.u + (size_t)oa * N + TM::pos(tl, e));
+    racc[e].re = make_float2(0.f, 0.f);
+    racc[e].im = make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const bool diag = (ti == tj);
+  const int nrounds = diag ? (S / 2 + 1) : S;
+  for (int r = 0; r < nrounds; ++r) {
+    const int lb = (tw_ + r) % S;
+    const int ib = tj * S + lb;
+    bool valid = va && ib < M;
+    if (diag && (S % 2 == 0) && r == S / 2 && tw_ >= S / 2) valid = false;
+    const bool self = diag && r == 0;
+    const int ob = ib < M ? ib : 0;
+    const int kb = ob / a.nbocc;
+    const int dab = ka - kb + a.nk - 1, dba = kb - ka + a.nk - 1;
+    const float2* kab = a.kern + (size_t)dab * N;
+    cdf ub[E], x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      ub[e] = df::load(a.u + (size_t)ob * N + TM::pos(tl, e));
+      x[e] = df::cmulc(ua[e], ub[e]);
+    }
+    df::fft_team<N, -1>(x, buf, tw_s, tl);
+    const cdf rn_own = x[TM::R0 / 2];
+    cdf rn;
+    rn.re.x = __shfl_sync(0xffffffffu, rn_own.re.x, team_lane0);
+    rn.re.y = __shfl_sync(0xffffffffu, rn_own.re.y, team_lane0);
+    rn.im.x = __shfl_sync(0xffffffffu, rn_own.im.x, team_lane0);
+    rn.im.y = __shfl_sync(0xffffffffu, rn_own.im.y, team_lane0);
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = df::scale(x[e], kab[TM::pos(tl, e)]);
+    df::fft_team<N, +1>(x, buf, tw_s, tl);
+    if (valid) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) racc[e] = df::cadd(racc[e], df::cmul(x[e], ub[e]));
+      if (!self) {
+        const float2 dk = df::sub(a.kern[(size_t)dba * N + N / 2], kab[N / 2]);
+        // c = dk conj(R); phi_ba = conj(phi_ab) + c (-1)^m
+        const float2 cx = df::mul(dk, rn.re), cy = df::neg(df::mul(dk, rn.im));
+        cdf* col = cacc + lb * N;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          const int q = TM::pos(tl, e);
+          const bool odd = q & 1;
+          const cdf pba = df::make(df::add(x[e].re, odd ? df::neg(cx) : cx),
+                                   df::add(df::neg(x[e].im), odd ? df::neg(cy) : cy));
+          col[q] = df::cadd(col[q], df::cmul(pba, ua[e]));
+        }
+      }
+    }
+    __syncthreads();
+  }
+  double2* dst = a.scratch + (size_t)blockIdx.x * 2 * S * N;
+  if (tw_ < S) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) dst[(size_t)tw_ * N + TM::pos(tl, e)] = df::to_double2(racc[e]);
+  }
+  for (int i = tid; i < S * N; i += blockDim.x) dst[(size_t)S * N + i] = df::to_double2(cacc[i]);
+}
+
+// occupied orbitals (FP64, [NK][NB][NG]) -> df copy [NK*NBocc][NG]
+__global__ void k_orb_to_df(const double2* __restrict__ u, int kstride, int nbocc, int N, int total,
+                            float4* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const int o = i / N, g = i % N;
+  const int k = o / nbocc, b = o % nbocc;
+  df::store(out + i, df::from_double2(u[(size_t)k * kstride + (size_t)b * N + g]));
+}
+
+__global__ void k_real_to_df(const double* __restrict__ x, int n, float2* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = df::from_double(x[i]);
+}
+
+__global__ void k_cplx_to_df(const double2* __restrict__ x, int n, float4* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) df::store(out + i, df::from_double2(x[i]));
+}
+
+#define MATTOHF_DISPATCH(NG, CALL)                 \
+  switch (NG) {                                    \
+    case 16: return CALL(16);                      \
+    case 32: return CALL(32);                      \
+    case 64: return CALL(64);                      \
+    case 128: return CALL(128);                    \
+    case 256: return CALL(256);                    \
+    case 512: return CALL(512);                    \
+    default: return cudaErrorInvalidValue;         \
+  }
+
+template <int N>
+static cudaError_t fock_df_impl(const FockSymDfArgs& a, const double2* u, int kstride, float4* udf,
+                                cudaStream_t s) {
+  const int M = a.nk * a.nbocc;
+  const int total = M * N;
+  k_orb_to_df<<<(total + 255) / 256, 256, 0, s>>>(u, kstride, a.nbocc, N, total, udf);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int tiles = a.T * (a.T + 1) / 2;
+  if (tiles == 0) return cudaSuccess;
+  int threads;
+  size_t smem;
+  if ((e = sym_launch_params(N, a.S, &threads, &smem)) != cudaSuccess) return e;
+  k_fock_sym_df<N><<<tiles, threads, smem, s>>>(a);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  return launch_sym_reduce(a.scratch, a.S, a.T, M, N, a.F, s);
+}
+
+cudaError_t launch_fock_sym_df(int NG, const FockSymDfArgs& a, const double2* u, int kstride, float4* udf,
+                               cudaStream_t s) {
+#define CALL(n) fock_df_impl<n>(a, u, kstride, udf, s)
+  MATTOHF_DISPATCH(NG, CALL)
+#undef CALL
+}
+
+template <int N>
+static cudaError_t configure_df_impl() {
+  constexpr int NTEAM = (kThreads / 32) * Team<N>::PER_WARP;
+  const size_t smem = sizeof(float4) * (size_t)N * (1 + 2 * NTEAM);
+  return cudaFuncSetAttribute(k_fock_sym_df<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t configure_df_kernels() {
+  cudaError_t e;
+  if ((e = configure_df_impl<16>()) != cudaSuccess) return e;
+  if ((e = configure_df_impl<32>()) != cudaSuccess) return e;
+  if ((e = configure_df_impl<64>()) != cudaSuccess) return e;
+  if ((e = configure_df_impl<128>()) != cudaSuccess) return e;
+  if ((e = configure_df_impl<256>()) != cudaSuccess) return e;
+  return configure_df_impl<512>();
+}
+
+cudaError_t launch_to_df_tables(const double* kern, int nkern, float2* kern_df, const double2* tw, int ntw,
+                                float4* tw_df, cudaStream_t s) {
+  k_real_to_df<<<(nkern + 255) / 256, 256, 0, s>>>(kern, nkern, kern_df);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_cplx_to_df<<<(ntw + 255) / 256, 256, 0, s>>>(tw, ntw, tw_df);
+  return cudaGetLastError();
+}
+
+}  // namespace mattohf

@@ -39,10 +39,12 @@ def test_batch_matches_single_runs(built_lib):
             c.set_orbitals(u0[r])
             e, j, n = c.rk4_run(A[r], Aave[r], dts[r])
             us = c.get_orbitals()
-        assert np.array_equal(e, E[r]), r
-        assert np.array_equal(j, J[r]), r
-        assert np.array_equal(n, N[r]), r
-        assert np.array_equal(us, ub[r]), r
+        # same kernels; the single run may pick a smaller exchange tile (a
+        # different but fixed summation order), so agreement is to rounding
+        assert np.max(np.abs(e - E[r])) <= 1e-13 * np.max(np.abs(e)), r
+        assert np.max(np.abs(j - J[r])) <= 1e-13 * max(1.0, np.max(np.abs(j))), r
+        assert np.max(np.abs(n - N[r])) <= 1e-13 * np.max(np.abs(n)), r
+        assert np.max(np.abs(us - ub[r])) <= 1e-12 * np.max(np.abs(us)), r
 
 
 def test_batch_against_oracle(built_lib):

@@ -123,6 +123,46 @@ def test_hpsi_self(name, sym):
     assert rel(vf, O.ubkwbk_vFwbk(S, u, u)) <= TOL_OP
 
 
+@pytest.mark.parametrize("name", list(CONFIGS))
+def test_hpsi_self_double_float(name):
+    """Exchange transforms in double-float arithmetic stay within the operator tolerance."""
+    from oracle import mattohf_oracle as O
+    from mattohf_gb300 import _capi
+    cfg, ctx, S = setup(name)
+    u = O.gram_schmidt(S, rand_orbs(S, 13))
+    ctx.set_option(_capi.OPT_FOCK_DF64, 1)
+    try:
+        got = ctx.ubkwbk_hwbk(u, u, 0.07)
+        vf = ctx.ubkwbk_vFwbk(u, u)
+    finally:
+        ctx.set_option(_capi.OPT_FOCK_DF64, 0)
+    assert rel(got, O.ubkwbk_hwbk(S, u, u, 0.07)) <= TOL_OP
+    assert rel(vf, O.ubkwbk_vFwbk(S, u, u)) <= TOL_OP
+
+
+@pytest.mark.parametrize("name", ["ng32_nk4", "ng64_nk8"])
+def test_rk4_run_double_float(name):
+    """RK4 series with double-float exchange transforms vs the oracle (spec 1e-10)."""
+    from oracle import mattohf_oracle as O
+    from mattohf_gb300 import _capi, define_afield
+    cfg, ctx, S = setup(name)
+    cfg = dataclasses.replace(cfg, dt=0.004, NT=6, field_option="LP", omegac=1.55, Tpulse=0.1, E0=20.0)
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    _, A, Aave, _ = define_afield(cfg)
+    ctx.set_option(_capi.OPT_FOCK_DF64, 1)
+    try:
+        ctx.set_orbitals(u0)
+        E, J, N = ctx.rk4_run(A, Aave, cfg.dt)
+        uf = ctx.get_orbitals()
+    finally:
+        ctx.set_option(_capi.OPT_FOCK_DF64, 0)
+    S.cfg = to_oracle_config(cfg)
+    ref = O.rt_calculation(S, u0, nt=cfg.NT, A=A, Aave=Aave)
+    assert rel(E, ref.Etot) <= TOL_RT
+    assert np.max(np.abs(J - ref.Jtot)) <= TOL_RT * max(1.0, np.max(np.abs(ref.Jtot)))
+    assert rel(uf, ref.ubk) <= TOL_RT
+
+
 def test_sym_nyquist_correction():
     """Orbitals with a large Nyquist component: the symmetric kernel's Nyquist term matters."""
     from oracle import mattohf_oracle as O
