@@ -486,14 +486,18 @@ def main():
     ap.add_argument("--runs", type=int, default=256)
     ap.add_argument("--adj-steps", type=int, default=4000)
     ap.add_argument("--fd-samples", type=int, default=32)
+    ap.add_argument("--profile-df", action="store_true",
+                    help="with --profile-case: double-float exchange transforms")
     ap.add_argument("--profile-case", action="store_true",
                     help="small profiling case: 3 applies of h[u]u on the workload (no timing)")
     args = ap.parse_args()
     if args.profile_case:
-        from mattohf_gb300 import build, Context
+        from mattohf_gb300 import build, Context, _capi
         build.build()
         cfg = make_cfg()
         with Context(cfg) as ctx:
+            if args.profile_df:
+                ctx.set_option(_capi.OPT_FOCK_DF64, 1)
             rng = np.random.default_rng(0)
             u = rng.standard_normal((cfg.NK, cfg.NB, cfg.NG)) + 1j * rng.standard_normal((cfg.NK, cfg.NB, cfg.NG))
             for _ in range(3):

@@ -7,6 +7,7 @@ namespace mattohf {
 
 constexpr int kThreads = 128;  // threads per CTA for the column/pair kernels (4 warps)
 constexpr int kDensChunks = 32; // column chunks of the two-stage density reduction
+constexpr int kCombineWarps = 1; // warps per CTA of the per-column combine kernels (spread over SMs)
 
 // How a kernel obtains the vector potential of the current launch.
 //   AVAL : use `A_val` directly

@@ -10,6 +10,13 @@
 
 namespace mattohf {
 
+// Fixed xor-shuffle tree over the 32 lanes of a warp (deterministic order).
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // ---------------------------------------------------------------------------
 // Density (F:55-71) and Hartree potential (F:147-162), one CTA.
 // ---------------------------------------------------------------------------
@@ -90,17 +97,22 @@ __device__ __forceinline__ void density_body(const DensArgs& a) {
     return;
   }
   for (int ig = tid; ig < N; ig += blockDim.x) a.vloc[ig] = vh_s[ig] + a.vion[ig];
-  if (tid == 0) {
-    // sequential sums, as the Fortran SUM intrinsic evaluates them
+  if (tid < 32) {
+    // Nele, Eion, EH: lane-strided partial sums, then a fixed shuffle tree
     double sn = 0.0, si = 0.0, sh = 0.0;
-    for (int ig = 0; ig < N; ++ig) {
+    for (int ig = tid; ig < N; ig += 32) {
       sn += rho_s[ig];
       si += a.vion[ig] * rho_s[ig];
       sh += vh_s[ig] * rho_s[ig];
     }
-    a.scal[0] = sn * a.dvcell;
-    a.scal[1] = si * a.dvcell;
-    a.scal[2] = 0.5 * sh * a.dvcell;
+    sn = warp_sum(sn);
+    si = warp_sum(si);
+    sh = warp_sum(sh);
+    if (tid == 0) {
+      a.scal[0] = sn * a.dvcell;
+      a.scal[1] = si * a.dvcell;
+      a.scal[2] = 0.5 * sh * a.dvcell;
+    }
   }
 }
 
@@ -372,16 +384,16 @@ template <int N>
 __device__ __forceinline__ void combine_body(const CombineArgs& a, const int ncols, const int cta) {
   using TM = Team<N>;
   constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
-  constexpr int NTEAM = (kThreads / 32) * PW;
+  constexpr int NTEAM = kCombineWarps * PW;
   __shared__ double2 tw_s[N];
   __shared__ double2 bufs[NTEAM][N];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tl = lane % T, team = warp * PW + lane / T;
-  for (int i = tid; i < N; i += kThreads) tw_s[i] = a.tw[i];
+  for (int i = tid; i < N; i += kCombineWarps * 32) tw_s[i] = a.tw[i];
   __syncthreads();
   const double A = afield_value(a.af);
   // warp-uniform: whole warps go idle together
-  const int col0 = (cta * (kThreads / 32) + warp) * PW;
+  const int col0 = (cta * kCombineWarps + warp) * PW;
   if (col0 >= ncols) return;
   const int col = col0 + lane / T;
   const bool valid = col < ncols;
@@ -503,13 +515,13 @@ __device__ __forceinline__ void combine_body(const CombineArgs& a, const int nco
 }
 
 template <int N>
-__global__ void __launch_bounds__(kThreads) k_combine(CombineArgs a, int ncols) {
+__global__ void __launch_bounds__(kCombineWarps * 32) k_combine(CombineArgs a, int ncols) {
   combine_body<N>(a, ncols, blockIdx.x);
 }
 
 // CTA prefix: pre[r] = sum over earlier runs of ceil(ncols_r / columns per CTA)
 template <int N>
-__global__ void __launch_bounds__(kThreads) k_combine_batch(const CombineArgs* __restrict__ args,
+__global__ void __launch_bounds__(kCombineWarps * 32) k_combine_batch(const CombineArgs* __restrict__ args,
                                                           const int* __restrict__ pre, int nruns) {
   const int r = find_run(pre, nruns, blockIdx.x);
   const CombineArgs& a = args[r];
@@ -518,14 +530,18 @@ __global__ void __launch_bounds__(kThreads) k_combine_batch(const CombineArgs* _
 
 // Deferred exchange energy Ex = 0.5 sum_occ occ <u|F u> dvcell (F:165-183),
 // added to the Etot of the step whose orbitals produced F.
-__device__ __forceinline__ void ex_finalize_body(const ExArgs& a) {
+__device__ __forceinline__ void ex_finalize_body(const ExArgs& a, int lane) {
   int idx = a.idx;
   if (idx < 0) idx = *a.it - 1;
   if (idx < 0) return;
   double ex = 0.0;
-  for (int ik = 0; ik < a.nk; ++ik)
-    for (int ib = 0; ib < a.nbocc; ++ib) ex += a.occ * a.colbuf[(size_t)(ik * a.nb + ib) * 4 + 2] * a.dvcell;
-  ex = 0.5 * ex;
+  const int ncol = a.nk * a.nbocc;
+  for (int o = lane; o < ncol; o += 32) {
+    const int ik = o / a.nbocc, ib = o % a.nbocc;
+    ex += a.occ * a.colbuf[(size_t)(ik * a.nb + ib) * 4 + 2] * a.dvcell;
+  }
+  ex = 0.5 * warp_sum(ex);
+  if (lane != 0) return;
   if (a.series_E) a.series_E[idx] = a.series_E[idx] + ex;
   if (a.out) {
     a.out[0] = a.out[0] + ex;
@@ -534,28 +550,32 @@ __device__ __forceinline__ void ex_finalize_body(const ExArgs& a) {
 }
 
 __global__ void k_ex_finalize(ExArgs a) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) ex_finalize_body(a);
+  if (blockIdx.x == 0 && threadIdx.x < 32) ex_finalize_body(a, threadIdx.x);
 }
 
 __global__ void k_ex_finalize_batch(const ExArgs* __restrict__ args, int nruns) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < nruns) ex_finalize_body(args[r]);
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r < nruns) ex_finalize_body(args[r], threadIdx.x & 31);
 }
 
 // ---------------------------------------------------------------------------
 // Observable reduction (F:74-91, F:165-183, F:289-318) in reference order.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void obs_reduce_body(const ObsReduceArgs& a) {
+__device__ __forceinline__ void obs_reduce_body(const ObsReduceArgs& a, int lane) {
   double ekin = 0.0, jre = 0.0, exr = 0.0;
-  for (int ik = 0; ik < a.nk; ++ik) {
-    for (int ib = 0; ib < a.nb; ++ib) {
-      const double occ = ib < a.nbocc ? a.occ : 0.0;
-      const double* cb = a.colbuf + (size_t)(ik * a.nb + ib) * 4;
-      ekin += occ * cb[0] * a.dvcell;
-      jre += occ * cb[1];
-      if (ib < a.nbocc && !a.defer_ex) exr += occ * cb[2] * a.dvcell;
-    }
+  const int ncol = a.nk * a.nb;
+  for (int c = lane; c < ncol; c += 32) {
+    const int ib = c % a.nb;
+    const double occ = ib < a.nbocc ? a.occ : 0.0;
+    const double* cb = a.colbuf + (size_t)c * 4;
+    ekin += occ * cb[0] * a.dvcell;
+    jre += occ * cb[1];
+    if (ib < a.nbocc && !a.defer_ex) exr += occ * cb[2] * a.dvcell;
   }
+  ekin = warp_sum(ekin);
+  jre = warp_sum(jre);
+  exr = warp_sum(exr);
+  if (lane != 0) return;
   const double Ex = (a.hf && !a.defer_ex) ? 0.5 * exr : 0.0;
   const double Eion = a.scal[1], EH = a.scal[2], Nele = a.scal[0];
   const double Etot = a.defer_ex ? (ekin + Eion + EH) : (ekin + Eion + EH + Ex);
@@ -578,13 +598,13 @@ __device__ __forceinline__ void obs_reduce_body(const ObsReduceArgs& a) {
 }
 
 __global__ void k_obs_reduce(ObsReduceArgs a) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) obs_reduce_body(a);
+  if (blockIdx.x == 0 && threadIdx.x < 32) obs_reduce_body(a, threadIdx.x);
 }
 
-// one thread per run; the step counter is advanced by k_step_advance afterwards
+// one warp per run; the step counter is advanced by k_step_advance afterwards
 __global__ void k_obs_reduce_batch(const ObsReduceArgs* __restrict__ args, int nruns) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < nruns) obs_reduce_body(args[r]);
+  const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (r < nruns) obs_reduce_body(args[r], threadIdx.x & 31);
 }
 
 __global__ void k_step_advance(int* it) {
@@ -642,10 +662,10 @@ static cudaError_t configure_impl() {
 
 template <int N>
 static cudaError_t combine_impl(const CombineArgs& a, int ncols, cudaStream_t s) {
-  constexpr int PER_CTA = (kThreads / 32) * Team<N>::PER_WARP;
+  constexpr int PER_CTA = kCombineWarps * Team<N>::PER_WARP;
   const int blocks = (ncols + PER_CTA - 1) / PER_CTA;
   if (blocks == 0) return cudaSuccess;
-  k_combine<N><<<blocks, kThreads, 0, s>>>(a, ncols);
+  k_combine<N><<<blocks, kCombineWarps * 32, 0, s>>>(a, ncols);
   return cudaGetLastError();
 }
 
@@ -774,12 +794,12 @@ cudaError_t launch_fock_sym_batch(int NG, const FockSymArgs* d_args, const int* 
 
 int combine_cols_per_cta(int NG) {
   switch (NG) {
-    case 16: return (kThreads / 32) * Team<16>::PER_WARP;
-    case 32: return (kThreads / 32) * Team<32>::PER_WARP;
-    case 64: return (kThreads / 32) * Team<64>::PER_WARP;
-    case 128: return (kThreads / 32) * Team<128>::PER_WARP;
-    case 256: return (kThreads / 32) * Team<256>::PER_WARP;
-    case 512: return (kThreads / 32) * Team<512>::PER_WARP;
+    case 16: return kCombineWarps * Team<16>::PER_WARP;
+    case 32: return kCombineWarps * Team<32>::PER_WARP;
+    case 64: return kCombineWarps * Team<64>::PER_WARP;
+    case 128: return kCombineWarps * Team<128>::PER_WARP;
+    case 256: return kCombineWarps * Team<256>::PER_WARP;
+    case 512: return kCombineWarps * Team<512>::PER_WARP;
     default: return 0;
   }
 }
@@ -787,18 +807,18 @@ int combine_cols_per_cta(int NG) {
 cudaError_t launch_combine_batch(int NG, const CombineArgs* d_args, const int* d_cta_pre, int nruns,
                                  int total_ctas, cudaStream_t s) {
   if (total_ctas <= 0) return cudaSuccess;
-#define CALL(n) (k_combine_batch<n><<<total_ctas, kThreads, 0, s>>>(d_args, d_cta_pre, nruns), cudaGetLastError())
+#define CALL(n) (k_combine_batch<n><<<total_ctas, kCombineWarps * 32, 0, s>>>(d_args, d_cta_pre, nruns), cudaGetLastError())
   MATTOHF_DISPATCH(NG, CALL)
 #undef CALL
 }
 
 cudaError_t launch_obs_reduce_batch(const ObsReduceArgs* d_args, int nruns, cudaStream_t s) {
-  k_obs_reduce_batch<<<(nruns + 127) / 128, 128, 0, s>>>(d_args, nruns);
+  k_obs_reduce_batch<<<(nruns + 3) / 4, 128, 0, s>>>(d_args, nruns);
   return cudaGetLastError();
 }
 
 cudaError_t launch_ex_finalize_batch(const ExArgs* d_args, int nruns, cudaStream_t s) {
-  k_ex_finalize_batch<<<(nruns + 127) / 128, 128, 0, s>>>(d_args, nruns);
+  k_ex_finalize_batch<<<(nruns + 3) / 4, 128, 0, s>>>(d_args, nruns);
   return cudaGetLastError();
 }
 
