@@ -119,6 +119,10 @@ int mattohf_density(mattohf_ctx* ctx, const double* ubk, double* dns, double* vH
 int mattohf_observables(mattohf_ctx* ctx, double A, double* Ecomps, double* Etot, double* Je,
                         double* Nele);
 
+/* The reference's alternative propagators on the device orbitals (4th-order
+ * Taylor expansion of exp(-i dt h), src/RT_calculation.f90:72-151):
+ * variant 0 = RT_TE_ubk, 1 = RT_TEPC_ubk (predictor-corrector), 2 = RT_TEPC2_ubk. */
+int mattohf_te_step(mattohf_ctx* ctx, int variant, double Aave, double dt);
 /* RT_RK4_ubk (src/RT_calculation.f90:154-173): one RK4 step of the device
  * orbitals with stage fields 2*Aave-A, Aave, Aave, A. */
 int mattohf_rk4_step(mattohf_ctx* ctx, double Aave, double A, double dt);

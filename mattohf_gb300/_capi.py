@@ -40,7 +40,7 @@ EXPORTS = [
     "mattohf_synchronize", "mattohf_diag_fp64_peak", "mattohf_fock_noalloc",
     "mattohf_batch_create", "mattohf_batch_destroy", "mattohf_batch_last_error", "mattohf_batch_run",
     "mattohf_batch_rk4_run", "mattohf_batch_last_run_ms", "mattohf_adjoint", "mattohf_adjoint_timing",
-    "mattohf_fourier", "mattohf_vck",
+    "mattohf_fourier", "mattohf_vck", "mattohf_te_step",
 ]
 
 
@@ -106,6 +106,7 @@ def load(path: str = LIB_PATH):
         "mattohf_adjoint": ([P, I, I, C.c_double, D, I, D, D, D], I),
         "mattohf_adjoint_timing": ([P, D, D], I),
         "mattohf_vck": ([P, D, I, D], I),
+        "mattohf_te_step": ([P, I, C.c_double, C.c_double], I),
         "mattohf_fourier": ([I, I, D, D, C.c_double, D, D, D, I, C.c_double, C.c_double, D], I),
     }
     for name, (args, res) in sig.items():

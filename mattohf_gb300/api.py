@@ -204,6 +204,11 @@ class Context:
     def RT_RK4_ubk(self, Aave: float, A: float, dt: float):
         self._check(self.lib.mattohf_rk4_step(self.h, float(Aave), float(A), float(dt)))
 
+    def RT_TE_ubk(self, Aave: float, dt: float, variant: str = "TE"):
+        """Taylor / predictor-corrector propagators (RT:72-151): 'TE', 'TEPC' or 'TEPC2'."""
+        v = {"TE": 0, "TEPC": 1, "TEPC2": 2}[variant]
+        self._check(self.lib.mattohf_te_step(self.h, v, float(Aave), float(dt)))
+
     def rk4_run(self, A, Aave, dt: float):
         """nt RK4 steps with per-step (Etot, Je, Nele) at A[it] (RT:38-60)."""
         A = np.ascontiguousarray(A, dtype=np.float64)

@@ -1509,6 +1509,53 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   return MATTOHF_OK;
 }
 
+// Taylor expansion of exp(-i dt h[base]) applied to `target` in place
+// (RT_TE_ubk, RT:83-89); uses d_k[2] (workbk) and d_k[3] (h workbk).
+static int enq_taylor(mattohf_ctx* ctx, double2* target, const double2* base, double Aave, double dt) {
+  const int NG = ctx->NG, NB = ctx->NB;
+  const size_t n = orb_elems(ctx, NB);
+  double2* w = ctx->d_k[2];
+  double2* hw = ctx->d_k[3];
+  CK(cudaMemcpyAsync(w, target, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->st));
+  for (int iorder = 1; iorder <= 4; ++iorder) {
+    CKR(enq_hpsi(ctx, blk(base, NB, NG, NB), blk(w, NB, NG, NB), blko(hw, NB, NG, NB), aval(Aave), CM_H));
+    CK(launch_te_update(w, hw, nullptr, dt, (double)iorder, target, n, ctx->st));
+  }
+  return MATTOHF_OK;
+}
+
+extern "C" int mattohf_te_step(mattohf_ctx* ctx, int variant, double Aave, double dt) {
+  CKR(check_ctx(ctx));
+  if (variant < 0 || variant > 2) return fail(ctx, MATTOHF_ERR_ARG, "variant must be 0 (TE), 1 (TEPC) or 2 (TEPC2)");
+  const int NG = ctx->NG, NB = ctx->NB;
+  const size_t n = orb_elems(ctx, NB);
+  double2* u0 = ctx->d_k[0];
+  double2* u1 = ctx->d_k[1];
+  CK(cudaMemcpyAsync(u0, ctx->d_u, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->st));
+  if (variant == 0) {
+    CKR(enq_taylor(ctx, ctx->d_u, u0, Aave, dt));
+  } else {
+    CK(cudaMemcpyAsync(u1, ctx->d_u, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->st));
+    CKR(enq_taylor(ctx, u1, u0, Aave, dt));  // predictor (RT:107-112, RT:135-141)
+    if (variant == 1) {
+      // corrector with the average of h[u0] and h[u1] (RT:114-118)
+      double2* w = ctx->d_k[2];
+      double2* h0 = ctx->d_k[3];
+      double2* h1 = ctx->d_us;
+      CK(cudaMemcpyAsync(w, ctx->d_u, sizeof(double2) * n, cudaMemcpyDeviceToDevice, ctx->st));
+      for (int iorder = 1; iorder <= 4; ++iorder) {
+        CKR(enq_hpsi(ctx, blk(u0, NB, NG, NB), blk(w, NB, NG, NB), blko(h0, NB, NG, NB), aval(Aave), CM_H));
+        CKR(enq_hpsi(ctx, blk(u1, NB, NG, NB), blk(w, NB, NG, NB), blko(h1, NB, NG, NB), aval(Aave), CM_H));
+        CK(launch_te_update(w, h0, h1, 0.5 * dt, (double)iorder, ctx->d_u, n, ctx->st));
+      }
+    } else {
+      CK(launch_half_sum(u0, u0, u1, n, ctx->st));  // ubk0 = (ubk0 + ubk1)/2 (RT:144)
+      CKR(enq_taylor(ctx, ctx->d_u, u0, Aave, dt));
+    }
+  }
+  return sync_and_flag(ctx);
+}
+
 extern "C" int mattohf_adjoint_timing(mattohf_ctx* ctx, double* forward_ms, double* total_ms) {
   if (!ctx) return MATTOHF_ERR_ARG;
   if (forward_ms) *forward_ms = ctx->last_adj_fwd_ms;

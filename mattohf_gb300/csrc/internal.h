@@ -240,6 +240,10 @@ cudaError_t launch_velocity(int NG, const double2* u, double2* out, const double
                             const double* kx, int nb, double A, double scale, int ncols, cudaStream_t s);
 cudaError_t launch_scale2(double2* x, double sc, size_t n, cudaStream_t s);
 
+cudaError_t launch_te_update(double2* w, const double2* h0, const double2* h1, double c, double iorder,
+                             double2* acc, size_t n, cudaStream_t s);
+cudaError_t launch_half_sum(double2* out, const double2* a, const double2* b, size_t n, cudaStream_t s);
+
 // Tables (k_table.cu)
 cudaError_t launch_vck_table(int NG, int NK, double acell, const double* d_q, int nq,
                              double* d_out, cudaStream_t s);

@@ -405,3 +405,39 @@ cudaError_t launch_scale2(double2* x, double sc, size_t n, cudaStream_t s) {
 }
 
 }  // namespace mattohf
+
+namespace mattohf {
+
+// Taylor-propagator update (RT:86-88, RT:110-117): w = -i c (h0 [+ h1]) / iorder ; acc += w
+__global__ void k_te_update(double2* __restrict__ w, const double2* __restrict__ h0,
+                            const double2* __restrict__ h1, double c, double iorder,
+                            double2* __restrict__ acc, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double2 s = h0[i];
+  if (h1) s = make_double2(s.x + h1[i].x, s.y + h1[i].y);
+  const double2 v = make_double2((c * s.y) / iorder, (-c * s.x) / iorder);
+  w[i] = v;
+  const double2 a = acc[i];
+  acc[i] = make_double2(a.x + v.x, a.y + v.y);
+}
+
+// out = 0.5 * (a + b)
+__global__ void k_half_sum(double2* __restrict__ out, const double2* __restrict__ a,
+                           const double2* __restrict__ b, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = make_double2(0.5 * (a[i].x + b[i].x), 0.5 * (a[i].y + b[i].y));
+}
+
+cudaError_t launch_te_update(double2* w, const double2* h0, const double2* h1, double c, double iorder,
+                             double2* acc, size_t n, cudaStream_t s) {
+  k_te_update<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w, h0, h1, c, iorder, acc, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_half_sum(double2* out, const double2* a, const double2* b, size_t n, cudaStream_t s) {
+  k_half_sum<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, a, b, n);
+  return cudaGetLastError();
+}
+
+}  // namespace mattohf

@@ -597,6 +597,34 @@ def rk4_step(sysm: System, ubk: np.ndarray, Aave: float, A: float, dt: float) ->
     return ubk + (k1 + 2.0 * k2 + 2.0 * k3 + k4) * dt / 6.0
 
 
+def _te(sysm: System, u: np.ndarray, base: np.ndarray, Aave: float, dt: float, norder: int = 4):
+    """u + sum_n (-i dt h[base])^n u / n! term by term (RT:83-89)."""
+    w = u.copy()
+    out = u.copy()
+    for iorder in range(1, norder + 1):
+        w = -(1j * dt) * ubkwbk_hwbk(sysm, base, w, Aave) / float(iorder)
+        out = out + w
+    return out
+
+
+def te_step(sysm: System, ubk: np.ndarray, Aave: float, dt: float, variant: str = "TE"):
+    """Alternative propagators RT_TE_ubk / RT_TEPC_ubk / RT_TEPC2_ubk (RT:72-151)."""
+    u0 = ubk.copy()
+    if variant == "TE":
+        return _te(sysm, ubk, u0, Aave, dt)
+    u1 = _te(sysm, ubk, u0, Aave, dt)
+    if variant == "TEPC":
+        w = ubk.copy()
+        out = ubk.copy()
+        for iorder in range(1, 5):
+            w = -(1j * dt * 0.5) * (ubkwbk_hwbk(sysm, u0, w, Aave) + ubkwbk_hwbk(sysm, u1, w, Aave)) / float(iorder)
+            out = out + w
+        return out
+    if variant == "TEPC2":
+        return _te(sysm, ubk, 0.5 * (u0 + u1), Aave, dt)
+    raise ValueError(variant)
+
+
 @dataclasses.dataclass
 class RTResult:
     time: np.ndarray

@@ -46,6 +46,8 @@ CONFIGS = {
     "ng128_nk4_nb3": make_cfg(NG=128, NK=4, NB=3, NBocc=2),
     "ng256_nk2": make_cfg(NG=256, NK=2, NB=2, NBocc=2),
     "ng512_nk2": make_cfg(NG=512, NK=2, NB=2, NBocc=1),
+    "ng32_nk1": make_cfg(NG=32, NK=1, NB=2, NBocc=2),        # single k-point: one kernel column
+    "ng64_nk5_nb4": make_cfg(NG=64, NK=5, NB=4, NBocc=3, acell=7.0),
 }
 
 _cache = {}
@@ -233,6 +235,18 @@ def test_rk4_step_matches_run():
     assert np.array_equal(a, b)
     ref = O.rk4_step(S, u0, 0.01, 0.02, 0.005)
     assert rel(a, ref) <= TOL_OP
+
+
+@pytest.mark.parametrize("variant", ["TE", "TEPC", "TEPC2"])
+def test_taylor_propagators(variant):
+    from oracle import mattohf_oracle as O
+    cfg, ctx, S = setup("ng16_nk3_unocc")
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    ctx.set_orbitals(u0)
+    ctx.RT_TE_ubk(0.02, 0.004, variant)
+    got = ctx.get_orbitals()
+    ref = O.te_step(S, u0, 0.02, 0.004, variant)
+    assert rel(got, ref) <= TOL_OP
 
 
 def test_graph_equals_eager():
