@@ -311,7 +311,7 @@ int enq_fock(mattohf_ctx* ctx, Block u, Block w, FockPlan* plan) {
       d.T = T;
       d.kern = ctx->d_kern_df;
       d.tw = ctx->d_tw_df;
-      d.scratch = ctx->d_sym;
+      d.scratch = reinterpret_cast<float4*>(ctx->d_sym);  // same 16-byte elements
       d.F = ctx->d_symF;
       CK(launch_fock_sym_df(NG, d, u.p, u.kstride, ctx->d_udf, ctx->st));
     } else {

@@ -96,7 +96,7 @@ struct FockSymDfArgs {
   int S, T;
   const float2* kern;   // df copy of the kernel table
   const float4* tw;     // df twiddles
-  double2* scratch;     // tile partials (FP64), as FockSymArgs
+  float4* scratch;      // tile partials (double-float), layout as FockSymArgs
   double2* F;           // reduced exchange [NK*nbocc][NG]
 };
 cudaError_t launch_fock_sym_df(int NG, const FockSymDfArgs& a, const double2* u, int kstride, float4* udf,

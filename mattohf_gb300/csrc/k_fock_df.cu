@@ -42,10 +42,12 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) {
   const bool va = tw_ < S && ia < M;
   const int oa = va ? ia : 0;
   const int ka = oa / a.nbocc;
-  cdf ua[E], racc[E];
+  // the row orbital is re-read from the (L1-resident) df copy where needed
+  // instead of being held in registers, to keep three CTAs per SM
+  const float4* ua_p = a.u + (size_t)oa * N;
+  cdf racc[E];
 #pragma unroll
   for (int e = 0; e < E; ++e) {
-    ua[e] = df::load(a.u + (size_t)oa * N + TM::pos(tl, e));
     racc[e].re = make_float2(0.f, 0.f);
     racc[e].im = make_float2(0.f, 0.f);
   }
@@ -62,11 +64,12 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) {
     const int kb = ob / a.nbocc;
     const int dab = ka - kb + a.nk - 1, dba = kb - ka + a.nk - 1;
     const float2* kab = a.kern + (size_t)dab * N;
-    cdf ub[E], x[E];
+    const float4* ub_p = a.u + (size_t)ob * N;
+    cdf x[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      ub[e] = df::load(a.u + (size_t)ob * N + TM::pos(tl, e));
-      x[e] = df::cmulc(ua[e], ub[e]);
+      const int q = TM::pos(tl, e);
+      x[e] = df::cmulc(df::load(ua_p + q), df::load(ub_p + q));
     }
     df::fft_team<N, -1>(x, buf, tw_s, tl);
     const cdf rn_own = x[TM::R0 / 2];
@@ -80,7 +83,7 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) {
     df::fft_team<N, +1>(x, buf, tw_s, tl);
     if (valid) {
 #pragma unroll
-      for (int e = 0; e < E; ++e) racc[e] = df::cadd(racc[e], df::cmul(x[e], ub[e]));
+      for (int e = 0; e < E; ++e) racc[e] = df::cadd(racc[e], df::cmul(x[e], df::load(ub_p + TM::pos(tl, e))));
       if (!self) {
         const float2 dk = df::sub(a.kern[(size_t)dba * N + N / 2], kab[N / 2]);
         // c = dk conj(R); phi_ba = conj(phi_ab) + c (-1)^m
@@ -92,18 +95,41 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) {
           const bool odd = q & 1;
           const cdf pba = df::make(df::add(x[e].re, odd ? df::neg(cx) : cx),
                                    df::add(df::neg(x[e].im), odd ? df::neg(cy) : cy));
-          col[q] = df::cadd(col[q], df::cmul(pba, ua[e]));
+          col[q] = df::cadd(col[q], df::cmul(pba, df::load(ua_p + q)));
         }
       }
     }
     __syncthreads();
   }
-  double2* dst = a.scratch + (size_t)blockIdx.x * 2 * S * N;
+  // partials stay double-float; k_sym_reduce_df sums them and converts once
+  float4* dst = a.scratch + (size_t)blockIdx.x * 2 * S * N;
   if (tw_ < S) {
 #pragma unroll
-    for (int e = 0; e < E; ++e) dst[(size_t)tw_ * N + TM::pos(tl, e)] = df::to_double2(racc[e]);
+    for (int e = 0; e < E; ++e) df::store(dst + (size_t)tw_ * N + TM::pos(tl, e), racc[e]);
   }
-  for (int i = tid; i < S * N; i += blockDim.x) dst[(size_t)S * N + i] = df::to_double2(cacc[i]);
+  for (int i = tid; i < S * N; i += blockDim.x) df::store(dst + (size_t)S * N + i, cacc[i]);
+}
+
+// Ordered double-float sum of the tile partials of every occupied output,
+// converted to FP64 once (same order as k_sym_reduce).
+__global__ void k_sym_reduce_df(const float4* __restrict__ part, int S, int T, int M, int N,
+                                double2* __restrict__ F) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= M * N) return;
+  const int o = idx / N, q = idx % N;
+  const int i = o / S, l = o % S;
+  const size_t SN = (size_t)S * N;
+  df::cdf f;
+  f.re = make_float2(0.f, 0.f);
+  f.im = make_float2(0.f, 0.f);
+  for (int j = 0; j < i; ++j) f = df::cadd(f, df::load(part + (size_t)sym_tp(j, i, T) * 2 * SN + SN + (size_t)l * N + q));
+  {
+    const size_t b = (size_t)sym_tp(i, i, T) * 2 * SN + (size_t)l * N + q;
+    f = df::cadd(f, df::load(part + b));
+    f = df::cadd(f, df::load(part + b + SN));
+  }
+  for (int j = i + 1; j < T; ++j) f = df::cadd(f, df::load(part + (size_t)sym_tp(i, j, T) * 2 * SN + (size_t)l * N + q));
+  F[idx] = df::to_double2(f);
 }
 
 // occupied orbitals (FP64, [NK][NB][NG]) -> df copy [NK*NBocc][NG]
@@ -152,7 +178,8 @@ static cudaError_t fock_df_impl(const FockSymDfArgs& a, const double2* u, int ks
   if ((e = sym_launch_params(N, a.S, &threads, &smem)) != cudaSuccess) return e;
   k_fock_sym_df<N><<<tiles, threads, smem, s>>>(a);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  return launch_sym_reduce(a.scratch, a.S, a.T, M, N, a.F, s);
+  k_sym_reduce_df<<<(M * N + 255) / 256, 256, 0, s>>>(a.scratch, a.S, a.T, M, N, a.F);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_fock_sym_df(int NG, const FockSymDfArgs& a, const double2* u, int kstride, float4* udf,
