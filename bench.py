@@ -474,6 +474,43 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def run_large(args):
+    """Largest configuration shape, one variant: a = 12, NG = 512, NK = 128,
+    NB = Nocc = 8, three ions (Z=1 at a/6, a/2, 5a/6), dt = 2.5e-4 (the
+    configured 0.01 is RK4-unstable here).  RK4 steps/s in FP64 and with the
+    double-float exchange, and the adjoint/forward ratio over a short window.
+    """
+    from mattohf_gb300 import Context, RunConfig, define_afield, aave_from_samples, _capi
+    import dataclasses
+    K, W = args.steps, args.warmup
+    cfg = RunConfig.from_pulse(0.1, 0.06, 200.0, acell=12.0, NG=512, NK=128, NB=8, NBocc=8, Zeff=[1.0],
+                               alpha=[1.0], Rion=[1 / 6, 0.5, 5 / 6], Kion=[1, 1, 1], dt=2.5e-4, NT=W + K)
+    A = define_afield(cfg)[1]
+    Aave = aave_from_samples(A)
+    out = {"metric": "TDHF RK4 steps/s (largest shape, one variant)", "unit": "steps/s", "dtype": "f64",
+           "data": "synthetic", "steps": K, "warmup": W,
+           "config": {"workload": "a=12, NG=512, NK=128, Nocc=NB=8, 3 ions, dt=2.5e-4"}}
+    with Context(cfg) as ctx:
+        ctx.Init_wf()
+        ctx.Gram_Schmidt()
+        u0 = ctx.get_orbitals()
+        for mode, key in ((0, "value"), (1, "double_float_exchange")):
+            ctx.set_option(_capi.OPT_FOCK_DF64, mode)
+            ctx.set_orbitals(u0)
+            ctx.rk4_run(A[:W], Aave[:W], cfg.dt)
+            ctx.set_orbitals(u0)
+            ctx.rk4_run(A[W:], Aave[W:], cfg.dt)
+            out[key] = K / (ctx.last_run_timing()[0] * 1e-3)
+        ctx.set_option(_capi.OPT_FOCK_DF64, 0)
+        ctx.set_orbitals(u0)
+        ctx.rk4_run(A[:K], Aave[:K], cfg.dt)
+        t_fwd = ctx.last_run_timing()[0]
+        ctx.set_orbitals(u0)
+        ctx.adjoint(A[:K], cfg.dt, "energy", ckpt_every=max(1, K // 4))
+        out["adjoint_over_forward"] = ctx.adjoint_timing()[1] / t_fwd
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -482,7 +519,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=6)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="plain", choices=["plain", "ensemble", "adjoint"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "ensemble", "adjoint", "large"])
     ap.add_argument("--runs", type=int, default=256)
     ap.add_argument("--adj-steps", type=int, default=4000)
     ap.add_argument("--fd-samples", type=int, default=32)
@@ -513,6 +550,10 @@ def main():
             from mattohf_gb300 import build
             build.build()
             run_adjoint(args)
+        elif args.workload == "large":
+            from mattohf_gb300 import build
+            build.build()
+            run_large(args)
         elif args.impl == "reference":
             run_reference(args, dist)
         else:

@@ -71,22 +71,31 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) {
       const int q = TM::pos(tl, e);
       x[e] = df::cmulc(df::load(ua_p + q), df::load(ub_p + q));
     }
-    df::fft_team<N, -1>(x, buf, tw_s, tl);
-    const cdf rn_own = x[TM::R0 / 2];
+    // Both transforms run through ONE copy of the forward FFT code (the
+    // kernel is instruction-cache bound): IFFT(y) = conj(FFT(conj(y))), so
+    // after the second pass x = conj(phi_ab).
     cdf rn;
-    rn.re.x = __shfl_sync(0xffffffffu, rn_own.re.x, team_lane0);
-    rn.re.y = __shfl_sync(0xffffffffu, rn_own.re.y, team_lane0);
-    rn.im.x = __shfl_sync(0xffffffffu, rn_own.im.x, team_lane0);
-    rn.im.y = __shfl_sync(0xffffffffu, rn_own.im.y, team_lane0);
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+      df::fft_team<N, -1>(x, buf, tw_s, tl);
+      if (pass == 0) {
+        const cdf rn_own = x[TM::R0 / 2];
+        rn.re.x = __shfl_sync(0xffffffffu, rn_own.re.x, team_lane0);
+        rn.re.y = __shfl_sync(0xffffffffu, rn_own.re.y, team_lane0);
+        rn.im.x = __shfl_sync(0xffffffffu, rn_own.im.x, team_lane0);
+        rn.im.y = __shfl_sync(0xffffffffu, rn_own.im.y, team_lane0);
 #pragma unroll
-    for (int e = 0; e < E; ++e) x[e] = df::scale(x[e], kab[TM::pos(tl, e)]);
-    df::fft_team<N, +1>(x, buf, tw_s, tl);
+        for (int e = 0; e < E; ++e) x[e] = df::conj(df::scale(x[e], kab[TM::pos(tl, e)]));
+      }
+    }
     if (valid) {
+      // row: out_a += phi_ab u_b with phi_ab = conj(x)
 #pragma unroll
-      for (int e = 0; e < E; ++e) racc[e] = df::cadd(racc[e], df::cmul(x[e], df::load(ub_p + TM::pos(tl, e))));
+      for (int e = 0; e < E; ++e)
+        racc[e] = df::cadd(racc[e], df::cmul(df::conj(x[e]), df::load(ub_p + TM::pos(tl, e))));
       if (!self) {
         const float2 dk = df::sub(a.kern[(size_t)dba * N + N / 2], kab[N / 2]);
-        // c = dk conj(R); phi_ba = conj(phi_ab) + c (-1)^m
+        // c = dk conj(R); phi_ba = conj(phi_ab) + c (-1)^m = x + c (-1)^m
         const float2 cx = df::mul(dk, rn.re), cy = df::neg(df::mul(dk, rn.im));
         cdf* col = cacc + lb * N;
 #pragma unroll
@@ -94,7 +103,7 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) {
           const int q = TM::pos(tl, e);
           const bool odd = q & 1;
           const cdf pba = df::make(df::add(x[e].re, odd ? df::neg(cx) : cx),
-                                   df::add(df::neg(x[e].im), odd ? df::neg(cy) : cy));
+                                   df::add(x[e].im, odd ? df::neg(cy) : cy));
           col[q] = df::cadd(col[q], df::cmul(pba, df::load(ua_p + q)));
         }
       }

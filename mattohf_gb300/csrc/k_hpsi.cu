@@ -254,13 +254,13 @@ __device__ __forceinline__ void fock_sym_body(const FockSymArgs& a, const int ti
   const int ia = ti * S + tw_;
   const bool va = tw_ < S && ia < M;
   const int ka = (va ? ia : 0) / a.nbocc, ba = (va ? ia : 0) % a.nbocc;
+  // orbitals are re-read from global memory (L1/L2-resident) where needed
+  // rather than held in registers: the kernel is FP64-pipe bound, and this
+  // keeps the largest grids free of register spills
   const double2* ucol_a = a.u.p + (size_t)ka * a.u.kstride + (size_t)ba * N;
-  double2 ua[E], racc[E];
+  double2 racc[E];
 #pragma unroll
-  for (int e = 0; e < E; ++e) {
-    ua[e] = ucol_a[TM::pos(tl, e)];
-    racc[e] = make_double2(0.0, 0.0);
-  }
+  for (int e = 0; e < E; ++e) racc[e] = make_double2(0.0, 0.0);
   __syncthreads();
   const bool diag = (ti == tj);
   const int nrounds = diag ? (S / 2 + 1) : S;
@@ -272,11 +272,11 @@ __device__ __forceinline__ void fock_sym_body(const FockSymArgs& a, const int ti
     const bool self = diag && r == 0;
     const int kb = (ib < M ? ib : 0) / a.nbocc, bb = (ib < M ? ib : 0) % a.nbocc;
     const double2* ucol_b = a.u.p + (size_t)kb * a.u.kstride + (size_t)bb * N;
-    double2 ub[E], x[E];
+    double2 x[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      ub[e] = ucol_b[TM::pos(tl, e)];
-      x[e] = cmulc(ua[e], ub[e]);
+      const int q = TM::pos(tl, e);
+      x[e] = cmulc(ucol_a[q], ucol_b[q]);
     }
     fft_team<N, -1>(x, buf, tw_s, tl);
     // Nyquist coefficient R_ab[N/2] lives in slot (p=0, r=R0/2) of the team's lane 0
@@ -293,7 +293,7 @@ __device__ __forceinline__ void fock_sym_body(const FockSymArgs& a, const int ti
     fft_team<N, +1>(x, buf, tw_s, tl);
     if (valid) {
 #pragma unroll
-      for (int e = 0; e < E; ++e) racc[e] = cfma(x[e], ub[e], racc[e]);
+      for (int e = 0; e < E; ++e) racc[e] = cfma(x[e], ucol_b[TM::pos(tl, e)], racc[e]);
       if (!self) {
         const double dk = __ldg(a.kern + (size_t)dba * N + N / 2) - __ldg(kab + N / 2);
         const double cx = dk * rnx, cy = -dk * rny;  // dk * conj(R)
@@ -303,7 +303,7 @@ __device__ __forceinline__ void fock_sym_body(const FockSymArgs& a, const int ti
           const int q = TM::pos(tl, e);
           const double sg = (q & 1) ? -1.0 : 1.0;
           const double2 pba = make_double2(fma(sg, cx, x[e].x), fma(sg, cy, -x[e].y));
-          col[q] = cfma(pba, ua[e], col[q]);
+          col[q] = cfma(pba, ucol_a[q], col[q]);
         }
       }
     }
