@@ -168,12 +168,10 @@ __global__ void __launch_bounds__(kThreads) k_fock(FockArgs a) {
   const int col = item / a.nchunks, chunk = item % a.nchunks;
   const int kr = col / a.w.nb, ibr = col % a.w.nb;
   const double2* wcol = a.w.p + (size_t)kr * a.w.kstride + (size_t)ibr * N;
-  double2 wv[E], acc[E];
+  // w and u columns are re-read (L1/L2) instead of held in registers
+  double2 acc[E];
 #pragma unroll
-  for (int e = 0; e < E; ++e) {
-    wv[e] = wcol[TM::pos(tl, e)];
-    acc[e] = make_double2(0.0, 0.0);
-  }
+  for (int e = 0; e < E; ++e) acc[e] = make_double2(0.0, 0.0);
   const int npairs = a.nk * a.nbocc;
   const int p0 = chunk * a.chunk;
   const int p1 = min(npairs, p0 + a.chunk);
@@ -185,11 +183,11 @@ __global__ void __launch_bounds__(kThreads) k_fock(FockArgs a) {
     const int kc = pp / a.nbocc, ibc = pp % a.nbocc;
     const double2* ucol = a.u.p + (size_t)kc * a.u.kstride + (size_t)ibc * N;
     const double* kern = a.kern + (size_t)(kr - kc + a.nk - 1) * N;
-    double2 uv[E], x[E];
+    double2 x[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      uv[e] = ucol[TM::pos(tl, e)];
-      x[e] = cmulc(wv[e], uv[e]);
+      const int q = TM::pos(tl, e);
+      x[e] = cmulc(wcol[q], ucol[q]);
     }
     fft_team<N, -1>(x, buf, tw_s, tl);
 #pragma unroll
@@ -200,7 +198,7 @@ __global__ void __launch_bounds__(kThreads) k_fock(FockArgs a) {
     fft_team<N, +1>(x, buf, tw_s, tl);
     if (valid) {
 #pragma unroll
-      for (int e = 0; e < E; ++e) acc[e] = cfma(x[e], uv[e], acc[e]);
+      for (int e = 0; e < E; ++e) acc[e] = cfma(x[e], ucol[TM::pos(tl, e)], acc[e]);
     }
   }
   // fixed-order reduction over teams
