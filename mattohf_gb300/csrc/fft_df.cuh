@@ -218,3 +218,78 @@ __device__ __forceinline__ void fft_team(cdf (&x)[Team<N>::E], cdf* buf, const c
 
 }  // namespace df
 }  // namespace mattohf
+
+namespace mattohf {
+namespace df {
+
+// Compact-code variant of fft_team: the same slot interface (values in
+// registers at Team<N>::pos), but every pass is the SAME radix-4 Stockham
+// butterfly block (plus one radix-2 pass when log2 N is odd), executed from a
+// runtime loop over passes through the team's shared-memory buffer.  A few
+// percent more arithmetic than the radix-8 plan, but the instruction
+// footprint of the whole transform is one butterfly block, which keeps the
+// double-float kernel out of instruction-cache stalls.
+template <int N>
+__device__ __forceinline__ void fft_team_compact(cdf (&x)[Team<N>::E], cdf* buf, const cdf* __restrict__ tw, int tl) {
+  using TM = Team<N>;
+  constexpr int T = TM::T;
+  constexpr int L2 = N == 16 ? 4 : N == 32 ? 5 : N == 64 ? 6 : N == 128 ? 7 : N == 256 ? 8 : 9;
+  constexpr int P4 = N / (4 * T);   // radix-4 butterflies per lane
+  constexpr int P2 = N / (2 * T);   // radix-2 butterflies per lane
+  static_assert(P4 >= 1, "team too large for a radix-4 pass");
+#pragma unroll
+  for (int e = 0; e < TM::E; ++e) buf[TM::pos(tl, e)] = x[e];
+  __syncwarp();
+  int ls = 0;  // log2 of the current stride NS
+#pragma unroll 1
+  for (int s = 0; s < L2 / 2; ++s, ls += 2) {
+    const int NS = 1 << ls;
+    cdf v[P4 * 4];
+#pragma unroll
+    for (int p = 0; p < P4; ++p) {
+      const int j = tl + T * p;
+      const int k = j & (NS - 1);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) v[p * 4 + r] = buf[j + r * (N / 4)];
+      if (NS > 1) {
+#pragma unroll
+        for (int r = 1; r < 4; ++r) v[p * 4 + r] = cmul(v[p * 4 + r], tw[(r * k) << (L2 - ls - 2)]);
+      }
+      Dft<4, -1>::run(&v[p * 4]);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int p = 0; p < P4; ++p) {
+      const int j = tl + T * p;
+      const int base = ((j >> ls) << (ls + 2)) + (j & (NS - 1));
+#pragma unroll
+      for (int r = 0; r < 4; ++r) buf[base + r * NS] = v[p * 4 + r];
+    }
+    __syncwarp();
+  }
+  if constexpr (L2 & 1) {
+    constexpr int NS = N / 2;
+    cdf v[P2 * 2];
+#pragma unroll
+    for (int p = 0; p < P2; ++p) {
+      const int j = tl + T * p;
+      v[p * 2] = buf[j];
+      v[p * 2 + 1] = cmul(buf[j + N / 2], tw[j]);
+      Dft<2, -1>::run(&v[p * 2]);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int p = 0; p < P2; ++p) {
+      const int j = tl + T * p;
+      buf[j] = v[p * 2];
+      buf[j + NS] = v[p * 2 + 1];
+    }
+    __syncwarp();
+  }
+#pragma unroll
+  for (int e = 0; e < TM::E; ++e) x[e] = buf[TM::pos(tl, e)];
+  __syncwarp();
+}
+
+}  // namespace df
+}  // namespace mattohf

@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) {
     cdf rn;
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
-      df::fft_team<N, -1>(x, buf, tw_s, tl);
+      df::fft_team_compact<N>(x, buf, tw_s, tl);
       if (pass == 0) {
         const cdf rn_own = x[TM::R0 / 2];
         rn.re.x = __shfl_sync(0xffffffffu, rn_own.re.x, team_lane0);
