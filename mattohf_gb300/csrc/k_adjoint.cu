@@ -45,14 +45,13 @@ __global__ void __launch_bounds__(kThreads) k_fock_adj(AdjFockArgs a) {
   const bool va = tw_ < S && ia < M;
   const int ka = (va ? ia : 0) / a.nbocc, ba = (va ? ia : 0) % a.nbocc;
   const size_t oa = (size_t)ka * a.kstride + (size_t)ba * N;
-  double2 vA[E], mA[E], racc[E];
+  // orbitals and adjoints are re-read (L1/L2) where needed instead of held in
+  // registers (the kernel is FP64-pipe bound; this avoids spills at NG=512)
+  const double2* vA = a.v + oa;
+  const double2* mA = a.mu + oa;
+  double2 racc[E];
 #pragma unroll
-  for (int e = 0; e < E; ++e) {
-    const int q = TM::pos(tl, e);
-    vA[e] = a.v[oa + q];
-    mA[e] = a.mu[oa + q];
-    racc[e] = make_double2(0.0, 0.0);
-  }
+  for (int e = 0; e < E; ++e) racc[e] = make_double2(0.0, 0.0);
   __syncthreads();
   const bool diag = (ti == tj);
   const int nrounds = diag ? (S / 2 + 1) : S;
@@ -67,16 +66,15 @@ __global__ void __launch_bounds__(kThreads) k_fock_adj(AdjFockArgs a) {
     const int dab = ka - kb + a.nk - 1, dba = kb - ka + a.nk - 1;
     const double* kab = a.kern + (size_t)dab * N;
     const double dk = __ldg(a.kern + (size_t)dba * N + N / 2) - __ldg(kab + N / 2);
-    double2 vB[E], mB[E], x[E];
+    const double2* vB = a.v + ob;
+    const double2* mB = a.mu + ob;
+    double2 x[E];
+    // ---- pass A: phi_ab = Phi_ab[v_a conj(v_b)]
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       const int q = TM::pos(tl, e);
-      vB[e] = a.v[ob + q];
-      mB[e] = a.mu[ob + q];
+      x[e] = cmulc(vA[q], vB[q]);
     }
-    // ---- pass A: phi_ab = Phi_ab[v_a conj(v_b)]
-#pragma unroll
-    for (int e = 0; e < E; ++e) x[e] = cmulc(vA[e], vB[e]);
     fft_team<N, -1>(x, buf, tw_s, tl);
     double rnx = __shfl_sync(0xffffffffu, x[TM::R0 / 2].x, team_lane0);
     double rny = __shfl_sync(0xffffffffu, x[TM::R0 / 2].y, team_lane0);
@@ -90,7 +88,8 @@ __global__ void __launch_bounds__(kThreads) k_fock_adj(AdjFockArgs a) {
       if (self) {
         // out_a += i conj(phi_aa) mu_a
 #pragma unroll
-        for (int e = 0; e < E; ++e) racc[e] = cadd(racc[e], mul_i(cmul(make_double2(x[e].x, -x[e].y), mA[e])));
+        for (int e = 0; e < E; ++e)
+          racc[e] = cadd(racc[e], mul_i(cmul(make_double2(x[e].x, -x[e].y), mA[TM::pos(tl, e)])));
       } else {
         // c = dk * conj(R); out_a += i (phi_ab + conj(c)(-1)^m) mu_b ; out_b += i conj(phi_ab) mu_a
         const double cx = dk * rnx, cy = -dk * rny;
@@ -100,14 +99,17 @@ __global__ void __launch_bounds__(kThreads) k_fock_adj(AdjFockArgs a) {
           const int q = TM::pos(tl, e);
           const double sg = (q & 1) ? -1.0 : 1.0;
           const double2 pr = make_double2(fma(sg, cx, x[e].x), fma(-sg, cy, x[e].y));
-          racc[e] = cadd(racc[e], mul_i(cmul(pr, mB[e])));
-          col[q] = cadd(col[q], mul_i(cmul(make_double2(x[e].x, -x[e].y), mA[e])));
+          racc[e] = cadd(racc[e], mul_i(cmul(pr, mB[q])));
+          col[q] = cadd(col[q], mul_i(cmul(make_double2(x[e].x, -x[e].y), mA[q])));
         }
       }
     }
     // ---- pass B: phi'_ab = Phi_ab[mu_a conj(v_b) - v_a conj(mu_b)]
 #pragma unroll
-    for (int e = 0; e < E; ++e) x[e] = csub(cmulc(mA[e], vB[e]), cmulc(vA[e], mB[e]));
+    for (int e = 0; e < E; ++e) {
+      const int q = TM::pos(tl, e);
+      x[e] = csub(cmulc(mA[q], vB[q]), cmulc(vA[q], mB[q]));
+    }
     fft_team<N, -1>(x, buf, tw_s, tl);
     rnx = __shfl_sync(0xffffffffu, x[TM::R0 / 2].x, team_lane0);
     rny = __shfl_sync(0xffffffffu, x[TM::R0 / 2].y, team_lane0);
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(kThreads) k_fock_adj(AdjFockArgs a) {
     if (valid) {
       // out_a += i v_b phi'_ab
 #pragma unroll
-      for (int e = 0; e < E; ++e) racc[e] = cadd(racc[e], mul_i(cmul(vB[e], x[e])));
+      for (int e = 0; e < E; ++e) racc[e] = cadd(racc[e], mul_i(cmul(vB[TM::pos(tl, e)], x[e])));
       if (!self) {
         // phi'_ba = -conj(phi'_ab) - c' (-1)^m,  c' = dk conj(R');  out_b += i v_a phi'_ba
         const double cx = dk * rnx, cy = -dk * rny;
@@ -130,7 +132,7 @@ __global__ void __launch_bounds__(kThreads) k_fock_adj(AdjFockArgs a) {
           const int q = TM::pos(tl, e);
           const double sg = (q & 1) ? -1.0 : 1.0;
           const double2 pba = make_double2(-fma(sg, cx, x[e].x), fma(-sg, cy, x[e].y));
-          col[q] = cadd(col[q], mul_i(cmul(vA[e], pba)));
+          col[q] = cadd(col[q], mul_i(cmul(vA[q], pba)));
         }
       }
     }

@@ -102,42 +102,50 @@ __global__ void k_project(const double2* __restrict__ x, const double2* __restri
   if (lane == 0) M[wid] = make_double2(sr * weight, si * weight);
 }
 
-// Cyclic Jacobi for a complex Hermitian m x m matrix, one CTA per k.
-// The matrix is built from the lower triangle of M (i > j) with a real
-// diagonal, like the reference's whw/ubhub assembly.  Converged when the
-// off-diagonal Frobenius norm is below 1e-15 of the full norm or after 60
-// sweeps (flag set).  Eigenvalues ascending; vectors in columns of V.
+// Parallel (round-robin ordered) Jacobi for a complex Hermitian m x m matrix,
+// one CTA per k.  The matrix is built from the lower triangle of M (i > j)
+// with a real diagonal, like the reference's whw/ubhub assembly.  Each sweep
+// is m'-1 rounds (m' = m rounded up to even) of m'/2 disjoint rotations
+// applied together (A <- J^H A J with J a product of commuting plane
+// rotations), so a sweep costs O(m) barriers instead of O(m^2).  Converged
+// when the off-diagonal Frobenius norm is below 1e-15 of the full norm, or
+// after 60 sweeps (flag set).  Eigenvalues ascending; vectors in columns of V.
 constexpr int kJacMax = 64;
 __global__ void __launch_bounds__(128) k_jacobi(const double2* __restrict__ Min, int m,
                                                double* __restrict__ evals,
                                                double2* __restrict__ evecs, int* flag) {
   extern __shared__ double2 jsm[];
-  double2* A = jsm;            // m*m, A[i*m+j]
-  double2* V = jsm + m * m;    // m*m
+  const int mp = m + (m & 1);  // even size; a padded index has no coupling
+  double2* A = jsm;            // mp*mp, A[i*mp+j]
+  double2* V = jsm + mp * mp;  // mp*mp
   __shared__ double red[128];
-  __shared__ int order[kJacMax];
+  __shared__ int order[kJacMax + 1];
+  __shared__ int pp[kJacMax / 2 + 1], qq[kJacMax / 2 + 1];
+  __shared__ double rc[kJacMax / 2 + 1], rs[kJacMax / 2 + 1], rpr[kJacMax / 2 + 1], rpi[kJacMax / 2 + 1];
   const int k = blockIdx.x;
   const double2* Mk = Min + (size_t)k * m * m;
   const int tid = threadIdx.x;
-  for (int idx = tid; idx < m * m; idx += blockDim.x) {
-    const int i = idx / m, j = idx % m;
-    double2 v;
-    if (i > j) v = Mk[i * m + j];
-    else if (i < j) { v = Mk[j * m + i]; v.y = -v.y; }
-    else v = make_double2(Mk[i * m + i].x, 0.0);
+  for (int idx = tid; idx < mp * mp; idx += blockDim.x) {
+    const int i = idx / mp, j = idx % mp;
+    double2 v = make_double2(0.0, 0.0);
+    if (i < m && j < m) {
+      if (i > j) v = Mk[i * m + j];
+      else if (i < j) { v = Mk[j * m + i]; v.y = -v.y; }
+      else v = make_double2(Mk[i * m + i].x, 0.0);
+    }
     A[idx] = v;
     V[idx] = make_double2(i == j ? 1.0 : 0.0, 0.0);
   }
   __syncthreads();
+  const int np = mp / 2;
   bool converged = false;
   for (int sweep = 0; sweep < 60 && !converged; ++sweep) {
-    // off-diagonal and total norms
     double off = 0.0, tot = 0.0;
-    for (int idx = tid; idx < m * m; idx += blockDim.x) {
+    for (int idx = tid; idx < mp * mp; idx += blockDim.x) {
       const double2 v = A[idx];
       const double a2 = v.x * v.x + v.y * v.y;
       tot += a2;
-      if (idx / m != idx % m) off += a2;
+      if (idx / mp != idx % mp) off += a2;
     }
     red[tid] = off;
     __syncthreads();
@@ -150,80 +158,87 @@ __global__ void __launch_bounds__(128) k_jacobi(const double2* __restrict__ Min,
     tot = red[0];
     __syncthreads();
     if (off <= 1e-30 * tot || off == 0.0) { converged = true; break; }
-    for (int p = 0; p < m - 1; ++p) {
-      for (int q = p + 1; q < m; ++q) {
-        const double2 apq = A[p * m + q];
+    for (int round = 0; round < mp - 1; ++round) {
+      // circle-method pairing: player mp-1 is fixed
+      if (tid < np) {
+        int p, q;
+        if (tid == 0) { p = mp - 1; q = round; }
+        else { p = (round + tid) % (mp - 1); q = (round - tid + mp - 1) % (mp - 1); }
+        if (p > q) { const int t = p; p = q; q = t; }
+        pp[tid] = p;
+        qq[tid] = q;
+        const double2 apq = A[p * mp + q];
         const double mag = sqrt(apq.x * apq.x + apq.y * apq.y);
-        const double app = A[p * m + p].x, aqq = A[q * m + q].x;
-        if (mag == 0.0 || mag <= 1e-300) continue;
-        // zero A[p][q]: with apq = mag*e^{i phi}, rotate columns p, q by
-        // J = [[c, -s e^{i phi}], [s e^{-i phi}, c]] acting as A <- J^H A J.
-        const double tau = (aqq - app) / (2.0 * mag);
-        const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-        const double c = 1.0 / sqrt(1.0 + t * t);
-        const double s = t * c;
-        const double ph_r = apq.x / mag, ph_i = apq.y / mag;  // e^{i phi}
-        // column update: A[:,p], A[:,q]
-        for (int r = tid; r < m; r += blockDim.x) {
-          const double2 xp = A[r * m + p], xq = A[r * m + q];
-          // new_p = c xp - s e^{-i phi} xq ; new_q = s e^{i phi} xp + c xq
-          double2 np, nq;
-          np.x = c * xp.x - s * (ph_r * xq.x + ph_i * xq.y);
-          np.y = c * xp.y - s * (ph_r * xq.y - ph_i * xq.x);
-          nq.x = c * xq.x + s * (ph_r * xp.x - ph_i * xp.y);
-          nq.y = c * xq.y + s * (ph_r * xp.y + ph_i * xp.x);
-          A[r * m + p] = np;
-          A[r * m + q] = nq;
-          const double2 vp = V[r * m + p], vq = V[r * m + q];
-          double2 wp, wq;
-          wp.x = c * vp.x - s * (ph_r * vq.x + ph_i * vq.y);
-          wp.y = c * vp.y - s * (ph_r * vq.y - ph_i * vq.x);
-          wq.x = c * vq.x + s * (ph_r * vp.x - ph_i * vp.y);
-          wq.y = c * vq.y + s * (ph_r * vp.y + ph_i * vp.x);
-          V[r * m + p] = wp;
-          V[r * m + q] = wq;
+        if (mag <= 1e-300) {
+          rc[tid] = 1.0; rs[tid] = 0.0; rpr[tid] = 1.0; rpi[tid] = 0.0;
+        } else {
+          // zero A[p][q] with J = [[c, s e^{i phi}], [-s e^{-i phi}, c]], apq = mag e^{i phi}
+          const double tau = (A[q * mp + q].x - A[p * mp + p].x) / (2.0 * mag);
+          const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+          const double c = 1.0 / sqrt(1.0 + t * t);
+          rc[tid] = c;
+          rs[tid] = t * c;
+          rpr[tid] = apq.x / mag;
+          rpi[tid] = apq.y / mag;
         }
-        __syncthreads();
-        // row update: A[p,:], A[q,:] with the conjugate transpose
-        for (int r = tid; r < m; r += blockDim.x) {
-          const double2 xp = A[p * m + r], xq = A[q * m + r];
-          double2 np, nq;
-          // new_p = c xp - s e^{i phi} xq ; new_q = s e^{-i phi} xp + c xq
-          np.x = c * xp.x - s * (ph_r * xq.x - ph_i * xq.y);
-          np.y = c * xp.y - s * (ph_r * xq.y + ph_i * xq.x);
-          nq.x = c * xq.x + s * (ph_r * xp.x + ph_i * xp.y);
-          nq.y = c * xq.y + s * (ph_r * xp.y - ph_i * xp.x);
-          A[p * m + r] = np;
-          A[q * m + r] = nq;
-        }
-        __syncthreads();
-        if (tid == 0) {
-          A[p * m + q] = make_double2(0.0, 0.0);
-          A[q * m + p] = make_double2(0.0, 0.0);
-          A[p * m + p].y = 0.0;
-          A[q * m + q].y = 0.0;
-        }
-        __syncthreads();
       }
+      __syncthreads();
+      // columns p, q of A and V
+      for (int w = tid; w < np * mp; w += blockDim.x) {
+        const int pr = w / mp, r = w % mp;
+        const int p = pp[pr], q = qq[pr];
+        const double c = rc[pr], s = rs[pr], ph_r = rpr[pr], ph_i = rpi[pr];
+        const double2 xp = A[r * mp + p], xq = A[r * mp + q];
+        A[r * mp + p] = make_double2(c * xp.x - s * (ph_r * xq.x + ph_i * xq.y),
+                                     c * xp.y - s * (ph_r * xq.y - ph_i * xq.x));
+        A[r * mp + q] = make_double2(c * xq.x + s * (ph_r * xp.x - ph_i * xp.y),
+                                     c * xq.y + s * (ph_r * xp.y + ph_i * xp.x));
+        const double2 vp = V[r * mp + p], vq = V[r * mp + q];
+        V[r * mp + p] = make_double2(c * vp.x - s * (ph_r * vq.x + ph_i * vq.y),
+                                     c * vp.y - s * (ph_r * vq.y - ph_i * vq.x));
+        V[r * mp + q] = make_double2(c * vq.x + s * (ph_r * vp.x - ph_i * vp.y),
+                                     c * vq.y + s * (ph_r * vp.y + ph_i * vp.x));
+      }
+      __syncthreads();
+      // rows p, q (conjugate transpose)
+      for (int w = tid; w < np * mp; w += blockDim.x) {
+        const int pr = w / mp, r = w % mp;
+        const int p = pp[pr], q = qq[pr];
+        const double c = rc[pr], s = rs[pr], ph_r = rpr[pr], ph_i = rpi[pr];
+        const double2 xp = A[p * mp + r], xq = A[q * mp + r];
+        A[p * mp + r] = make_double2(c * xp.x - s * (ph_r * xq.x - ph_i * xq.y),
+                                     c * xp.y - s * (ph_r * xq.y + ph_i * xq.x));
+        A[q * mp + r] = make_double2(c * xq.x + s * (ph_r * xp.x + ph_i * xp.y),
+                                     c * xq.y + s * (ph_r * xp.y - ph_i * xp.x));
+      }
+      __syncthreads();
+      if (tid < np && rs[tid] != 0.0) {
+        const int p = pp[tid], q = qq[tid];
+        A[p * mp + q] = make_double2(0.0, 0.0);
+        A[q * mp + p] = make_double2(0.0, 0.0);
+        A[p * mp + p].y = 0.0;
+        A[q * mp + q].y = 0.0;
+      }
+      __syncthreads();
     }
   }
   if (!converged && tid == 0 && flag) *flag = 2;
-  // ascending order (stable selection by index on ties)
+  // ascending order over the m real indices (stable on ties)
   if (tid == 0) {
     for (int i = 0; i < m; ++i) order[i] = i;
     for (int i = 1; i < m; ++i) {
       const int oi = order[i];
-      const double v = A[oi * m + oi].x;
+      const double v = A[oi * mp + oi].x;
       int j = i - 1;
-      while (j >= 0 && A[order[j] * m + order[j]].x > v) { order[j + 1] = order[j]; --j; }
+      while (j >= 0 && A[order[j] * mp + order[j]].x > v) { order[j + 1] = order[j]; --j; }
       order[j + 1] = oi;
     }
   }
   __syncthreads();
-  for (int i = tid; i < m; i += blockDim.x) evals[(size_t)k * m + i] = A[order[i] * m + order[i]].x;
+  for (int i = tid; i < m; i += blockDim.x) evals[(size_t)k * m + i] = A[order[i] * mp + order[i]].x;
   for (int idx = tid; idx < m * m; idx += blockDim.x) {
     const int r = idx / m, cidx = idx % m;
-    evecs[(size_t)k * m * m + idx] = V[r * m + order[cidx]];  // [row][col]
+    evecs[(size_t)k * m * m + idx] = V[r * mp + order[cidx]];  // [row][col]
   }
 }
 
@@ -297,7 +312,12 @@ cudaError_t launch_project(int NG, const double2* x, const double2* y, int kstri
 cudaError_t launch_jacobi(const double2* M, int m, double* evals, double2* evecs, int nk,
                           int* flag, cudaStream_t s) {
   if (m > kJacMax) return cudaErrorInvalidValue;
-  const size_t smem = sizeof(double2) * 2 * (size_t)m * m;
+  const int mp = m + (m & 1);
+  const size_t smem = sizeof(double2) * 2 * (size_t)mp * mp;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
   k_jacobi<<<nk, 128, smem, s>>>(M, m, evals, evecs, flag);
   return cudaGetLastError();
 }
