@@ -44,6 +44,7 @@ extern "C" {
 #define MATTOHF_OPT_SYMMETRIC 4    /* 1: use the occupied-pair Hermitian symmetry when w == u (default 1) */
 #define MATTOHF_OPT_FOCK_DF64 6   /* 1: symmetric exchange transforms in double-float (2 x FP32, 48-bit
                                       significand) arithmetic on the FP32 pipe; default 0 (FP64) */
+#define MATTOHF_OPT_SYM_TILE 7     /* symmetric-exchange tile size (orbitals per CTA side); 0 = automatic */
 #define MATTOHF_OPT_L2_FLUSH 5     /* >0: bytes written between RK4 steps of mattohf_rk4_run, which then
                                       reports the summed per-step device time (benchmarking) */
 
@@ -191,6 +192,8 @@ mattohf_ctx* mattohf_batch_run(mattohf_batch* b, int run);
 int mattohf_batch_rk4_run(mattohf_batch* b, int nt, const double* dt, const double* A,
                           const double* Aave, double* Etot, double* Je, double* Nele);
 int mattohf_batch_last_run_ms(mattohf_batch* b, double* ms);
+/* Batch options: MATTOHF_OPT_FOCK_DF64 only. */
+int mattohf_batch_set_option(mattohf_batch* b, int option, long long value);
 
 /* Diagnostic (no reference counterpart): measured FP64 FMA throughput of
  * `device` in TFLOP/s (2 flops per DFMA), the roofline denominator of the

@@ -28,6 +28,7 @@ OPT_KERNEL_TIMING = 3
 OPT_SYMMETRIC = 4
 OPT_L2_FLUSH = 5
 OPT_FOCK_DF64 = 6
+OPT_SYM_TILE = 7
 
 # every symbol include/mattohf.h declares
 EXPORTS = [
@@ -40,7 +41,7 @@ EXPORTS = [
     "mattohf_synchronize", "mattohf_diag_fp64_peak", "mattohf_fock_noalloc",
     "mattohf_batch_create", "mattohf_batch_destroy", "mattohf_batch_last_error", "mattohf_batch_run",
     "mattohf_batch_rk4_run", "mattohf_batch_last_run_ms", "mattohf_adjoint", "mattohf_adjoint_timing",
-    "mattohf_fourier", "mattohf_vck", "mattohf_te_step",
+    "mattohf_fourier", "mattohf_vck", "mattohf_te_step", "mattohf_batch_set_option",
 ]
 
 
@@ -103,6 +104,7 @@ def load(path: str = LIB_PATH):
         "mattohf_batch_run": ([P, I], P),
         "mattohf_batch_rk4_run": ([P, I, D, D, D, D, D, D], I),
         "mattohf_batch_last_run_ms": ([P, D], I),
+        "mattohf_batch_set_option": ([P, I, C.c_longlong], I),
         "mattohf_adjoint": ([P, I, I, C.c_double, D, I, D, D, D], I),
         "mattohf_adjoint_timing": ([P, D, D], I),
         "mattohf_vck": ([P, D, I, D], I),

@@ -332,6 +332,9 @@ class Batch:
         self._check(self.lib.mattohf_batch_last_run_ms(self.h, C.byref(ms)))
         return ms.value
 
+    def set_option(self, opt: int, value: int):
+        self._check(self.lib.mattohf_batch_set_option(self.h, opt, int(value)))
+
     def close(self):
         if getattr(self, "h", None):
             for m in self.members:

@@ -77,6 +77,7 @@ struct mattohf_ctx {
   float2* d_kern_df = nullptr;
   float4* d_tw_df = nullptr;
   int opt_df = 0;             // exchange transforms in double-float arithmetic
+  int opt_tile = 0;           // symmetric-exchange tile size (0 = automatic)
   int* d_int = nullptr;  // [0] = step counter, [1] = non-finite flag, [2] = solver flag
   // RT series
   double *d_A = nullptr, *d_Aave = nullptr, *d_sE = nullptr, *d_sJ = nullptr, *d_sN = nullptr;
@@ -263,12 +264,16 @@ int timed_end(mattohf_ctx* ctx) {
   return MATTOHF_OK;
 }
 
+int sym_tile(const mattohf_ctx* ctx) {
+  return ctx->opt_tile > 0 ? ctx->opt_tile : choose_sym_tile(ctx->NG, ctx->NK * ctx->NBocc);
+}
+
 // Every buffer the RK4 step's exchange applies need, allocated up front so a
 // graph capture never has to grow one.
 int ensure_fock_buffers(mattohf_ctx* ctx) {
   CKR(ensure_scratch(ctx, ctx->NK * ctx->NB));
   const int M = ctx->NK * ctx->NBocc;
-  const int S = choose_sym_tile(ctx->NG, M);
+  const int S = sym_tile(ctx);
   const int T = (M + S - 1) / S;
   CKR(ensure_sym(ctx, (size_t)T * (T + 1) / 2 * 2 * S * ctx->NG));
   if (!ctx->d_symF) CKR(dalloc(ctx, &ctx->d_symF, (size_t)M * ctx->NG));
@@ -286,7 +291,7 @@ int enq_fock(mattohf_ctx* ctx, Block u, Block w, FockPlan* plan) {
   const int NG = ctx->NG;
   if (same && ctx->opt_sym) {
     const int M = ctx->NK * ctx->NBocc;
-    const int S = choose_sym_tile(NG, M);
+    const int S = sym_tile(ctx);
     const int T = (M + S - 1) / S;
     CKR(ensure_sym(ctx, (size_t)T * (T + 1) / 2 * 2 * S * NG));
     if (!ctx->d_symF) CKR(dalloc(ctx, &ctx->d_symF, (size_t)M * NG));
@@ -721,6 +726,11 @@ int mattohf_set_option(mattohf_ctx* ctx, int option, long long value) {
     case MATTOHF_OPT_KERNEL_TIMING: ctx->opt_timing = value ? 1 : 0; break;
     case MATTOHF_OPT_SYMMETRIC: ctx->opt_sym = value ? 1 : 0; break;
     case MATTOHF_OPT_FOCK_DF64: ctx->opt_df = value ? 1 : 0; break;
+    case MATTOHF_OPT_SYM_TILE:
+      if (value < 0 || value > fock_sym_teams(ctx->NG) || (value & (value - 1)))
+        return fail(ctx, MATTOHF_ERR_ARG, "tile size must be 0 or a power of two up to the CTA's teams");
+      ctx->opt_tile = (int)value;
+      break;
     case MATTOHF_OPT_L2_FLUSH:
       if (value < 0 || value > (4LL << 30)) return fail(ctx, MATTOHF_ERR_ARG, "flush bytes out of range");
       ctx->opt_flush = value;
@@ -1269,7 +1279,7 @@ int enq_adjoint_step(mattohf_ctx* ctx, double dt, size_t elems) {
   const double cst[3] = {0.5 * dt, 0.5 * dt, dt};
   const int amodes[4] = {AM, AAVE, AAVE, ACUR};
   const int M = NK * ctx->NBocc;
-  const int S = choose_sym_tile(NG, M);
+  const int S = sym_tile(ctx);
   const int T = (M + S - 1) / S;
   for (int s = 3; s >= 0; --s) {
     CK(launch_stage_copy(ctx->d_vbuf, nullptr, ctx->d_store, n, seg0, s, elems, 0, ctx->st));
@@ -1375,7 +1385,7 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   CKR(ensure_series(ctx, nt));
   CKR(ensure_scratch(ctx, NK * NB));
   const int M = NK * ctx->NBocc;
-  const int S = choose_sym_tile(NG, M);
+  const int S = sym_tile(ctx);
   const int T = (M + S - 1) / S;
   CKR(ensure_sym(ctx, (size_t)T * (T + 1) / 2 * 2 * S * NG));
   if (!ctx->d_symF) CKR(dalloc(ctx, &ctx->d_symF, (size_t)M * NG));
@@ -1579,7 +1589,9 @@ struct mattohf_batch {
   static constexpr int kVariants = 6;  // stages 0..3, observables, observables with exchange
   DensArgs* d_dens[kVariants] = {};
   FockSymArgs* d_fsym[kVariants] = {};
+  FockSymDfArgs* d_fsym_df[kVariants] = {};
   CombineArgs* d_comb[kVariants] = {};
+  int opt_df = 0;  // exchange transforms in double-float arithmetic
   ObsReduceArgs* d_obs = nullptr;
   ExArgs* d_ex = nullptr;
   ExArgs* d_exf = nullptr;
@@ -1616,6 +1628,15 @@ int bupload(mattohf_batch* b, T** d, const std::vector<T>& h) {
   return MATTOHF_OK;
 }
 
+// Exchange partials of every run for argument variant v (FP64 or double-float).
+cudaError_t batch_exchange(mattohf_batch* b, int v) {
+  if (b->opt_df)
+    return launch_fock_sym_df_batch(b->NG, b->d_fsym[v], b->d_fsym_df[v], b->d_tile_pre, b->R, b->total_tiles,
+                                    b->d_elem_pre, b->total_elems, b->st);
+  return launch_fock_sym_batch(b->NG, b->d_fsym[v], b->d_tile_pre, b->R, b->total_tiles, b->d_elem_pre,
+                               b->total_elems, b->st);
+}
+
 // (Re)build every per-run argument array for runs of `nt` steps.
 int batch_prepare(mattohf_batch* b, int nt) {
   if (b->built_nt >= nt && b->exec) return MATTOHF_OK;
@@ -1626,6 +1647,7 @@ int batch_prepare(mattohf_batch* b, int nt) {
   const int R = b->R, NG = b->NG;
   std::vector<DensArgs> dens[mattohf_batch::kVariants];
   std::vector<FockSymArgs> fsym[mattohf_batch::kVariants];
+  std::vector<FockSymDfArgs> fsdf[mattohf_batch::kVariants];
   std::vector<CombineArgs> comb[mattohf_batch::kVariants];
   std::vector<ObsReduceArgs> obs(R);
   std::vector<ExArgs> ex(R), exf(R);
@@ -1641,6 +1663,7 @@ int batch_prepare(mattohf_batch* b, int nt) {
     const int T = (M + S - 1) / S;
     if ((rc = ensure_sym(ctx, (size_t)T * (T + 1) / 2 * 2 * S * NG))) return bfail(b, rc, ctx->err);
     if (!ctx->d_symF && (rc = dalloc(ctx, &ctx->d_symF, (size_t)M * NG))) return bfail(b, rc, ctx->err);
+    if (!ctx->d_udf && (rc = dalloc(ctx, &ctx->d_udf, (size_t)M * NG))) return bfail(b, rc, ctx->err);
     tile_pre[r + 1] = tile_pre[r] + T * (T + 1) / 2;
     elem_pre[r + 1] = elem_pre[r] + M * NG;
     cta_pre[r + 1] = cta_pre[r] + (ctx->NK * ctx->NB + cpc - 1) / cpc;
@@ -1686,6 +1709,17 @@ int batch_prepare(mattohf_batch* b, int nt) {
       f.scratch = ctx->d_sym;
       f.F = ctx->d_symF;
       fsym[v].push_back(f);
+      FockSymDfArgs fd;
+      fd.u = ctx->d_udf;
+      fd.nk = ctx->NK;
+      fd.nbocc = ctx->NBocc;
+      fd.S = S;
+      fd.T = T;
+      fd.kern = ctx->d_kern_df;
+      fd.tw = ctx->d_tw_df;
+      fd.scratch = reinterpret_cast<float4*>(ctx->d_sym);
+      fd.F = ctx->d_symF;
+      fsdf[v].push_back(fd);
       FockPlan fp;
       fp.any = (v != 4);
       fp.sym = ctx->d_symF;
@@ -1733,7 +1767,7 @@ int batch_prepare(mattohf_batch* b, int nt) {
   int rc;
   for (int v = 0; v < mattohf_batch::kVariants; ++v) {
     if ((rc = bupload(b, &b->d_dens[v], dens[v])) || (rc = bupload(b, &b->d_fsym[v], fsym[v])) ||
-        (rc = bupload(b, &b->d_comb[v], comb[v])))
+        (rc = bupload(b, &b->d_fsym_df[v], fsdf[v])) || (rc = bupload(b, &b->d_comb[v], comb[v])))
       return rc;
   }
   if ((rc = bupload(b, &b->d_obs, obs)) || (rc = bupload(b, &b->d_ex, ex)) || (rc = bupload(b, &b->d_exf, exf)) ||
@@ -1750,9 +1784,7 @@ int batch_prepare(mattohf_batch* b, int nt) {
   cudaError_t e = cudaSuccess;
   for (int s = 0; s < 4 && e == cudaSuccess; ++s) {
     e = launch_density_batch(NG, b->d_dens[s], R, b->st);
-    if (e == cudaSuccess)
-      e = launch_fock_sym_batch(NG, b->d_fsym[s], b->d_tile_pre, R, b->total_tiles, b->d_elem_pre,
-                                b->total_elems, b->st);
+    if (e == cudaSuccess) e = batch_exchange(b, s);
     if (e == cudaSuccess) e = launch_combine_batch(NG, b->d_comb[s], b->d_cta_pre, R, b->total_ctas, b->st);
     if (e == cudaSuccess && s == 0) e = launch_ex_finalize_batch(b->d_ex, R, b->st);
   }
@@ -1814,6 +1846,7 @@ int mattohf_batch_destroy(mattohf_batch* b) {
   for (int v = 0; v < mattohf_batch::kVariants; ++v) {
     cudaFree(b->d_dens[v]);
     cudaFree(b->d_fsym[v]);
+    cudaFree(b->d_fsym_df[v]);
     cudaFree(b->d_comb[v]);
   }
   void* ptrs[] = {b->d_obs, b->d_ex, b->d_exf, b->d_tile_pre, b->d_elem_pre, b->d_cta_pre, b->d_int};
@@ -1883,7 +1916,7 @@ int mattohf_batch_rk4_run(mattohf_batch* b, int nt, const double* dt, const doub
   // exchange energy of the last step's orbitals
   const int NG = b->NG;
   BCK(launch_density_batch(NG, b->d_dens[5], b->R, b->st));
-  BCK(launch_fock_sym_batch(NG, b->d_fsym[5], b->d_tile_pre, b->R, b->total_tiles, b->d_elem_pre, b->total_elems, b->st));
+  BCK(batch_exchange(b, 5));
   BCK(launch_combine_batch(NG, b->d_comb[5], b->d_cta_pre, b->R, b->total_ctas, b->st));
   BCK(launch_ex_finalize_batch(b->d_exf, b->R, b->st));
   BCK(cudaEventRecord(e1, b->st));
@@ -1903,6 +1936,18 @@ int mattohf_batch_rk4_run(mattohf_batch* b, int nt, const double* dt, const doub
   BCK(cudaMemcpyAsync(&flag, b->d_int + 1, sizeof(int), cudaMemcpyDeviceToHost, b->st));
   BCK(cudaStreamSynchronize(b->st));
   if (flag) return bfail(b, MATTOHF_ERR_NONFINITE, "non-finite state in the ensemble");
+  return MATTOHF_OK;
+}
+
+int mattohf_batch_set_option(mattohf_batch* b, int option, long long value) {
+  if (!b) return MATTOHF_ERR_ARG;
+  if (option != MATTOHF_OPT_FOCK_DF64) return bfail(b, MATTOHF_ERR_ARG, "unsupported batch option");
+  b->opt_df = value ? 1 : 0;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  b->built_nt = -1;
   return MATTOHF_OK;
 }
 

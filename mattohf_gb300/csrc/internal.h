@@ -102,6 +102,9 @@ struct FockSymDfArgs {
 cudaError_t launch_fock_sym_df(int NG, const FockSymDfArgs& a, const double2* u, int kstride, float4* udf,
                                cudaStream_t s);
 cudaError_t configure_df_kernels();
+cudaError_t launch_fock_sym_df_batch(int NG, const FockSymArgs* d_src, const FockSymDfArgs* d_args,
+                                     const int* d_tile_pre, int nruns, int total_tiles, const int* d_elem_pre,
+                                     int total_elems, cudaStream_t s);
 cudaError_t launch_to_df_tables(const double* kern, int nkern, float2* kern_df, const double2* tw, int ntw,
                                 float4* tw_df, cudaStream_t s);
 

@@ -13,7 +13,7 @@
 namespace mattohf {
 
 template <int N>
-__global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) {
+__device__ __forceinline__ void fock_sym_df_body(const FockSymDfArgs& a, const int tile) {
   using TM = Team<N>;
   using df::cdf;
   constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) {
     z.im = make_float2(0.f, 0.f);
     cacc[i] = z;
   }
-  int ti = 0, rem = blockIdx.x;
+  int ti = 0, rem = tile;
   while (rem >= a.T - ti) { rem -= a.T - ti; ++ti; }
   const int tj = ti + rem;
   const int M = a.nk * a.nbocc;
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) {
     __syncthreads();
   }
   // partials stay double-float; k_sym_reduce_df sums them and converts once
-  float4* dst = a.scratch + (size_t)blockIdx.x * 2 * S * N;
+  float4* dst = a.scratch + (size_t)tile * 2 * S * N;
   if (tw_ < S) {
 #pragma unroll
     for (int e = 0; e < E; ++e) df::store(dst + (size_t)tw_ * N + TM::pos(tl, e), racc[e]);
@@ -119,11 +119,31 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) {
   for (int i = tid; i < S * N; i += blockDim.x) df::store(dst + (size_t)S * N + i, cacc[i]);
 }
 
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_fock_sym_df(FockSymDfArgs a) { fock_sym_df_body<N>(a, blockIdx.x); }
+
+__device__ __forceinline__ int df_find_run(const int* __restrict__ pre, int nruns, int i) {
+  int lo = 0, hi = nruns - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pre[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// many runs per launch: tile pairs of all runs, mapped through a prefix array
+template <int N>
+__global__ void __launch_bounds__(kThreads) k_fock_sym_df_batch(const FockSymDfArgs* __restrict__ args,
+                                                              const int* __restrict__ pre, int nruns) {
+  const int r = df_find_run(pre, nruns, blockIdx.x);
+  fock_sym_df_body<N>(args[r], blockIdx.x - pre[r]);
+}
+
 // Ordered double-float sum of the tile partials of every occupied output,
 // converted to FP64 once (same order as k_sym_reduce).
-__global__ void k_sym_reduce_df(const float4* __restrict__ part, int S, int T, int M, int N,
-                                double2* __restrict__ F) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void sym_reduce_df_body(const float4* __restrict__ part, int S, int T, int M, int N,
+                                                   double2* __restrict__ F, int idx) {
   if (idx >= M * N) return;
   const int o = idx / N, q = idx % N;
   const int i = o / S, l = o % S;
@@ -139,6 +159,33 @@ __global__ void k_sym_reduce_df(const float4* __restrict__ part, int S, int T, i
   }
   for (int j = i + 1; j < T; ++j) f = df::cadd(f, df::load(part + (size_t)sym_tp(i, j, T) * 2 * SN + (size_t)l * N + q));
   F[idx] = df::to_double2(f);
+}
+
+__global__ void k_sym_reduce_df(const float4* __restrict__ part, int S, int T, int M, int N,
+                                double2* __restrict__ F) {
+  sym_reduce_df_body(part, S, T, M, N, F, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void k_sym_reduce_df_batch(const FockSymDfArgs* __restrict__ args, const int* __restrict__ pre,
+                                      int nruns, int N) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= pre[nruns]) return;
+  const int r = df_find_run(pre, nruns, idx);
+  const FockSymDfArgs& a = args[r];
+  sym_reduce_df_body(a.scratch, a.S, a.T, a.nk * a.nbocc, N, a.F, idx - pre[r]);
+}
+
+// df copies of every run's occupied orbitals (element prefix as for the reduction)
+__global__ void k_orb_to_df_batch(const FockSymArgs* __restrict__ src, const FockSymDfArgs* __restrict__ dst,
+                                  const int* __restrict__ pre, int nruns, int N) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= pre[nruns]) return;
+  const int r = df_find_run(pre, nruns, idx);
+  const int i = idx - pre[r];
+  const FockSymArgs& s = src[r];
+  const int o = i / N, g = i % N;
+  const int k = o / s.nbocc, b = o % s.nbocc;
+  df::store(const_cast<float4*>(dst[r].u) + i, df::from_double2(s.u.p[(size_t)k * s.u.kstride + (size_t)b * N + g]));
 }
 
 // occupied orbitals (FP64, [NK][NB][NG]) -> df copy [NK*NBocc][NG]
@@ -191,6 +238,29 @@ static cudaError_t fock_df_impl(const FockSymDfArgs& a, const double2* u, int ks
   return cudaGetLastError();
 }
 
+template <int N>
+static cudaError_t fock_df_batch_impl(const FockSymArgs* d_src, const FockSymDfArgs* d_args, const int* d_tile_pre,
+                                      int nruns, int total_tiles, const int* d_elem_pre, int total_elems,
+                                      cudaStream_t s) {
+  k_orb_to_df_batch<<<(total_elems + 255) / 256, 256, 0, s>>>(d_src, d_args, d_elem_pre, nruns, N);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || total_tiles <= 0) return e;
+  constexpr int NTEAM = (kThreads / 32) * Team<N>::PER_WARP;
+  const size_t smem = sizeof(float4) * (size_t)N * (1 + 2 * NTEAM);
+  k_fock_sym_df_batch<N><<<total_tiles, kThreads, smem, s>>>(d_args, d_tile_pre, nruns);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  k_sym_reduce_df_batch<<<(total_elems + 255) / 256, 256, 0, s>>>(d_args, d_elem_pre, nruns, N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fock_sym_df_batch(int NG, const FockSymArgs* d_src, const FockSymDfArgs* d_args,
+                                     const int* d_tile_pre, int nruns, int total_tiles, const int* d_elem_pre,
+                                     int total_elems, cudaStream_t s) {
+#define CALL(n) fock_df_batch_impl<n>(d_src, d_args, d_tile_pre, nruns, total_tiles, d_elem_pre, total_elems, s)
+  MATTOHF_DISPATCH(NG, CALL)
+#undef CALL
+}
+
 cudaError_t launch_fock_sym_df(int NG, const FockSymDfArgs& a, const double2* u, int kstride, float4* udf,
                                cudaStream_t s) {
 #define CALL(n) fock_df_impl<n>(a, u, kstride, udf, s)
@@ -202,7 +272,9 @@ template <int N>
 static cudaError_t configure_df_impl() {
   constexpr int NTEAM = (kThreads / 32) * Team<N>::PER_WARP;
   const size_t smem = sizeof(float4) * (size_t)N * (1 + 2 * NTEAM);
-  return cudaFuncSetAttribute(k_fock_sym_df<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(k_fock_sym_df<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_fock_sym_df_batch<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 cudaError_t configure_df_kernels() {

@@ -67,3 +67,39 @@ def test_batch_against_oracle(built_lib):
     ref = O.rt_calculation(S, u2, nt=nt, A=A[2], Aave=Aave[2])
     assert np.max(np.abs(E[2] - ref.Etot)) <= 1e-10 * np.max(np.abs(ref.Etot))
     assert np.max(np.abs(J[2] - ref.Jtot)) <= 1e-10
+
+
+def test_batch_double_float_matches_single_runs(built_lib):
+    """Batched double-float exchange vs the same runs advanced one at a time in double-float,
+    and vs the FP64 batch within the 1e-10 real-time tolerance."""
+    from mattohf_gb300 import Batch, Context, _capi
+    cfgs = _cfgs()
+    nt = 4
+    rng = np.random.default_rng(3)
+    A = 0.02 * rng.standard_normal((len(cfgs), nt))
+    Aave = np.concatenate([0.5 * A[:, :1], 0.5 * (A[:, 1:] + A[:, :-1])], axis=1)
+    dts = np.array([0.004, 0.003, 0.002, 0.004, 0.005])
+    with Batch(cfgs) as b:
+        u0 = []
+        for r in range(len(cfgs)):
+            b[r].Init_wf()
+            b[r].Gram_Schmidt()
+            u0.append(b[r].get_orbitals())
+        E64, J64, _ = b.rk4_run(A, Aave, dts)
+        for r in range(len(cfgs)):
+            b[r].set_orbitals(u0[r])
+        b.set_option(_capi.OPT_FOCK_DF64, 1)
+        E, J, N = b.rk4_run(A, Aave, dts)
+        ub = [b[r].get_orbitals() for r in range(len(cfgs))]
+    assert np.max(np.abs(E - E64)) <= 1e-10 * np.max(np.abs(E64))
+    assert np.max(np.abs(J - J64)) <= 1e-10 * max(1.0, np.max(np.abs(J64)))
+    for r, cfg in enumerate(cfgs):
+        with Context(cfg) as c:
+            c.set_option(_capi.OPT_FOCK_DF64, 1)
+            c.set_orbitals(u0[r])
+            e, j, n = c.rk4_run(A[r], Aave[r], dts[r])
+            us = c.get_orbitals()
+        assert np.max(np.abs(e - E[r])) <= 1e-12 * np.max(np.abs(e)), r
+        assert np.max(np.abs(j - J[r])) <= 1e-12 * max(1.0, np.max(np.abs(j))), r
+        assert np.max(np.abs(n - N[r])) <= 1e-12 * np.max(np.abs(n)), r
+        assert np.max(np.abs(us - ub[r])) <= 1e-11 * np.max(np.abs(us)), r
