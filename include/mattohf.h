@@ -107,6 +107,25 @@ int mattohf_hpsi(mattohf_ctx* ctx, const double* ubk, const double* wbk, int nbw
 /* Same on device pointers, asynchronous on the context stream. */
 int mattohf_hpsi_device(mattohf_ctx* ctx, const double* d_ubk, const double* d_wbk, int nbw,
                         double A, double* d_hwbk);
+/* One rank's share of a run split over ranks by OUTPUT k-point.  The reference
+ * splits the (k,k') pairs of ubkwbk_vFwbk over MPI ranks (NKK ranges,
+ * src/Initialization.f90:64-76, loop src/Functions.f90:247) and all-reduces
+ * the whole result (src/Functions.f90:258).  Here each rank owns whole output
+ * k-points k0 .. k0+nkl-1: it needs the occupied orbitals of every k-point (one
+ * all-gather by the caller) and no reduction of the result.
+ * d_uocc: [NK][NBocc][NG] occupied orbitals of all k-points; d_wbk, d_hwbk:
+ * [nkl][nbw][NG]; all device memory, asynchronous on the context stream.
+ * term 0 = h[u] w (ubkwbk_hwbk rows), 1 = exchange only (ubkwbk_vFwbk rows),
+ * 2 = kinetic only (ubk_tubk rows). */
+int mattohf_hpsi_kslice_device(mattohf_ctx* ctx, const double* d_uocc, int k0, int nkl,
+                               const double* d_wbk, int nbw, double A, int term, double* d_hwbk);
+/* Observables of the k-slice [k0, k0+nkl) of a split run (d_ubk: [nkl][NB][NG]).
+ * partial = {Ekin, Je, Ex} contributions of the slice (sum them over ranks);
+ * scal = {Nele, Eion, EH} of the whole density (the same on every rank).
+ * Etot = sum(Ekin) + Eion + EH + sum(Ex) (F:74-91, F:165-183, F:289-318).
+ * Synchronous. */
+int mattohf_observables_kslice_device(mattohf_ctx* ctx, const double* d_uocc, int k0, int nkl,
+                                      const double* d_ubk, double A, double* partial, double* scal);
 /* ubkwbk_vFwbk (src/Functions.f90:237-261): the Fock term alone. */
 int mattohf_fock(mattohf_ctx* ctx, const double* ubk, const double* wbk, int nbw, double* vFwbk);
 /* ubk_tubk (src/Functions.f90:212-234): the kinetic term alone. */

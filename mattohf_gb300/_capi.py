@@ -36,6 +36,7 @@ EXPORTS = [
     "mattohf_set_option", "mattohf_get_grids", "mattohf_get_coulomb", "mattohf_get_vion",
     "mattohf_set_vion", "mattohf_set_orbitals", "mattohf_get_orbitals", "mattohf_init_wf",
     "mattohf_gram_schmidt", "mattohf_hpsi", "mattohf_hpsi_device", "mattohf_fock",
+    "mattohf_hpsi_kslice_device", "mattohf_observables_kslice_device",
     "mattohf_kinetic", "mattohf_density", "mattohf_observables", "mattohf_rk4_step",
     "mattohf_rk4_run", "mattohf_last_run_timing", "mattohf_gs_run", "mattohf_eps",
     "mattohf_synchronize", "mattohf_diag_fp64_peak", "mattohf_fock_noalloc",
@@ -86,6 +87,8 @@ def load(path: str = LIB_PATH):
         "mattohf_gram_schmidt": ([P], I),
         "mattohf_hpsi": ([P, D, D, I, C.c_double, D], I),
         "mattohf_hpsi_device": ([P, P, P, I, C.c_double, P], I),
+        "mattohf_hpsi_kslice_device": ([P, P, I, I, P, I, C.c_double, I, P], I),
+        "mattohf_observables_kslice_device": ([P, P, I, I, P, C.c_double, D, D], I),
         "mattohf_fock": ([P, D, D, I, D], I),
         "mattohf_kinetic": ([P, D, I, C.c_double, D], I),
         "mattohf_density": ([P, D, D, D], I),

@@ -882,6 +882,88 @@ int mattohf_hpsi_device(mattohf_ctx* ctx, const double* d_ubk, const double* d_w
                   blko((double2*)d_hwbk, nbw, NG, nbw), aval(A), CM_H);
 }
 
+// Rows of the output k-points k0 .. k0+nkl-1 only.  The pair kernel and the
+// combine index the kernel table by d = kr - kc + NK - 1 and kx by kr, so a
+// slice is the same launch with kern and kx advanced by k0 rows.
+static int kslice_args(mattohf_ctx* ctx, const double* d_uocc, int k0, int nkl, const double* d_w, int nbw) {
+  CKR(check_ctx(ctx));
+  if (!d_uocc || !d_w || nbw < 1 || nkl < 1 || k0 < 0 || k0 + nkl > ctx->NK)
+    return fail(ctx, MATTOHF_ERR_ARG, "bad k-slice arguments");
+  return MATTOHF_OK;
+}
+
+static int enq_kslice(mattohf_ctx* ctx, const double* d_uocc, int k0, int nkl, const double* d_w, int nbw,
+                      AField af, int mode, BlockOut out) {
+  const int NG = ctx->NG;
+  Block u = blk((const double2*)d_uocc, ctx->NBocc, NG, ctx->NBocc);
+  Block w = blk((const double2*)d_w, nbw, NG, nbw);
+  const int ncols = nkl * nbw;
+  if (mode == CM_H || mode == CM_OBS) CKR(enq_density(ctx, u));
+  CKR(ensure_scratch(ctx, ncols));
+  FockPlan fp;
+  if (ctx->hf && mode != CM_T) {
+    FockArgs a;
+    a.u = u;
+    a.w = w;
+    a.nk = ctx->NK;
+    a.nbocc = ctx->NBocc;
+    a.kern = ctx->d_kern + (size_t)k0 * NG;
+    a.tw = ctx->tw;
+    a.scratch = ctx->d_scratch;
+    fock_split(ctx, ncols, &a.nchunks, &a.chunk);
+    fp.nchunks = a.nchunks;
+    fp.any = true;
+    CK(launch_fock(NG, a, ncols, ctx->st));
+  } else if (mode == CM_F) {
+    CK(cudaMemsetAsync(out.p, 0, sizeof(double2) * (size_t)nkl * out.kstride, ctx->st));
+    return MATTOHF_OK;
+  }
+  CombineArgs c = combine_base(ctx, w, af, mode, fp);
+  c.kx = ctx->d_kx + k0;
+  c.nk = nkl;
+  c.out = out;
+  CK(launch_combine(NG, c, ncols, ctx->st));
+  return MATTOHF_OK;
+}
+
+int mattohf_hpsi_kslice_device(mattohf_ctx* ctx, const double* d_uocc, int k0, int nkl, const double* d_wbk,
+                               int nbw, double A, int term, double* d_hwbk) {
+  CKR(kslice_args(ctx, d_uocc, k0, nkl, d_wbk, nbw));
+  if (!d_hwbk || term < 0 || term > 2) return fail(ctx, MATTOHF_ERR_ARG, "bad k-slice output or term");
+  const int mode = term == 0 ? CM_H : (term == 1 ? CM_F : CM_T);
+  return enq_kslice(ctx, d_uocc, k0, nkl, d_wbk, nbw, aval(A), mode,
+                    blko((double2*)d_hwbk, nbw, ctx->NG, nbw));
+}
+
+int mattohf_observables_kslice_device(mattohf_ctx* ctx, const double* d_uocc, int k0, int nkl,
+                                      const double* d_ubk, double A, double* partial, double* scal) {
+  CKR(kslice_args(ctx, d_uocc, k0, nkl, d_ubk, ctx->NB));
+  if (!partial || !scal) return fail(ctx, MATTOHF_ERR_ARG, "null observable outputs");
+  const int NB = ctx->NB;
+  CKR(enq_kslice(ctx, d_uocc, k0, nkl, d_ubk, NB, aval(A), CM_OBS, BlockOut()));
+  std::vector<double> cb((size_t)nkl * NB * 4);
+  double s[3];
+  CK(cudaMemcpyAsync(cb.data(), ctx->d_colbuf, sizeof(double) * cb.size(), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(s, ctx->d_scal, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->st));
+  CKR(sync_and_flag(ctx));
+  // the single-context reduction's column order (k, then band)
+  double ekin = 0.0, jre = 0.0, exr = 0.0;
+  for (int c = 0; c < nkl * NB; ++c) {
+    const int ib = c % NB;
+    const double occ = ib < ctx->NBocc ? ctx->occ : 0.0;
+    ekin += occ * cb[(size_t)c * 4] * ctx->dvcell;
+    jre += occ * cb[(size_t)c * 4 + 1];
+    if (ib < ctx->NBocc) exr += occ * cb[(size_t)c * 4 + 2] * ctx->dvcell;
+  }
+  partial[0] = ekin;
+  partial[1] = -(jre * ctx->dvcell / ctx->vcell);
+  partial[2] = ctx->hf ? 0.5 * exr : 0.0;
+  scal[0] = s[0];
+  scal[1] = s[1];
+  scal[2] = s[2];
+  return MATTOHF_OK;
+}
+
 int mattohf_density(mattohf_ctx* ctx, const double* ubk, double* dns, double* vH) {
   CKR(check_ctx(ctx));
   if (!ubk) return fail(ctx, MATTOHF_ERR_ARG, "null ubk");
