@@ -33,6 +33,8 @@ WORKLOAD = dict(acell=10.0, NG=256, NK=64, NB=4, NBocc=4, Zeff=[1.5, 0.5], alpha
                 Rion=[0.25, 0.75], Kion=[1, 2])
 PULSE = dict(A0=0.1, w=0.057, T=600.0)
 DT = 7e-4
+# DRAM bytes (read + write) of one symmetric-exchange launch on WORKLOAD, ncu
+FOCK_SYM_DRAM_BYTES_NG256_NK64_NB4 = 1_242_624 + 7_576_064
 NSCF_INIT, NCG_INIT = 3, 4
 METRIC = "TDHF RK4 steps/s"
 WORKLOAD_NAME = ("plain HF RK4, exchange-dominated: a=10, NG=256, NK=64, Nocc=NB=4, "
@@ -272,11 +274,11 @@ def run_gpu(args, dist):
     achieved = flops / (fock_ms / nf * 1e-3) / 1e12
     peak = C.c_double()
     lib.mattohf_diag_fp64_peak(dev, C.byref(peak))
+    # dram__bytes_read.sum + dram__bytes_write.sum of one k_fock_sym<256> launch on
+    # this workload, from the ncu capture in profiles/k_fock_sym_ng256_nk64_nb4.md
     prof_traffic = None
-    tp = os.path.join(ROOT, "profiles", "fock_traffic.json")
-    if os.path.exists(tp):
-        with open(tp) as fh:
-            prof_traffic = json.load(fh).get("bytes_per_launch")
+    if (cfg.NG, cfg.NK, cfg.NBocc) == (256, 64, 4):
+        prof_traffic = FOCK_SYM_DRAM_BYTES_NG256_NK64_NB4
 
     # --- the same timed region with the exchange transforms in double-float
     #     arithmetic (MATTOHF_OPT_FOCK_DF64; parity-tested at the FP64 tolerances)
@@ -334,7 +336,7 @@ def run_gpu(args, dist):
                        "l2": "flushed (512 MiB write) between timed steps", "graph": True},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                          "frac": achieved / peak.value if peak.value else None,
-                         "traffic": prof_traffic, "kernel": "k_fock",
+                         "traffic": prof_traffic, "kernel": "k_fock_sym",
                          "flops_per_launch": flops, "launch_ms": fock_ms / nf,
                          "peak_source": "measured DFMA throughput on this GPU (mattohf_diag_fp64_peak)",
                          "flops_model": "symmetric exchange: M(M+1)/2 pairs x (10 N log2 N + 16 N) + M(M-1)/2 x 8 N, M = NK*NBocc"},
