@@ -48,6 +48,8 @@ CONFIGS = {
     "ng512_nk2": make_cfg(NG=512, NK=2, NB=2, NBocc=1),
     "ng32_nk1": make_cfg(NG=32, NK=1, NB=2, NBocc=2),        # single k-point: one kernel column
     "ng64_nk5_nb4": make_cfg(NG=64, NK=5, NB=4, NBocc=3, acell=7.0),
+    # any functional but 'HF' drops the exchange term (src/Functions.f90:85-87, 204-207, 276-278)
+    "ng64_nk4_no_exchange": make_cfg(NG=64, NK=4, NB=3, NBocc=2, functional="PZ"),
 }
 
 _cache = {}
