@@ -55,6 +55,9 @@ struct mattohf_ctx {
   std::vector<double> Zeff, alpha, Rion;
   std::vector<int> Kion;
   cudaStream_t st = nullptr;
+  // side stream: the density of an RK4 stage runs beside that stage's exchange
+  cudaStream_t st_side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // tables
   double2* tw = nullptr;
   double *d_Gx = nullptr, *d_kx = nullptr, *d_vCG = nullptr, *d_vcq = nullptr, *d_kern = nullptr;
@@ -207,7 +210,7 @@ AField aval(double A) {
   return f;
 }
 
-int enq_density(mattohf_ctx* ctx, Block u) {
+int enq_density(mattohf_ctx* ctx, Block u, cudaStream_t st = nullptr) {
   DensArgs a;
   a.u = u;
   a.nbocc = ctx->NBocc;
@@ -223,7 +226,7 @@ int enq_density(mattohf_ctx* ctx, Block u) {
   a.part = ctx->d_dpart;
   a.mu = nullptr;
   a.gvion = nullptr;
-  CK(launch_density(ctx->NG, a, ctx->st));
+  CK(launch_density(ctx->NG, a, st ? st : ctx->st));
   return MATTOHF_OK;
 }
 
@@ -478,9 +481,18 @@ int enq_rk4(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt,
   for (int s = 0; s < 4; ++s) {
     const double2* in = (s == 0) ? ctx->d_u : ctx->d_us;
     Block ub = blk(in, NB, NG, NB);
-    CKR(enq_density(ctx, ub));
     FockPlan fp;
-    if (ctx->hf) CKR(enq_fock(ctx, ub, ub, &fp));
+    if (ctx->hf) {
+      // the density (read only by the combine) runs beside the exchange
+      CK(cudaEventRecord(ctx->ev_fork, ctx->st));
+      CK(cudaStreamWaitEvent(ctx->st_side, ctx->ev_fork, 0));
+      CKR(enq_density(ctx, ub, ctx->st_side));
+      CK(cudaEventRecord(ctx->ev_join, ctx->st_side));
+      CKR(enq_fock(ctx, ub, ub, &fp));
+      CK(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
+    } else {
+      CKR(enq_density(ctx, ub));
+    }
     CombineArgs a = combine_base(ctx, ub, fs[s], modes[s], fp);
     a.out = blko(ctx->d_us, NB, NG, NB);
     a.dt = dt;
@@ -647,6 +659,9 @@ int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out) {
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
     e = cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->st_side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
     e = configure_kernels();
     if (e == cudaSuccess) e = configure_adjoint_kernels();
@@ -710,6 +725,9 @@ int mattohf_destroy(mattohf_ctx* ctx) {
                   ctx->d_udf, ctx->d_kern_df, ctx->d_tw_df};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->st_side) cudaStreamDestroy(ctx->st_side);
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;
   return MATTOHF_OK;
