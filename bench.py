@@ -536,10 +536,27 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=4000)
     ap.add_argument("--fd-samples", type=int, default=32)
     ap.add_argument("--profile-df", action="store_true",
-                    help="with --profile-case: double-float exchange transforms")
+                    help="with --profile-case / --profile-step: double-float exchange transforms")
     ap.add_argument("--profile-case", action="store_true",
                     help="small profiling case: 3 applies of h[u]u on the workload (no timing)")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="profiling case: 3 RK4 steps of the workload without graph replay (no timing)")
     args = ap.parse_args()
+    if args.profile_step:
+        from mattohf_gb300 import build, Context, _capi
+        build.build()
+        cfg = make_cfg()
+        with Context(cfg) as ctx:
+            rng = np.random.default_rng(0)
+            shape = (cfg.NK, cfg.NB, cfg.NG)
+            ctx.set_orbitals(rng.standard_normal(shape) + 1j * rng.standard_normal(shape))
+            ctx.Gram_Schmidt()
+            if args.profile_df:
+                ctx.set_option(_capi.OPT_FOCK_DF64, 1)
+            ctx.set_option(_capi.OPT_GRAPH, 0)
+            A = np.full(3, 0.01)
+            ctx.rk4_run(A, A, 1e-4)
+        return
     if args.profile_case:
         from mattohf_gb300 import build, Context, _capi
         build.build()

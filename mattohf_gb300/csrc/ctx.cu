@@ -65,6 +65,7 @@ struct mattohf_ctx {
   double* d_dpart = nullptr;  // [kDensChunks][NG] density partials
   // state
   double2 *d_u = nullptr, *d_us = nullptr, *d_k[4] = {nullptr, nullptr, nullptr, nullptr};
+  double2* d_hpre = nullptr;  // T_A w + vloc w of an RK4 stage, made beside the exchange
   // staging for host-array entry points
   double2 *d_a = nullptr, *d_b = nullptr, *d_c = nullptr;
   size_t stage_cap = 0;
@@ -482,11 +483,17 @@ int enq_rk4(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt,
     const double2* in = (s == 0) ? ctx->d_u : ctx->d_us;
     Block ub = blk(in, NB, NG, NB);
     FockPlan fp;
-    if (ctx->hf) {
-      // the density (read only by the combine) runs beside the exchange
+    const bool side = ctx->hf != 0;
+    if (side) {
+      // The density and the kinetic + local-potential part of h w need only
+      // the stage input: they run on the side stream beside the exchange.
       CK(cudaEventRecord(ctx->ev_fork, ctx->st));
       CK(cudaStreamWaitEvent(ctx->st_side, ctx->ev_fork, 0));
       CKR(enq_density(ctx, ub, ctx->st_side));
+      CombineArgs pre = combine_base(ctx, ub, fs[s], modes[s], FockPlan());
+      pre.split = 1;
+      pre.hpre = ctx->d_hpre;
+      CK(launch_combine(NG, pre, ctx->NK * NB, ctx->st_side));
       CK(cudaEventRecord(ctx->ev_join, ctx->st_side));
       CKR(enq_fock(ctx, ub, ub, &fp));
       CK(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
@@ -497,6 +504,10 @@ int enq_rk4(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt,
     a.out = blko(ctx->d_us, NB, NG, NB);
     a.dt = dt;
     a.ex_cols = (s == 0 && ex_series != nullptr && ctx->hf) ? 1 : 0;
+    if (side) {
+      a.split = 2;
+      a.hpre = ctx->d_hpre;
+    }
     CK(launch_combine(NG, a, ctx->NK * NB, ctx->st));
     if (a.ex_cols) CK(launch_ex_finalize(ex_args(ctx, ex_series, -1, nullptr), ctx->st));
   }
@@ -678,6 +689,7 @@ int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out) {
     return bail(rc);
   for (int s = 0; s < 4; ++s)
     if ((rc = dalloc(ctx, &ctx->d_k[s], nu))) return bail(rc);
+  if ((rc = dalloc(ctx, &ctx->d_hpre, nu))) return bail(rc);
   if (cudaMemsetAsync(ctx->d_u, 0, nu * sizeof(double2), ctx->st) != cudaSuccess ||
       cudaMemsetAsync(ctx->d_int, 0, 8 * sizeof(int), ctx->st) != cudaSuccess ||
       cudaMemcpyAsync(ctx->d_Gx, ctx->Gx.data(), NG * sizeof(double), cudaMemcpyHostToDevice, ctx->st) != cudaSuccess ||
@@ -722,7 +734,7 @@ int mattohf_destroy(mattohf_ctx* ctx) {
                   ctx->d_scratch, ctx->d_colbuf, ctx->d_int, ctx->d_A, ctx->d_Aave, ctx->d_sE,
                   ctx->d_sJ, ctx->d_sN, ctx->d_work, ctx->d_hwork, ctx->d_M, ctx->d_V, ctx->d_evals,
                   ctx->d_eps, ctx->d_err, ctx->d_sym, ctx->d_symF, ctx->d_dpart,
-                  ctx->d_udf, ctx->d_kern_df, ctx->d_tw_df};
+                  ctx->d_udf, ctx->d_kern_df, ctx->d_tw_df, ctx->d_hpre};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);

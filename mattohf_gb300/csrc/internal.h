@@ -112,6 +112,40 @@ __host__ __device__ __forceinline__ int sym_tp(int i, int j, int T) {
   return i * T - (i * (i - 1)) / 2 + (j - i);
 }
 
+// The reduction of the symmetric-exchange partials sums, for output orbital
+// (tile i, slot l) at grid point q, the T + 1 terms t = 0 .. T in a fixed
+// order: the column partials of tile pairs (t, i), t < i; the row and then the
+// column partial of (i, i); the row partials of (i, t - 1), t > i + 1.
+// Each output element is split into kRedQ contiguous runs of terms summed by
+// separate threads, then added in run order: deterministic, and kRedQ times
+// more loads in flight than one thread per element.
+constexpr int kRedQ = 4;    // term runs per output element
+constexpr int kRedE = 64;   // output elements per CTA (CTA = kRedQ * kRedE threads)
+__device__ __forceinline__ size_t sym_term(int t, int i, int l, int q, int S, int T, int N) {
+  const size_t SN = (size_t)S * N;
+  size_t tp;
+  bool col;
+  if (t < i) {
+    tp = sym_tp(t, i, T);
+    col = true;
+  } else if (t == i) {
+    tp = sym_tp(i, i, T);
+    col = false;
+  } else if (t == i + 1) {
+    tp = sym_tp(i, i, T);
+    col = true;
+  } else {
+    tp = sym_tp(i, t - 1, T);
+    col = false;
+  }
+  return tp * 2 * SN + (col ? SN : 0) + (size_t)l * N + q;
+}
+__device__ __forceinline__ void sym_run_bounds(int T, int c, int* t0, int* t1) {
+  const int nt = T + 1, L = (nt + kRedQ - 1) / kRedQ;
+  *t0 = c * L;
+  *t1 = min(nt, *t0 + L);
+}
+
 enum CombineMode : int {
   CM_H = 0,     // out = T_A w + vloc w + F
   CM_RK0 = 1,   // k0 = -i h ; next = u0 + (0.5 dt) k0
@@ -146,6 +180,10 @@ struct CombineArgs {
   double occ;
   double* colbuf;           // CM_OBS: [ncols][4] = Ekin part, J part, Re<w|F>, Im<w|F>
   int* nonfinite;           // set to 1 if any output is not finite
+  // 0: whole combine.  1: only T_A w + vloc w -> hpre (runs beside the
+  // exchange).  2: hpre + exchange, then the mode's epilogue (no transforms).
+  int split;
+  double2* hpre;            // [NK][NB][NG]
 };
 
 struct ObsReduceArgs {

@@ -141,38 +141,63 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym_df_batch(const FockSymDfA
 }
 
 // Ordered double-float sum of the tile partials of every occupied output,
-// converted to FP64 once (same order as k_sym_reduce).
-__device__ __forceinline__ void sym_reduce_df_body(const float4* __restrict__ part, int S, int T, int M, int N,
-                                                   double2* __restrict__ F, int idx) {
-  if (idx >= M * N) return;
+// converted to FP64 once (same term order and runs as k_sym_reduce).
+__device__ __forceinline__ df::cdf sym_run_sum_df(const float4* __restrict__ part, int S, int T, int N, int idx,
+                                                  int c) {
   const int o = idx / N, q = idx % N;
   const int i = o / S, l = o % S;
-  const size_t SN = (size_t)S * N;
+  int t0, t1;
+  sym_run_bounds(T, c, &t0, &t1);
   df::cdf f;
   f.re = make_float2(0.f, 0.f);
   f.im = make_float2(0.f, 0.f);
-  for (int j = 0; j < i; ++j) f = df::cadd(f, df::load(part + (size_t)sym_tp(j, i, T) * 2 * SN + SN + (size_t)l * N + q));
-  {
-    const size_t b = (size_t)sym_tp(i, i, T) * 2 * SN + (size_t)l * N + q;
-    f = df::cadd(f, df::load(part + b));
-    f = df::cadd(f, df::load(part + b + SN));
+#pragma unroll 4
+  for (int t = t0; t < t1; ++t) f = df::cadd(f, df::load(part + sym_term(t, i, l, q, S, T, N)));
+  return f;
+}
+
+__device__ __forceinline__ void sym_reduce_finish_df(const df::cdf& f, bool valid, double2* __restrict__ out) {
+  __shared__ df::cdf red[kRedQ][kRedE];
+  const int e = threadIdx.x % kRedE, c = threadIdx.x / kRedE;
+  red[c][e] = f;
+  __syncthreads();
+  if (c == 0 && valid) {
+    df::cdf s = red[0][e];
+#pragma unroll
+    for (int k = 1; k < kRedQ; ++k) s = df::cadd(s, red[k][e]);
+    *out = df::to_double2(s);
   }
-  for (int j = i + 1; j < T; ++j) f = df::cadd(f, df::load(part + (size_t)sym_tp(i, j, T) * 2 * SN + (size_t)l * N + q));
-  F[idx] = df::to_double2(f);
 }
 
-__global__ void k_sym_reduce_df(const float4* __restrict__ part, int S, int T, int M, int N,
-                                double2* __restrict__ F) {
-  sym_reduce_df_body(part, S, T, M, N, F, blockIdx.x * blockDim.x + threadIdx.x);
+__global__ void __launch_bounds__(kRedQ* kRedE) k_sym_reduce_df(const float4* __restrict__ part, int S, int T,
+                                                                int M, int N, double2* __restrict__ F) {
+  const int e = threadIdx.x % kRedE, c = threadIdx.x / kRedE;
+  const int idx = blockIdx.x * kRedE + e;
+  const bool valid = idx < M * N;
+  df::cdf f;
+  f.re = make_float2(0.f, 0.f);
+  f.im = make_float2(0.f, 0.f);
+  if (valid) f = sym_run_sum_df(part, S, T, N, idx, c);
+  sym_reduce_finish_df(f, valid, F + (valid ? idx : 0));
 }
 
-__global__ void k_sym_reduce_df_batch(const FockSymDfArgs* __restrict__ args, const int* __restrict__ pre,
-                                      int nruns, int N) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= pre[nruns]) return;
-  const int r = df_find_run(pre, nruns, idx);
-  const FockSymDfArgs& a = args[r];
-  sym_reduce_df_body(a.scratch, a.S, a.T, a.nk * a.nbocc, N, a.F, idx - pre[r]);
+__global__ void __launch_bounds__(kRedQ* kRedE) k_sym_reduce_df_batch(const FockSymDfArgs* __restrict__ args,
+                                                                      const int* __restrict__ pre, int nruns,
+                                                                      int N) {
+  const int e = threadIdx.x % kRedE, c = threadIdx.x / kRedE;
+  const int idx = blockIdx.x * kRedE + e;
+  const bool valid = idx < pre[nruns];
+  df::cdf f;
+  f.re = make_float2(0.f, 0.f);
+  f.im = make_float2(0.f, 0.f);
+  double2* out = nullptr;
+  if (valid) {
+    const int r = df_find_run(pre, nruns, idx);
+    const FockSymDfArgs& a = args[r];
+    f = sym_run_sum_df(a.scratch, a.S, a.T, N, idx - pre[r], c);
+    out = a.F + (idx - pre[r]);
+  }
+  sym_reduce_finish_df(f, valid, out);
 }
 
 // df copies of every run's occupied orbitals (element prefix as for the reduction)
@@ -234,7 +259,7 @@ static cudaError_t fock_df_impl(const FockSymDfArgs& a, const double2* u, int ks
   if ((e = sym_launch_params(N, a.S, &threads, &smem)) != cudaSuccess) return e;
   k_fock_sym_df<N><<<tiles, threads, smem, s>>>(a);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  k_sym_reduce_df<<<(M * N + 255) / 256, 256, 0, s>>>(a.scratch, a.S, a.T, M, N, a.F);
+  k_sym_reduce_df<<<(M * N + kRedE - 1) / kRedE, kRedQ * kRedE, 0, s>>>(a.scratch, a.S, a.T, M, N, a.F);
   return cudaGetLastError();
 }
 
@@ -249,7 +274,8 @@ static cudaError_t fock_df_batch_impl(const FockSymArgs* d_src, const FockSymDfA
   const size_t smem = sizeof(float4) * (size_t)N * (1 + 2 * NTEAM);
   k_fock_sym_df_batch<N><<<total_tiles, kThreads, smem, s>>>(d_args, d_tile_pre, nruns);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  k_sym_reduce_df_batch<<<(total_elems + 255) / 256, 256, 0, s>>>(d_args, d_elem_pre, nruns, N);
+  k_sym_reduce_df_batch<<<(total_elems + kRedE - 1) / kRedE, kRedQ * kRedE, 0, s>>>(d_args, d_elem_pre, nruns,
+                                                                                     N);
   return cudaGetLastError();
 }
 

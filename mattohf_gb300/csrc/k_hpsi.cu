@@ -329,36 +329,58 @@ __global__ void __launch_bounds__(kThreads) k_fock_sym_batch(const FockSymArgs* 
 // Sum the tile-pair partials of every occupied output into F[o][q] (fixed
 // order over tiles: column partials of earlier tiles, the diagonal tile's row
 // and column partials, row partials of later tiles).
-__device__ __forceinline__ void sym_reduce_body(const double2* __restrict__ part, int S, int T, int M,
-                                                int N, double2* __restrict__ F, int idx) {
-  if (idx >= M * N) return;
+// Run c of the ordered partial sum of output element idx (see sym_term).
+__device__ __forceinline__ double2 sym_run_sum(const double2* __restrict__ part, int S, int T, int N, int idx,
+                                               int c) {
   const int o = idx / N, q = idx % N;
   const int i = o / S, l = o % S;
-  const size_t SN = (size_t)S * N;
+  int t0, t1;
+  sym_run_bounds(T, c, &t0, &t1);
   double2 f = make_double2(0.0, 0.0);
-  for (int j = 0; j < i; ++j) f = cadd(f, part[(size_t)sym_tp(j, i, T) * 2 * SN + SN + (size_t)l * N + q]);
-  {
-    const size_t b = (size_t)sym_tp(i, i, T) * 2 * SN + (size_t)l * N + q;
-    f = cadd(f, part[b]);
-    f = cadd(f, part[b + SN]);
-  }
-  for (int j = i + 1; j < T; ++j) f = cadd(f, part[(size_t)sym_tp(i, j, T) * 2 * SN + (size_t)l * N + q]);
-  F[idx] = f;
+#pragma unroll 4
+  for (int t = t0; t < t1; ++t) f = cadd(f, part[sym_term(t, i, l, q, S, T, N)]);
+  return f;
 }
 
-__global__ void k_sym_reduce(const double2* __restrict__ part, int S, int T, int M, int N,
-                             double2* __restrict__ F) {
-  sym_reduce_body(part, S, T, M, N, F, blockIdx.x * blockDim.x + threadIdx.x);
+// kRedQ runs per element through shared memory, added in run order.
+__device__ __forceinline__ void sym_reduce_finish(double2 f, bool valid, double2* __restrict__ out) {
+  __shared__ double2 red[kRedQ][kRedE];
+  const int e = threadIdx.x % kRedE, c = threadIdx.x / kRedE;
+  red[c][e] = f;
+  __syncthreads();
+  if (c == 0 && valid) {
+    double2 s = red[0][e];
+#pragma unroll
+    for (int k = 1; k < kRedQ; ++k) s = cadd(s, red[k][e]);
+    *out = s;
+  }
+}
+
+__global__ void __launch_bounds__(kRedQ* kRedE) k_sym_reduce(const double2* __restrict__ part, int S, int T,
+                                                             int M, int N, double2* __restrict__ F) {
+  const int e = threadIdx.x % kRedE, c = threadIdx.x / kRedE;
+  const int idx = blockIdx.x * kRedE + e;
+  const bool valid = idx < M * N;
+  const double2 f = valid ? sym_run_sum(part, S, T, N, idx, c) : make_double2(0.0, 0.0);
+  sym_reduce_finish(f, valid, F + (valid ? idx : 0));
 }
 
 // element prefix: pre[r] = sum over earlier runs of M_r * N
-__global__ void k_sym_reduce_batch(const FockSymArgs* __restrict__ args, const int* __restrict__ pre,
-                                   int nruns, int N) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= pre[nruns]) return;
-  const int r = find_run(pre, nruns, idx);
-  const FockSymArgs& a = args[r];
-  sym_reduce_body(a.scratch, a.S, a.T, a.nk * a.nbocc, N, a.F, idx - pre[r]);
+__global__ void __launch_bounds__(kRedQ* kRedE) k_sym_reduce_batch(const FockSymArgs* __restrict__ args,
+                                                                   const int* __restrict__ pre, int nruns,
+                                                                   int N) {
+  const int e = threadIdx.x % kRedE, c = threadIdx.x / kRedE;
+  const int idx = blockIdx.x * kRedE + e;
+  const bool valid = idx < pre[nruns];
+  double2 f = make_double2(0.0, 0.0);
+  double2* out = nullptr;
+  if (valid) {
+    const int r = find_run(pre, nruns, idx);
+    const FockSymArgs& a = args[r];
+    f = sym_run_sum(a.scratch, a.S, a.T, N, idx - pre[r], c);
+    out = a.F + (idx - pre[r]);
+  }
+  sym_reduce_finish(f, valid, out);
 }
 
 // Exchange term of output column (ik, ib) at grid point q, summed over the
@@ -404,7 +426,10 @@ __device__ __forceinline__ void combine_body(const CombineArgs& a, const int nco
     wv[e] = wcol[TM::pos(tl, e)];
     x[e] = wv[e];
   }
-  fft_team<N, -1>(x, bufs[team], tw_s, tl);
+  // split == 2: the kinetic and local-potential part was made by the split == 1
+  // pass (beside the exchange); only the exchange and the epilogue remain
+  const bool post = a.split == 2;
+  if (!post) fft_team<N, -1>(x, bufs[team], tw_s, tl);
   const double kAx = a.kx[ik] + A;
   const double kA2 = kAx * kAx;
   if (a.mode == CM_OBS) {
@@ -440,13 +465,27 @@ __device__ __forceinline__ void combine_body(const CombineArgs& a, const int nco
     }
     return;
   }
+  if (!post) {
 #pragma unroll
-  for (int e = 0; e < E; ++e) {
-    const double G = a.Gx[TM::pos(tl, e)];
-    const double m = 0.5 * (G * G + 2.0 * G * kAx + kA2);
-    x[e] = make_double2(m * x[e].x / (double)N, m * x[e].y / (double)N);
+    for (int e = 0; e < E; ++e) {
+      const double G = a.Gx[TM::pos(tl, e)];
+      const double m = 0.5 * (G * G + 2.0 * G * kAx + kA2);
+      x[e] = make_double2(m * x[e].x / (double)N, m * x[e].y / (double)N);
+    }
+    fft_team<N, +1>(x, bufs[team], tw_s, tl);
   }
-  fft_team<N, +1>(x, bufs[team], tw_s, tl);
+  const size_t ocol = (size_t)ik * a.w.nb * N + (size_t)ib * N;  // [NK][NB][NG]
+  if (a.split == 1) {
+    if (valid) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int q = TM::pos(tl, e);
+        const double v = a.vloc[q];
+        a.hpre[ocol + q] = make_double2(x[e].x + v * wv[e].x, x[e].y + v * wv[e].y);
+      }
+    }
+    return;
+  }
   // deferred exchange energy: <w|F> of occupied columns (stage 1 of an RK4 step)
   double exr = 0.0, exi = 0.0;
   bool bad = false;
@@ -458,6 +497,7 @@ __device__ __forceinline__ void combine_body(const CombineArgs& a, const int nco
       h = x[e];
     } else {
       if (a.mode == CM_F) h = make_double2(0.0, 0.0);
+      else if (post) h = a.hpre[ocol + q];
       else {
         const double v = a.vloc[q];
         h = make_double2(x[e].x + v * wv[e].x, x[e].y + v * wv[e].y);
@@ -649,7 +689,7 @@ static cudaError_t fock_sym_impl(const FockSymArgs& a, cudaStream_t s) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int M = a.nk * a.nbocc;
-  k_sym_reduce<<<(M * N + 255) / 256, 256, 0, s>>>(a.scratch, a.S, a.T, M, N, a.F);
+  k_sym_reduce<<<(M * N + kRedE - 1) / kRedE, kRedQ * kRedE, 0, s>>>(a.scratch, a.S, a.T, M, N, a.F);
   return cudaGetLastError();
 }
 
@@ -778,7 +818,7 @@ static cudaError_t fock_sym_batch_impl(const FockSymArgs* d_args, const int* d_t
   k_fock_sym_batch<N><<<total_tiles, kThreads, sym_smem<N>(), s>>>(d_args, d_tile_pre, nruns);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_sym_reduce_batch<<<(total_elems + 255) / 256, 256, 0, s>>>(d_args, d_elem_pre, nruns, N);
+  k_sym_reduce_batch<<<(total_elems + kRedE - 1) / kRedE, kRedQ * kRedE, 0, s>>>(d_args, d_elem_pre, nruns, N);
   return cudaGetLastError();
 }
 
@@ -826,7 +866,7 @@ cudaError_t launch_step_advance(int* it, cudaStream_t s) {
 }
 
 cudaError_t launch_sym_reduce(const double2* part, int S, int T, int M, int N, double2* F, cudaStream_t s) {
-  k_sym_reduce<<<(M * N + 255) / 256, 256, 0, s>>>(part, S, T, M, N, F);
+  k_sym_reduce<<<(M * N + kRedE - 1) / kRedE, kRedQ * kRedE, 0, s>>>(part, S, T, M, N, F);
   return cudaGetLastError();
 }
 
