@@ -1703,6 +1703,9 @@ struct mattohf_batch {
   FockSymArgs* d_fsym[kVariants] = {};
   FockSymDfArgs* d_fsym_df[kVariants] = {};
   CombineArgs* d_comb[kVariants] = {};
+  CombineArgs* d_comb_pre[4] = {};  // stages' kinetic + local-potential pass (beside the exchange)
+  cudaStream_t st_side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int opt_df = 0;  // exchange transforms in double-float arithmetic
   ObsReduceArgs* d_obs = nullptr;
   ExArgs* d_ex = nullptr;
@@ -1761,6 +1764,7 @@ int batch_prepare(mattohf_batch* b, int nt) {
   std::vector<FockSymArgs> fsym[mattohf_batch::kVariants];
   std::vector<FockSymDfArgs> fsdf[mattohf_batch::kVariants];
   std::vector<CombineArgs> comb[mattohf_batch::kVariants];
+  std::vector<CombineArgs> comb_pre[4];
   std::vector<ObsReduceArgs> obs(R);
   std::vector<ExArgs> ex(R), exf(R);
   std::vector<int> tile_pre(R + 1, 0), elem_pre(R + 1, 0), cta_pre(R + 1, 0);
@@ -1849,6 +1853,14 @@ int batch_prepare(mattohf_batch* b, int nt) {
       c.dt = b->dts[r];
       c.ex_cols = (v == 0 && ctx->hf) ? 1 : 0;
       c.nonfinite = b->d_int + 1;
+      if (v < 4) {
+        CombineArgs cp = c;
+        cp.split = 1;
+        cp.hpre = ctx->d_hpre;
+        comb_pre[v].push_back(cp);
+        c.split = 2;
+        c.hpre = ctx->d_hpre;
+      }
       comb[v].push_back(c);
     }
     ObsReduceArgs o;
@@ -1881,6 +1893,7 @@ int batch_prepare(mattohf_batch* b, int nt) {
     if ((rc = bupload(b, &b->d_dens[v], dens[v])) || (rc = bupload(b, &b->d_fsym[v], fsym[v])) ||
         (rc = bupload(b, &b->d_fsym_df[v], fsdf[v])) || (rc = bupload(b, &b->d_comb[v], comb[v])))
       return rc;
+    if (v < 4 && (rc = bupload(b, &b->d_comb_pre[v], comb_pre[v]))) return rc;
   }
   if ((rc = bupload(b, &b->d_obs, obs)) || (rc = bupload(b, &b->d_ex, ex)) || (rc = bupload(b, &b->d_exf, exf)) ||
       (rc = bupload(b, &b->d_tile_pre, tile_pre)) || (rc = bupload(b, &b->d_elem_pre, elem_pre)) ||
@@ -1895,8 +1908,17 @@ int batch_prepare(mattohf_batch* b, int nt) {
   BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaSuccess;
   for (int s = 0; s < 4 && e == cudaSuccess; ++s) {
-    e = launch_density_batch(NG, b->d_dens[s], R, b->st);
-    if (e == cudaSuccess) e = batch_exchange(b, s);
+    // density and the kinetic + local-potential pass beside the exchange
+    e = cudaEventRecord(b->ev_fork, b->st);
+    if (e != cudaSuccess) break;
+    cudaError_t es = cudaStreamWaitEvent(b->st_side, b->ev_fork, 0);
+    if (es == cudaSuccess) es = launch_density_batch(NG, b->d_dens[s], R, b->st_side);
+    if (es == cudaSuccess)
+      es = launch_combine_batch(NG, b->d_comb_pre[s], b->d_cta_pre, R, b->total_ctas, b->st_side);
+    const cudaError_t ej = cudaEventRecord(b->ev_join, b->st_side);
+    e = batch_exchange(b, s);
+    const cudaError_t ew = cudaStreamWaitEvent(b->st, b->ev_join, 0);
+    if (e == cudaSuccess) e = es != cudaSuccess ? es : (ej != cudaSuccess ? ej : ew);
     if (e == cudaSuccess) e = launch_combine_batch(NG, b->d_comb[s], b->d_cta_pre, R, b->total_ctas, b->st);
     if (e == cudaSuccess && s == 0) e = launch_ex_finalize_batch(b->d_ex, R, b->st);
   }
@@ -1941,6 +1963,9 @@ int mattohf_batch_create(int nruns, const mattohf_config* cfgs, mattohf_batch** 
   }
   if (cudaSetDevice(b->device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->st_side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaMalloc(&b->d_int, 4 * sizeof(int)) != cudaSuccess ||
       cudaMemset(b->d_int, 0, 4 * sizeof(int)) != cudaSuccess) {
     mattohf_batch_destroy(b);
@@ -1965,6 +1990,10 @@ int mattohf_batch_destroy(mattohf_batch* b) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto* c : b->runs) mattohf_destroy(c);
+  for (int v = 0; v < 4; ++v) cudaFree(b->d_comb_pre[v]);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_join) cudaEventDestroy(b->ev_join);
+  if (b->st_side) cudaStreamDestroy(b->st_side);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
   return MATTOHF_OK;
