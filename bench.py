@@ -279,6 +279,8 @@ def run_gpu(args, dist):
     achieved = flops / (fock_ms / nf * 1e-3) / 1e12
     peak = C.c_double()
     lib.mattohf_diag_fp64_peak(dev, C.byref(peak))
+    dmma = C.c_double()
+    lib.mattohf_diag_dmma_peak(dev, C.byref(dmma))
     # dram__bytes_read.sum + dram__bytes_write.sum of one k_fock_sym<256> launch on
     # this workload, from the ncu capture in profiles/k_fock_sym_ng256_nk64_nb4.md
     prof_traffic = None
@@ -344,6 +346,10 @@ def run_gpu(args, dist):
                          "traffic": prof_traffic, "kernel": "k_fock_sym",
                          "flops_per_launch": flops, "launch_ms": fock_ms / nf,
                          "peak_source": "measured DFMA throughput on this GPU (mattohf_diag_fp64_peak)",
+                         "fp64_tensor_peak": dmma.value,
+                         "fp64_tensor_peak_source": "measured DMMA (mma.sync m8n8k4 f64) throughput, "
+                                                    "mattohf_diag_dmma_peak",
+                         "hbm_peak_gbs": hbm_peak(),
                          "flops_model": "symmetric exchange: M(M+1)/2 pairs x (10 N log2 N + 16 N) + M(M-1)/2 x 8 N, M = NK*NBocc"},
             "cpu_baseline": cpu, "e2e": e2e, "double_float_exchange": double_float, "gpu_launches": launches_per_step * K, "clocks": clocks}
     if dist.rank == 0:
@@ -353,6 +359,15 @@ def run_gpu(args, dist):
 
 ENSEMBLE_DT = 1.5e-3
 ADJ_DT = 2.5e-3
+
+
+def hbm_peak():
+    """Measured copy bandwidth of this GPU pool (MEASURED_PEAKS.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh).get("hbm_gbs")
+    except (OSError, ValueError):
+        return None
 
 
 def run_ensemble(args):

@@ -218,6 +218,9 @@ int mattohf_batch_set_option(mattohf_batch* b, int option, long long value);
  * `device` in TFLOP/s (2 flops per DFMA), the roofline denominator of the
  * FP64-bound kernels. */
 int mattohf_diag_fp64_peak(int device, double* tflops);
+/* Measured FP64 tensor-core (DMMA, mma.sync m8n8k4 f64) throughput in TFLOP/s;
+ * no reference counterpart.  Used to decide against a DFT-as-GEMM exchange. */
+int mattohf_diag_dmma_peak(int device, double* tflops);
 
 /* Exchange term vFwbk = ubkwbk_vFwbk(ubk, wbk) on caller-owned DEVICE buffers
  * without allocating any device memory.  No counterpart in the reference: it

@@ -39,7 +39,7 @@ EXPORTS = [
     "mattohf_hpsi_kslice_device", "mattohf_observables_kslice_device",
     "mattohf_kinetic", "mattohf_density", "mattohf_observables", "mattohf_rk4_step",
     "mattohf_rk4_run", "mattohf_last_run_timing", "mattohf_gs_run", "mattohf_eps",
-    "mattohf_synchronize", "mattohf_diag_fp64_peak", "mattohf_fock_noalloc",
+    "mattohf_synchronize", "mattohf_diag_fp64_peak", "mattohf_diag_dmma_peak", "mattohf_fock_noalloc",
     "mattohf_batch_create", "mattohf_batch_destroy", "mattohf_batch_last_error", "mattohf_batch_run",
     "mattohf_batch_rk4_run", "mattohf_batch_last_run_ms", "mattohf_adjoint", "mattohf_adjoint_timing",
     "mattohf_fourier", "mattohf_vck", "mattohf_te_step", "mattohf_batch_set_option",
@@ -99,6 +99,7 @@ def load(path: str = LIB_PATH):
         "mattohf_gs_run": ([P, I, I, D, D, D, D, D], I),
         "mattohf_eps": ([P, D, D], I),
         "mattohf_synchronize": ([P], I),
+        "mattohf_diag_dmma_peak": ([I, D], I),
         "mattohf_diag_fp64_peak": ([I, D], I),
         "mattohf_fock_noalloc": ([I, I, I, I, I, P, P, P, P, P], I),
         "mattohf_batch_create": ([I, C.POINTER(mattohf_config), C.POINTER(P)], I),

@@ -46,6 +46,26 @@ __global__ void k_dfma_probe(double* out, int iters, double a, double b) {
   if (s == -12345.0) out[0] = s;
 }
 
+// FP64 tensor-core (DMMA, mma.sync m8n8k4 f64) throughput probe: 8
+// independent accumulator pairs per lane; 512 FLOP per warp instruction.
+__global__ void k_dmma_probe(double* out, int iters) {
+  const double a = 1.0 + threadIdx.x * 1e-9, b = 1.0 - threadIdx.x * 1e-9;
+  double c[8][2];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) c[j][0] = c[j][1] = 0.0;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                   : "+d"(c[j][0]), "+d"(c[j][1])
+                   : "d"(a), "d"(b));
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += c[j][0] + c[j][1];
+  if (s == -12345.0) out[0] = s;
+}
+
 }  // namespace
 
 struct mattohf_ctx {
@@ -1341,6 +1361,33 @@ int mattohf_diag_fp64_peak(int device, double* tflops) {
   if (e != cudaSuccess || ms <= 0) return MATTOHF_ERR_CUDA;
   const double fmas = (double)blocks * threads * iters * 16 * 8;
   *tflops = 2.0 * fmas / (ms * 1e-3) / 1e12;
+  return MATTOHF_OK;
+}
+
+int mattohf_diag_dmma_peak(int device, double* tflops) {
+  if (!tflops) return MATTOHF_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return MATTOHF_ERR_CUDA;
+  int nsm = 0;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return MATTOHF_ERR_CUDA;
+  double* d = nullptr;
+  if (cudaMalloc(&d, sizeof(double)) != cudaSuccess) return MATTOHF_ERR_ALLOC;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = nsm * 8, threads = 256, iters = 400;
+  k_dmma_probe<<<blocks, threads>>>(d, iters);
+  cudaEventRecord(e0);
+  k_dmma_probe<<<blocks, threads>>>(d, iters);
+  cudaEventRecord(e1);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  if (e != cudaSuccess || ms <= 0) return MATTOHF_ERR_CUDA;
+  const double warp_mmas = (double)blocks * (threads / 32) * iters * 8;
+  *tflops = warp_mmas * 512.0 / (ms * 1e-3) / 1e12;
   return MATTOHF_OK;
 }
 
