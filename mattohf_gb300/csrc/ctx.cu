@@ -493,12 +493,17 @@ ExArgs ex_args(mattohf_ctx* ctx, double* series, int idx, double* out) {
 // device series indexed by the device step counter.  With `ex_series` the
 // first stage also completes Etot(it-1) with the exchange energy of the
 // step's input orbitals (the same exchange operator the stage applies).
+int launch_store_stage(mattohf_ctx* ctx, const double2* src, int slot);
+
+// One RK4 step.  With `store`, the four stage inputs also go to the adjoint's
+// stage store at slot (it - seg0) * 4 + s.
 int enq_rk4(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt,
-            double* ex_series = nullptr) {
+            double* ex_series = nullptr, bool store = false) {
   const int NG = ctx->NG, NB = ctx->NB;
   const int modes[4] = {CM_RK0, CM_RK1, CM_RK2, CM_RK3};
   const AField fs[4] = {f_m, f_ave, f_ave, f_cur};
   CKR(ensure_scratch(ctx, ctx->NK * NB));
+  if (store) CKR(launch_store_stage(ctx, ctx->d_u, 0));
   for (int s = 0; s < 4; ++s) {
     const double2* in = (s == 0) ? ctx->d_u : ctx->d_us;
     Block ub = blk(in, NB, NG, NB);
@@ -530,6 +535,7 @@ int enq_rk4(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt,
     }
     CK(launch_combine(NG, a, ctx->NK * NB, ctx->st));
     if (a.ex_cols) CK(launch_ex_finalize(ex_args(ctx, ex_series, -1, nullptr), ctx->st));
+    if (store && s < 3) CKR(launch_store_stage(ctx, ctx->d_us, s + 1));
   }
   return MATTOHF_OK;
 }
@@ -1406,26 +1412,9 @@ namespace {
 
 // Recompute one forward step from d_u, storing its four stage inputs in the
 // segment store at slot (it - seg0)*4 + s.
-int enq_recompute_step(mattohf_ctx* ctx, AField fm, AField fave, AField fcur, double dt, size_t elems) {
-  const int NG = ctx->NG, NB = ctx->NB;
-  const int modes[4] = {CM_RK0, CM_RK1, CM_RK2, CM_RK3};
-  const AField fs[4] = {fm, fave, fave, fcur};
-  int* it = ctx->d_int;
-  int* seg0 = ctx->d_adj_int + 1;
-  CK(launch_stage_copy(nullptr, ctx->d_u, ctx->d_store, it, seg0, 0, elems, 1, ctx->st));
-  for (int s = 0; s < 4; ++s) {
-    const double2* in = (s == 0) ? ctx->d_u : ctx->d_us;
-    Block ub = blk(in, NB, NG, NB);
-    CKR(enq_density(ctx, ub));
-    FockPlan fp;
-    if (ctx->hf) CKR(enq_fock(ctx, ub, ub, &fp));
-    CombineArgs a = combine_base(ctx, ub, fs[s], modes[s], fp);
-    a.out = blko(ctx->d_us, NB, NG, NB);
-    a.dt = dt;
-    CK(launch_combine(NG, a, ctx->NK * NB, ctx->st));
-    if (s < 3) CK(launch_stage_copy(nullptr, ctx->d_us, ctx->d_store, it, seg0, s + 1, elems, 1, ctx->st));
-  }
-  CK(launch_counter_add(it, 1, ctx->st));
+int enq_recompute_step(mattohf_ctx* ctx, AField fm, AField fave, AField fcur, double dt) {
+  CKR(enq_rk4(ctx, fm, fave, fcur, dt, nullptr, true));
+  CK(launch_counter_add(ctx->d_int, 1, ctx->st));
   return MATTOHF_OK;
 }
 
@@ -1508,6 +1497,12 @@ int enq_adjoint_step(mattohf_ctx* ctx, double dt, size_t elems) {
   return MATTOHF_OK;
 }
 
+int launch_store_stage(mattohf_ctx* ctx, const double2* src, int slot) {
+  CK(launch_stage_copy(nullptr, src, ctx->d_store, ctx->d_int, ctx->d_adj_int + 1, slot, orb_elems(ctx, ctx->NB), 1,
+                       ctx->st));
+  return MATTOHF_OK;
+}
+
 int capture(mattohf_ctx* ctx, cudaGraphExec_t* exec, const std::function<int()>& body) {
   cudaGraph_t g;
   ctx->capturing = true;
@@ -1533,12 +1528,20 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   if (ctx->NB != ctx->NBocc) return fail(ctx, MATTOHF_ERR_ARG, "the adjoint needs all bands occupied (NB == NBocc)");
   const int NG = ctx->NG, NB = ctx->NB, NK = ctx->NK;
   const size_t elems = orb_elems(ctx, NB);
-  // checkpoint interval: default sqrt(nt), at most what fits the budget of device memory left
-  int C = ckpt_every > 0 ? ckpt_every : std::max(1, (int)std::lround(std::sqrt((double)nt)));
-  C = std::min(C, nt);
-  const int nseg = (nt + C - 1) / C;
+  // Checkpoint interval C.  C >= nt: the forward pass itself stores every
+  // stage input and the backward pass needs no recomputation.  Automatic
+  // (ckpt_every <= 0): that whenever it fits in three quarters of the free
+  // device memory, else sqrt(nt) (checkpoints plus one segment of stage inputs).
   size_t freeb = 0, totalb = 0;
   CK(cudaMemGetInfo(&freeb, &totalb));
+  int C = ckpt_every;
+  if (C <= 0) {
+    const size_t all = sizeof(double2) * elems * (4 * (size_t)nt + 12);
+    C = all <= freeb / 4 * 3 ? nt : std::max(1, (int)std::lround(std::sqrt((double)nt)));
+  }
+  C = std::min(C, nt);
+  const bool store_all = C == nt;
+  const int nseg = (nt + C - 1) / C;
   const size_t need = sizeof(double2) * elems * ((size_t)nseg + 4 * (size_t)C + 10);
   if (need > freeb) return fail(ctx, MATTOHF_ERR_ALLOC, "checkpoint storage exceeds free device memory; lower ckpt_every");
   CKR(ensure_series(ctx, nt));
@@ -1599,14 +1602,17 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
     cudaEventDestroy(e1);
     cudaEventDestroy(e2);
   };
+  // stage-store base step: the store slot of step it is (it - seg0)
+  CK(cudaMemsetAsync(ctx->d_adj_int, 0, 4 * sizeof(int), ctx->st));
   int rc = capture(ctx, &gfwd, [&]() {
+    if (store_all) return enq_recompute_step(ctx, fm, fave, fcur, dt);
     CK(launch_checkpoint(ctx->d_ckpt, ctx->d_u, ctx->d_int, C, elems, ctx->st));
     CKR(enq_rk4(ctx, fm, fave, fcur, dt, nullptr));
     CK(launch_counter_add(ctx->d_int, 1, ctx->st));
     return MATTOHF_OK;
   });
-  if (rc == MATTOHF_OK)
-    rc = capture(ctx, &grec, [&]() { return enq_recompute_step(ctx, fm, fave, fcur, dt, elems); });
+  if (rc == MATTOHF_OK && !store_all)
+    rc = capture(ctx, &grec, [&]() { return enq_recompute_step(ctx, fm, fave, fcur, dt); });
   if (rc == MATTOHF_OK) rc = capture(ctx, &gadj, [&]() { return enq_adjoint_step(ctx, dt, elems); });
   if (rc != MATTOHF_OK) {
     cleanup();
@@ -1637,11 +1643,14 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int s0 = seg * C, len = std::min(C, nt - s0);
     const int hv[2] = {s0 + len - 1, s0};
-    CK(cudaMemcpyAsync(ctx->d_u, ctx->d_ckpt + (size_t)seg * elems, sizeof(double2) * elems,
-                       cudaMemcpyDeviceToDevice, ctx->st));
-    CK(cudaMemcpyAsync(ctx->d_int, &s0, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+    if (!store_all) {
+      CK(cudaMemcpyAsync(ctx->d_u, ctx->d_ckpt + (size_t)seg * elems, sizeof(double2) * elems,
+                         cudaMemcpyDeviceToDevice, ctx->st));
+      CK(cudaMemcpyAsync(ctx->d_int, &s0, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+      CK(cudaMemcpyAsync(ctx->d_adj_int + 1, &s0, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+      for (int j = 0; j < len; ++j) CK(cudaGraphLaunch(grec, ctx->st));
+    }
     CK(cudaMemcpyAsync(ctx->d_adj_int, hv, 2 * sizeof(int), cudaMemcpyHostToDevice, ctx->st));
-    for (int j = 0; j < len; ++j) CK(cudaGraphLaunch(grec, ctx->st));
     for (int j = 0; j < len; ++j) CK(cudaGraphLaunch(gadj, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));  // host values above are stack-resident
   }
