@@ -1429,10 +1429,18 @@ int enq_adjoint_step(mattohf_ctx* ctx, double dt, size_t elems) {
   const int M = NK * ctx->NBocc;
   const int S = sym_tile(ctx);
   const int T = (M + S - 1) / S;
+  const bool side = ctx->hf != 0;
+  cudaStream_t ss = side ? ctx->st_side : ctx->st;
   for (int s = 3; s >= 0; --s) {
     CK(launch_stage_copy(ctx->d_vbuf, nullptr, ctx->d_store, n, seg0, s, elems, 0, ctx->st));
     Block vb = blk(ctx->d_vbuf, NB, NG, NB);
-    CKR(enq_density(ctx, vb));  // vloc = vH[rho(v)] + vion
+    // the densities and the exchange-free part of the combine run on the side
+    // stream, beside the adjoint exchange
+    if (side) {
+      CK(cudaEventRecord(ctx->ev_fork, ctx->st));
+      CK(cudaStreamWaitEvent(ctx->st_side, ctx->ev_fork, 0));
+    }
+    CKR(enq_density(ctx, vb, ss));  // vloc = vH[rho(v)] + vion
     // sigma = sum Im(conj(mu) v) -> psi = vH[sigma]; accumulate the vion gradient
     DensArgs d;
     d.u = vb;
@@ -1449,24 +1457,7 @@ int enq_adjoint_step(mattohf_ctx* ctx, double dt, size_t elems) {
     d.part = ctx->d_dpart2;
     d.mu = ctx->d_lamk[s];
     d.gvion = ctx->d_gvion;
-    CK(launch_density(NG, d, ctx->st));
-    if (ctx->hf) {
-      AdjFockArgs f;
-      f.v = ctx->d_vbuf;
-      f.mu = ctx->d_lamk[s];
-      f.kstride = NB * NG;
-      f.nk = NK;
-      f.nbocc = ctx->NBocc;
-      f.S = S;
-      f.T = T;
-      f.kern = ctx->d_kern;
-      f.tw = ctx->tw;
-      f.scratch = ctx->d_sym;
-      CKR(timed_begin(ctx));
-      CK(launch_fock_adj(NG, f, ctx->st));
-      CK(launch_sym_reduce(ctx->d_sym, S, T, M, NG, ctx->d_Fa, ctx->st));
-      CKR(timed_end(ctx));
-    }
+    CK(launch_density(NG, d, ss));
     AdjCombineArgs c;
     c.mu = ctx->d_lamk[s];
     c.v = ctx->d_vbuf;
@@ -1490,6 +1481,33 @@ int enq_adjoint_step(mattohf_ctx* ctx, double dt, size_t elems) {
     c.gstage = ctx->d_gstage;
     c.n = n;
     c.slot = s;
+    c.split = 0;
+    c.lpre = ctx->d_hpre;
+    if (side) {
+      AdjCombineArgs pre = c;
+      pre.split = 1;
+      CK(launch_adj_combine(NG, pre, NK * NB, ctx->st_side));
+      CK(cudaEventRecord(ctx->ev_join, ctx->st_side));
+      c.split = 2;
+    }
+    if (ctx->hf) {
+      AdjFockArgs f;
+      f.v = ctx->d_vbuf;
+      f.mu = ctx->d_lamk[s];
+      f.kstride = NB * NG;
+      f.nk = NK;
+      f.nbocc = ctx->NBocc;
+      f.S = S;
+      f.T = T;
+      f.kern = ctx->d_kern;
+      f.tw = ctx->tw;
+      f.scratch = ctx->d_sym;
+      CKR(timed_begin(ctx));
+      CK(launch_fock_adj(NG, f, ctx->st));
+      CK(launch_sym_reduce(ctx->d_sym, S, T, M, NG, ctx->d_Fa, ctx->st));
+      CKR(timed_end(ctx));
+    }
+    if (side) CK(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
     CK(launch_adj_combine(NG, c, NK * NB, ctx->st));
   }
   CK(cudaMemcpyAsync(ctx->d_lam, ctx->d_lamu, sizeof(double2) * elems, cudaMemcpyDeviceToDevice, ctx->st));

@@ -265,6 +265,11 @@ struct AdjCombineArgs {
   double* gstage;       // [nt][4] stage-field gradients
   const int* n;         // current step
   int slot;             // stage index 0..3
+  // 0: whole pass.  1: the part without the exchange, i (T_a + vloc) mu -> lpre,
+  // and the field-gradient partials (runs beside the exchange).  2: lpre + Fa
+  // + Hartree response, then the stage bookkeeping (no transforms).
+  int split;
+  double2* lpre;        // [NK][NB][NG]
 };
 cudaError_t launch_fock_adj(int NG, const AdjFockArgs& a, cudaStream_t s);
 cudaError_t configure_adjoint_kernels();

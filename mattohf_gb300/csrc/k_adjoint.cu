@@ -169,6 +169,23 @@ __global__ void __launch_bounds__(kThreads) k_adj_combine(AdjCombineArgs a, int 
   const int c = valid ? col : col0;
   const int ik = c / a.nb;
   const size_t o = (size_t)c * N;
+  if (a.split == 2) {
+    if (!valid) return;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int q = TM::pos(tl, e);
+      double2 lu = cadd(a.lpre[o + q], a.Fa[o + q]);
+      const double ps = 2.0 * a.occ * a.psi[q];
+      const double2 vv = a.v[o + q];
+      lu = make_double2(fma(ps, vv.x, lu.x), fma(ps, vv.y, lu.y));
+      a.lam_u[o + q] = cadd(a.lam_u[o + q], lu);
+      if (a.lam_prev) {
+        const double2 p = a.lam_prev[o + q];
+        a.lam_prev[o + q] = make_double2(fma(a.cprev, lu.x, p.x), fma(a.cprev, lu.y, p.y));
+      }
+    }
+    return;
+  }
   double2 mu[E], v[E], x[E];
 #pragma unroll
   for (int e = 0; e < E; ++e) {
@@ -201,6 +218,10 @@ __global__ void __launch_bounds__(kThreads) k_adj_combine(AdjCombineArgs a, int 
     const int q = TM::pos(tl, e);
     const double vl = a.vloc[q];
     double2 lu = mul_i(make_double2(x[e].x + vl * mu[e].x, x[e].y + vl * mu[e].y));
+    if (a.split == 1) {
+      a.lpre[o + q] = lu;
+      continue;
+    }
     lu = cadd(lu, a.Fa[o + q]);
     const double ps = 2.0 * a.occ * a.psi[q];
     lu = make_double2(fma(ps, v[e].x, lu.x), fma(ps, v[e].y, lu.y));
@@ -352,7 +373,7 @@ static cudaError_t adj_combine_impl(const AdjCombineArgs& a, int ncols, cudaStre
   constexpr int PER_CTA = (kThreads / 32) * Team<N>::PER_WARP;
   k_adj_combine<N><<<(ncols + PER_CTA - 1) / PER_CTA, kThreads, 0, s>>>(a, ncols);
   cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  if (e != cudaSuccess || a.split == 2) return e;  // the field-gradient partials come from the other passes
   k_adj_gsum<<<1, 32, 0, s>>>(a.gcol, ncols, a.gstage, a.n, a.slot);
   return cudaGetLastError();
 }
