@@ -590,7 +590,45 @@ def main():
                     help="small profiling case: 3 applies of h[u]u on the workload (no timing)")
     ap.add_argument("--profile-step", action="store_true",
                     help="profiling case: 3 RK4 steps of the workload without graph replay (no timing)")
+    ap.add_argument("--profile-gs", action="store_true",
+                    help="profiling case: one ground-state SCF iteration of the workload (no timing)")
+    ap.add_argument("--profile-adjoint", action="store_true",
+                    help="profiling case: a 4-step adjoint on the differentiation shape (no timing)")
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="profiling case: 2 batched steps of the first 32 runs of the ensemble mix (no timing)")
     args = ap.parse_args()
+    if args.profile_batch:
+        from mattohf_gb300 import build, Batch, RunConfig
+        build.build()
+        rng = np.random.default_rng(1)
+        nks = rng.choice([8, 16, 32, 64], size=256)[:32]
+        noc = rng.integers(1, 5, size=256)[:32]
+        cfgs = [RunConfig(acell=10.0, NG=128, NK=int(k), NB=int(o), NBocc=int(o), Zeff=[2.0], alpha=[1.0],
+                          Rion=[0.5], Kion=[1]) for k, o in zip(nks, noc)]
+        with Batch(cfgs) as b:
+            for r in range(len(cfgs)):
+                b[r].Init_wf()
+                b[r].Gram_Schmidt()
+            A = np.full((len(cfgs), 2), 0.01)
+            b.rk4_run(A, A, ENSEMBLE_DT)
+        return
+    if args.profile_gs:
+        from mattohf_gb300 import build, Context
+        build.build()
+        with Context(make_cfg()) as ctx:
+            ctx.Init_wf()
+            ctx.Gram_Schmidt()
+            ctx.GS_calculation(1, NCG_INIT)
+        return
+    if args.profile_adjoint:
+        from mattohf_gb300 import build, Context, RunConfig
+        build.build()
+        cfg = RunConfig(acell=10.0, NG=128, NK=16, NB=2, NBocc=2, Zeff=[2.0], alpha=[1.0], Rion=[0.5], Kion=[1])
+        with Context(cfg) as ctx:
+            ctx.Init_wf()
+            ctx.Gram_Schmidt()
+            ctx.adjoint(0.01 * np.sin(0.3 * np.arange(1, 5)), ADJ_DT, "energy", ckpt_every=2)
+        return
     if args.profile_step:
         from mattohf_gb300 import build, Context, _capi
         build.build()
