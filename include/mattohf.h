@@ -189,8 +189,10 @@ int mattohf_fourier(int device, int nt, const double* time, const double* J, dou
  * with its gradient dLdA[nt] with respect to every field sample and
  * dLdvion[NG] with respect to the ion potential on the grid (either output
  * may be NULL).  Backward RK4 adjoint with checkpoints every ckpt_every
- * steps (0: about sqrt(nt)) and recomputation between checkpoints.  Requires
- * NB == NBocc.  Leaves the orbitals at u_nt. */
+ * steps and recomputation between checkpoints; ckpt_every >= nt stores every
+ * stage input in the forward pass (no recomputation); 0 picks that whenever it
+ * fits in three quarters of the free device memory, else about sqrt(nt).
+ * Requires NB == NBocc.  Leaves the orbitals at u_nt. */
 int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double dt, const double* A, int ckpt_every,
                     double* L, double* dLdA, double* dLdvion);
 /* Device times of the last mattohf_adjoint: the forward pass alone and the whole gradient. */

@@ -17,6 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libmattohf.so")
+DRIVER = os.path.join(OUT_DIR, "mattohf")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["ctx.cu", "k_hpsi.cu", "k_gs.cu", "k_table.cu", "noalloc.cu", "k_adjoint.cu", "k_spectra.cu", "k_fock_df.cu"]
 
@@ -65,12 +66,29 @@ def build(force: bool = False, verbose_ptxas: bool = False, jobs: int = 0) -> st
                 errors.append(" ".join(cmd) + "\n" + res.stdout + res.stderr)
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
+    relinked = False
     if force or jobs_list or not os.path.exists(LIB):
         cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-Xcompiler", "-fPIC"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError("link failed:\n" + res.stdout + res.stderr)
+        relinked = True
+    build_driver(force or relinked)
     return LIB
+
+
+def build_driver(force: bool = False) -> str:
+    """The C++ drop-in driver ``_lib/mattohf`` (reads input.dat, writes the reference's outputs)."""
+    src = os.path.join(CSRC, "mattohf_main.cpp")
+    hdr = os.path.join(HERE, "..", "include", "mattohf.h")
+    if force or not _newer(DRIVER, [src, hdr, LIB]):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(HERE, "..", "include"), src, "-o", DRIVER,
+               "-L" + OUT_DIR, "-lmattohf", "-Wl,-rpath,$ORIGIN"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("driver build failed:\n" + res.stdout + res.stderr)
+    return DRIVER
 
 
 if __name__ == "__main__":

@@ -125,3 +125,63 @@ def test_fourier_matches_oracle(built_lib):
     w2, JF2, _, _ = O.window_fourier_tr(oc, t, J, 0.3, E, A)
     fw = fourier(cfg, t, J, 0.3, E, A, window=True)
     assert np.max(np.abs(fw[:, 1] + 1j * fw[:, 2] - JF2)) <= 1e-12 * np.max(np.abs(JF2))
+
+
+# ---------------------------------------------------------------------------
+# C++ drop-in driver (mattohf_gb300/_lib/mattohf, built by build())
+# ---------------------------------------------------------------------------
+def _cpp_driver():
+    from mattohf_gb300 import build
+    build.build()
+    return build.DRIVER
+
+
+def _run_cpp(name_line: str, out_dir, cwd):
+    import subprocess
+    return subprocess.run([_cpp_driver(), str(out_dir)], input=name_line + "\n", capture_output=True, text=True,
+                          cwd=str(cwd), timeout=600)
+
+
+def test_cpp_driver_rejects_missing_input(tmp_path):
+    r = _run_cpp("'no_such_input.dat'", tmp_path, tmp_path)
+    assert r.returncode == 1
+    assert "cannot open input file 'no_such_input.dat'" in r.stderr
+
+
+def test_cpp_driver_rejects_bad_integer(tmp_path):
+    (tmp_path / "bad.dat").write_text("NG\n  1.5x\n")
+    r = _run_cpp('"bad.dat"', tmp_path, tmp_path)
+    assert r.returncode == 1
+    assert "bad integer value '1.5x'" in r.stderr
+
+
+def _numbers(path):
+    """Every number in a file, in order (headers are identical in both drivers' files)."""
+    import re
+    num = re.compile(r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[eE][-+]?\d+)?")
+    return np.array([float(t) for line in open(path) for t in num.findall(line)])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("field", ["LP", "LR"])
+def test_cpp_driver_matches_python_driver(tmp_path, built_lib, field):
+    """Every output file of the C++ driver against the Python driver on the same input."""
+    from mattohf_gb300 import read_input
+    from mattohf_gb300.driver import run
+    text = INPUT.replace("'LP'", f"'{field}'")
+    (tmp_path / "input.dat").write_text(text)
+    py_dir, cpp_dir = tmp_path / "py", tmp_path / "cpp"
+    py_dir.mkdir()
+    cpp_dir.mkdir()
+    run(read_input(str(tmp_path / "input.dat")), out_dir=str(py_dir), log=lambda *a: None)
+    r = _run_cpp("'input.dat'", cpp_dir, tmp_path)
+    assert r.returncode == 0, r.stderr
+    files = sorted(os.listdir(py_dir))
+    assert files == sorted(os.listdir(cpp_dir))
+    assert ("tiny_sigmaeps.out" in files) == (field == "LR")
+    for f in files:
+        a, b = _numbers(py_dir / f), _numbers(cpp_dir / f)
+        assert a.shape == b.shape, f
+        # same kernels in the same order; host-side sums (SCF density change,
+        # DoS broadening) may round differently from numpy's pairwise sums
+        assert np.allclose(a, b, rtol=1e-11, atol=1e-300), f
