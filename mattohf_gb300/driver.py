@@ -122,21 +122,21 @@ def run(cfg: RunConfig, out_dir: str = ".", rt_chunk: int = 1000, log=print) -> 
     NG, NK, NB, NBocc = cfg.NG, cfg.NK, cfg.NB, cfg.NBocc
     with open(p("potential.out"), "w") as fh:
         for x, v in zip(g["rx"], ctx.vion):
-            fh.write(f" {x!r:>24} {v!r:>24}\n")
+            fh.write(f" {float(x)!r:>24} {float(v)!r:>24}\n")
     vCG, vCq = ctx.coulomb()
     with open(p("vk.out"), "w") as fh:
         kk = np.add.outer(g["Gx"], g["kx"])          # k_vCk(Gx(ig)+kx(ik)), I:149-155
         vk = ctx.vck(kk.ravel()).reshape(kk.shape)
         for ig in range(NG):
             for ik in range(NK):
-                fh.write(f" {kk[ig, ik]!r:>24} {vk[ig, ik]!r:>24}\n")
+                fh.write(f" {float(kk[ig, ik])!r:>24} {float(vk[ig, ik])!r:>24}\n")
     ctx.Init_wf()
     ctx.Gram_Schmidt()
     occ = np.zeros((NK, NB))
     occ[:, :NBocc] = 2.0 / NK
     e0 = ctx.observables(0.0)
-    log(f" Number of particle per cell {e0['Nele']!r}")
-    log(f" Total energy at initial = {e0['Etot']!r}")
+    log(f" Number of particle per cell {float(e0['Nele'])!r}")
+    log(f" Total energy at initial = {float(e0['Etot'])!r}")
     # ---- ground state (GS:26-121)
     t_gs = time.perf_counter()
     dprev = ctx.ubk_dns(ctx.get_orbitals())
@@ -221,7 +221,7 @@ def run(cfg: RunConfig, out_dir: str = ".", rt_chunk: int = 1000, log=print) -> 
     log(f"Time for GS calculatoin ={t_gs:12.4E} [sec]")
     log(f"Time for RT calculatoin ={t_rt:12.4E} [sec]")
     log(f"Time for an interaction in RT ={t_rt / max(NT, 1):12.4E} [sec]")
-    log(f"Fluence of the field: {np.sum(E ** 2) * cfg.dt * ATOMFLUENCE!r} J/cm^2")
+    log(f"Fluence of the field: {float(np.sum(E ** 2) * cfg.dt * ATOMFLUENCE)!r} J/cm^2")
     ctx.close()
     return {"Etot": Et, "Je": Je, "Nele": Ne, "A": A, "E": E, "time": time_, "t_rt": t_rt,
             "t_total": time.perf_counter() - t_all}
