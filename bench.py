@@ -339,10 +339,15 @@ def run_gpu(args, dist):
         Ac, Aavec = fields(cfg, steps_cpu)
         t = port.run(u0, steps_cpu, Ac, Aavec)
         thr = port.threads
+        # the same port on one core (one step)
+        port.lib.cref_set_threads(1)
+        t1 = port.run(u0, 1, Ac, Aavec)
+        port.lib.cref_set_threads(thr)
         port.close()
         cpu = {"value": steps_cpu / t, "unit": "steps/s", "cores": thr, "kind": "port",
                "sample": f"{steps_cpu} RK4+observable steps of the same workload (C restatement, "
-                         f"OpenMP over output columns)"}
+                         f"OpenMP over output columns)",
+               "one_core": {"value": 1.0 / t1, "unit": "steps/s", "cores": 1, "sample": "1 step"}}
     # per step: 4 stages x (k_dens_partial, k_density, kinetic k_combine pass, k_fock_sym,
     # k_sym_reduce, exchange k_combine pass) + k_ex_finalize + observables (k_dens_partial,
     # k_density, k_combine, k_obs_reduce); per run: the closing exchange apply (7 launches)

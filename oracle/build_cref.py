@@ -39,4 +39,6 @@ def load():
     lib.cref_rk4_run.argtypes = [P, D, C.c_int, C.c_double, D, D, D, D, D]
     lib.cref_get_tables.argtypes = [P, D, D]
     lib.cref_threads.restype = C.c_int
+    lib.cref_set_threads.argtypes = [C.c_int]
+    lib.cref_set_threads.restype = C.c_int
     return lib

@@ -158,6 +158,16 @@ int cref_threads(void) {
 #endif
 }
 
+/* Threads for the following calls (n >= 1); returns the count now in effect. */
+int cref_set_threads(int n) {
+#ifdef _OPENMP
+  if (n >= 1) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+  return cref_threads();
+}
+
 /* ------------------------------------------------------------ kernels ---- */
 static void density(const cref* c, const double* u, double* rho) {
   const int NG = c->NG, NB = c->NB;
