@@ -45,6 +45,8 @@ extern "C" {
 #define MATTOHF_OPT_FOCK_DF64 6   /* 1: symmetric exchange transforms in double-float (2 x FP32, 48-bit
                                       significand) arithmetic on the FP32 pipe; default 0 (FP64) */
 #define MATTOHF_OPT_SYM_TILE 7     /* symmetric-exchange tile size (orbitals per CTA side); 0 = automatic */
+#define MATTOHF_OPT_SMALL_STAGES 8 /* mattohf_rk4_run with one fused launch per RK4 stage (one CTA per
+                                      column; for small problems): 0 off, 1 on, 2 automatic (default) */
 #define MATTOHF_OPT_L2_FLUSH 5     /* >0: bytes written between RK4 steps of mattohf_rk4_run, which then
                                       reports the summed per-step device time (benchmarking) */
 

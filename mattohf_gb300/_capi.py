@@ -29,6 +29,7 @@ OPT_SYMMETRIC = 4
 OPT_L2_FLUSH = 5
 OPT_FOCK_DF64 = 6
 OPT_SYM_TILE = 7
+OPT_SMALL_STAGES = 8
 
 # every symbol include/mattohf.h declares
 EXPORTS = [

@@ -102,6 +102,9 @@ struct mattohf_ctx {
   float4* d_tw_df = nullptr;
   int opt_df = 0;             // exchange transforms in double-float arithmetic
   int opt_tile = 0;           // symmetric-exchange tile size (0 = automatic)
+  int opt_small = 2;          // fused small-problem RK4 stages: 0 off, 1 on, 2 automatic
+  bool step_small = false;    // the captured step graph uses the fused stages
+  unsigned* d_ticket = nullptr;  // CTA completion counter of the fused stages
   int* d_int = nullptr;  // [0] = step counter, [1] = non-finite flag, [2] = solver flag
   // RT series
   double *d_A = nullptr, *d_Aave = nullptr, *d_sE = nullptr, *d_sJ = nullptr, *d_sN = nullptr;
@@ -540,6 +543,75 @@ int enq_rk4(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt,
   return MATTOHF_OK;
 }
 
+// Fused small-problem stages: is this context's RK loop better served by
+// one launch per stage (one CTA per column) than by the tiled exchange?
+bool use_small(const mattohf_ctx* ctx) {
+  if (ctx->opt_small == 0 || ctx->opt_df || ctx->opt_timing || !small_stage_supported(ctx->NG)) return false;
+  if (ctx->opt_small == 1) return true;
+  const size_t M = (size_t)ctx->NK * ctx->NBocc;
+  return ctx->NK * ctx->NB <= 256 && M * M * ctx->NG <= ((size_t)1 << 20);
+}
+
+SmallStageArgs small_base(mattohf_ctx* ctx, double dt) {
+  SmallStageArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.u0 = ctx->d_u;
+  for (int s = 0; s < 3; ++s) a.kbuf[s] = ctx->d_k[s];
+  a.dt = dt;
+  a.nk = ctx->NK;
+  a.nb = ctx->NB;
+  a.nbocc = ctx->NBocc;
+  a.hf = ctx->hf;
+  a.occ = ctx->occ;
+  a.dvcell = ctx->dvcell;
+  a.vcell = ctx->vcell;
+  a.kern = ctx->d_kern;
+  a.vCG = ctx->d_vCG;
+  a.vion = ctx->d_vion;
+  a.Gx = ctx->d_Gx;
+  a.kx = ctx->d_kx;
+  a.tw = ctx->tw;
+  a.colbuf = ctx->d_colbuf;
+  a.scal = ctx->d_scal;
+  a.series_E = ctx->d_sE;
+  a.series_J = ctx->d_sJ;
+  a.series_N = ctx->d_sN;
+  a.it = ctx->d_int;
+  a.nonfinite = ctx->d_int + 1;
+  a.ticket = ctx->d_ticket;
+  return a;
+}
+
+// One RK4 step as four fused stage launches.  Stage inputs and outputs
+// alternate between d_us and d_hpre so that no launch writes its own input.
+// Stage 0 also writes the observables of the previous step (its input).
+int enq_small_step(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt) {
+  SmallStageArgs a = small_base(ctx, dt);
+  const double2* in[4] = {ctx->d_u, ctx->d_us, ctx->d_hpre, ctx->d_us};
+  double2* out[4] = {ctx->d_us, ctx->d_hpre, ctx->d_us, nullptr};
+  const AField fs[4] = {f_m, f_ave, f_ave, f_cur};
+  for (int s = 0; s < 4; ++s) {
+    a.u = in[s];
+    a.out = out[s];
+    a.mode = s;
+    a.af = fs[s];
+    CK(launch_small_stage(ctx->NG, a, ctx->st));
+  }
+  return MATTOHF_OK;
+}
+
+// Observables of the last step's orbitals (the stage-0 launch that would
+// supply them does not happen).
+int enq_small_close(mattohf_ctx* ctx) {
+  SmallStageArgs a = small_base(ctx, 0.0);
+  a.u = ctx->d_u;
+  a.mode = 4;
+  a.af = aval(0.0);
+  a.out_obs = ctx->d_out;
+  CK(launch_small_stage(ctx->NG, a, ctx->st));
+  return MATTOHF_OK;
+}
+
 int check_ctx(mattohf_ctx* ctx) {
   if (!ctx) return MATTOHF_ERR_ARG;
   cudaError_t e = cudaSetDevice(ctx->device);
@@ -703,6 +775,7 @@ int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out) {
     e = configure_kernels();
     if (e == cudaSuccess) e = configure_adjoint_kernels();
     if (e == cudaSuccess) e = configure_df_kernels();
+    if (e == cudaSuccess) e = configure_small_kernels();
     if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
   }
   const size_t nu = orb_elems(ctx, ctx->NB);
@@ -716,6 +789,9 @@ int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out) {
   for (int s = 0; s < 4; ++s)
     if ((rc = dalloc(ctx, &ctx->d_k[s], nu))) return bail(rc);
   if ((rc = dalloc(ctx, &ctx->d_hpre, nu))) return bail(rc);
+  if (cudaMalloc(&ctx->d_ticket, sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(ctx->d_ticket, 0, sizeof(unsigned)) != cudaSuccess)
+    return bail(MATTOHF_ERR_ALLOC);
   if (cudaMemsetAsync(ctx->d_u, 0, nu * sizeof(double2), ctx->st) != cudaSuccess ||
       cudaMemsetAsync(ctx->d_int, 0, 8 * sizeof(int), ctx->st) != cudaSuccess ||
       cudaMemcpyAsync(ctx->d_Gx, ctx->Gx.data(), NG * sizeof(double), cudaMemcpyHostToDevice, ctx->st) != cudaSuccess ||
@@ -760,7 +836,7 @@ int mattohf_destroy(mattohf_ctx* ctx) {
                   ctx->d_scratch, ctx->d_colbuf, ctx->d_int, ctx->d_A, ctx->d_Aave, ctx->d_sE,
                   ctx->d_sJ, ctx->d_sN, ctx->d_work, ctx->d_hwork, ctx->d_M, ctx->d_V, ctx->d_evals,
                   ctx->d_eps, ctx->d_err, ctx->d_sym, ctx->d_symF, ctx->d_dpart,
-                  ctx->d_udf, ctx->d_kern_df, ctx->d_tw_df, ctx->d_hpre};
+                  ctx->d_udf, ctx->d_kern_df, ctx->d_tw_df, ctx->d_hpre, ctx->d_ticket};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
@@ -786,6 +862,12 @@ int mattohf_set_option(mattohf_ctx* ctx, int option, long long value) {
       if (value < 0 || value > fock_sym_teams(ctx->NG) || (value & (value - 1)))
         return fail(ctx, MATTOHF_ERR_ARG, "tile size must be 0 or a power of two up to the CTA's teams");
       ctx->opt_tile = (int)value;
+      break;
+    case MATTOHF_OPT_SMALL_STAGES:
+      if (value < 0 || value > 2) return fail(ctx, MATTOHF_ERR_ARG, "small-stage option must be 0, 1 or 2");
+      if (value == 1 && !small_stage_supported(ctx->NG))
+        return fail(ctx, MATTOHF_ERR_ARG, "fused small stages need NG <= 256");
+      ctx->opt_small = (int)value;
       break;
     case MATTOHF_OPT_L2_FLUSH:
       if (value < 0 || value > (4LL << 30)) return fail(ctx, MATTOHF_ERR_ARG, "flush bytes out of range");
@@ -1091,13 +1173,20 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
   fave.mode = AAVE;
   fcur.mode = ACUR;
   const bool use_graph = ctx->opt_graph && !ctx->opt_timing;
-  if (use_graph && (!ctx->step_exec || ctx->step_dt != dt)) {
+  const bool small = use_small(ctx);
+  CK(cudaMemsetAsync(ctx->d_ticket, 0, sizeof(unsigned), ctx->st));
+  if (use_graph && (!ctx->step_exec || ctx->step_dt != dt || ctx->step_small != small)) {
     destroy_graph(ctx);
     cudaGraph_t g;
     ctx->capturing = true;
     CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
-    int rc = enq_rk4(ctx, fm, fave, fcur, dt, ctx->d_sE);
-    if (rc == MATTOHF_OK) rc = enq_observables(ctx, ctx->d_u, fcur, true, true);
+    int rc = MATTOHF_OK;
+    if (small) {
+      rc = enq_small_step(ctx, fm, fave, fcur, dt);
+    } else {
+      rc = enq_rk4(ctx, fm, fave, fcur, dt, ctx->d_sE);
+      if (rc == MATTOHF_OK) rc = enq_observables(ctx, ctx->d_u, fcur, true, true);
+    }
     cudaError_t ec = cudaStreamEndCapture(ctx->st, &g);
     ctx->capturing = false;
     if (rc != MATTOHF_OK) return rc;
@@ -1106,6 +1195,7 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
     cudaGraphDestroy(g);
     CK(ei);
     ctx->step_dt = dt;
+    ctx->step_small = small;
   }
   ctx->fock_event_used = 0;
   // Optional per-step timing with an L2 flush between steps: each step (and
@@ -1138,6 +1228,8 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
     }
     if (use_graph) {
       CK(cudaGraphLaunch(ctx->step_exec, ctx->st));
+    } else if (small) {
+      CKR(enq_small_step(ctx, fm, fave, fcur, dt));
     } else {
       CKR(enq_rk4(ctx, fm, fave, fcur, dt, ctx->d_sE));
       CKR(enq_observables(ctx, ctx->d_u, fcur, true, true));
@@ -1161,7 +1253,9 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
       CK(cudaMemsetAsync(ctx->d_flush, 0x5a, (size_t)ctx->opt_flush, ctx->st));
       CK(cudaEventRecord(ctx->step_events[2 * nt], ctx->st));
     }
-    if (ctx->hf) {
+    if (small) {
+      CKR(enq_small_close(ctx));
+    } else if (ctx->hf) {
       FockPlan fp;
       CKR(enq_observables(ctx, ctx->d_u, aval(0.0), false, false, &fp));
       (void)fp;

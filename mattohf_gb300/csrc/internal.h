@@ -186,6 +186,39 @@ struct CombineArgs {
   double2* hpre;            // [NK][NB][NG]
 };
 
+// Fused RK4 stage for small problems (k_small.cu): one CTA per output column
+// does the density, Hartree potential, exchange, kinetic term and the stage's
+// RK4 update of its column, so a step is 4 launches instead of about 29.
+struct SmallStageArgs {
+  const double2* u;         // stage input [NK][NB][NG]
+  double2* u0;              // base state (updated in place by stage 3)
+  double2* out;             // stage output (stages 0..2), never the input
+  double2* kbuf[3];         // RK4 stage derivatives
+  int mode;                 // 0..3: RK4 stage; 4: observables of u0 only (closing pass)
+  double dt;
+  AField af;
+  int nk, nb, nbocc, hf;
+  double occ, dvcell, vcell;
+  const double* kern;       // (2NK-1) x NG exchange kernel table
+  const double* vCG;
+  const double* vion;
+  const double* Gx;
+  const double* kx;
+  const double2* tw;
+  double* colbuf;           // [ncols][4]: Ekin part, J part, Re<u|F>, Im<u|F>
+  double* scal;             // [3]: Nele, Eion, EH of the input density
+  double* series_E;         // per-step observables, indexed by the step counter
+  double* series_J;
+  double* series_N;
+  int* it;                  // step counter
+  int* nonfinite;
+  unsigned* ticket;         // CTA completion counter (last CTA finalizes; reset by it)
+  double* out_obs;          // mode 4: [7] Etot, Ekin, Eion, EH, Ex, Je, Nele
+};
+cudaError_t launch_small_stage(int NG, const SmallStageArgs& a, cudaStream_t s);
+bool small_stage_supported(int NG);
+cudaError_t configure_small_kernels();
+
 struct ObsReduceArgs {
   const double* colbuf;     // [nk*nb][4]
   const double* scal;       // dens scalars: Nele, Eion, EH

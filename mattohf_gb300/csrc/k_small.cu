@@ -1,0 +1,355 @@
+// Fused RK4 stage for small problems.
+//
+// For small grids and few orbitals every kernel of the general path is
+// latency-bound, and a step of about 29 dependent launches costs more than the
+// arithmetic.  Here one launch does a whole RK4 stage (src/RT_calculation.f90:
+// 154-173), with one CTA per output column (k, b):
+//   * the density of the stage input (F:55-71, reference order ig -> ik -> ib),
+//     recomputed by every CTA, and the Hartree potential (F:147-162);
+//   * the exchange of the column against every occupied orbital (F:237-261,
+//     all ordered pairs, no symmetry: teams of the CTA share the pairs and are
+//     reduced in a fixed order);
+//   * the kinetic term (F:212-234), h w, and the stage's RK4 update of the
+//     column, into a buffer that is never the stage input (no read/write race
+//     between CTAs).
+// Observables (F:74-119, F:165-183, F:289-318) are folded in: stage 3 stores
+// Ekin and Je of each updated column; the next stage 0 (or the closing pass,
+// mode 4) recomputes the density and <u|F u>, and its last CTA to finish
+// writes Etot, Je, Nele of the previous step.  "Last CTA" is decided by an
+// atomic ticket after a fence; nothing waits on another CTA.
+#include "fft.cuh"
+#include "internal.h"
+
+namespace mattohf {
+
+constexpr int kSmallThreads = 256;
+
+__device__ __forceinline__ double small_warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int N>
+struct SmallLayout {
+  static constexpr int NTEAM = (kSmallThreads / 32) * Team<N>::PER_WARP;
+  // tw[N], bufs[NTEAM][N], F[N] (double2); rho[N], vh[N] (double)
+  static constexpr size_t bytes = sizeof(double2) * (size_t)N * (2 + NTEAM) + sizeof(double) * 2 * (size_t)N;
+};
+
+// Last CTA of the launch: the observables of the stage input (mode 0 with a
+// previous step, mode 4), or the step counter (mode 3).
+__device__ void small_finalize(const SmallStageArgs& a) {
+  const int lane = threadIdx.x;
+  if (a.mode == 3) {
+    if (lane == 0) *a.it = *a.it + 1;
+    return;
+  }
+  const int idx = *a.it - 1;
+  if (idx < 0) return;
+  const int ncol = a.nk * a.nb;
+  double ekin = 0.0, jre = 0.0, exr = 0.0;
+  for (int c = lane; c < ncol; c += 32) {
+    const int ib = c % a.nb;
+    const double occ = ib < a.nbocc ? a.occ : 0.0;
+    const double* cb = a.colbuf + (size_t)c * 4;
+    ekin += occ * __ldcg(cb) * a.dvcell;
+    jre += occ * __ldcg(cb + 1);
+    if (ib < a.nbocc) exr += occ * __ldcg(cb + 2) * a.dvcell;
+  }
+  ekin = small_warp_sum(ekin);
+  jre = small_warp_sum(jre);
+  exr = small_warp_sum(exr);
+  if (lane != 0) return;
+  const double Nele = __ldcg(a.scal), Eion = __ldcg(a.scal + 1), EH = __ldcg(a.scal + 2);
+  const double Ex = a.hf ? 0.5 * exr : 0.0;
+  const double Etot = (ekin + Eion + EH) + Ex;
+  const double Je = -(jre * a.dvcell / a.vcell);
+  if (a.series_E) a.series_E[idx] = Etot;
+  if (a.series_J) a.series_J[idx] = Je;
+  if (a.series_N) a.series_N[idx] = Nele;
+  if (a.out_obs) {
+    a.out_obs[0] = Etot;
+    a.out_obs[1] = ekin;
+    a.out_obs[2] = Eion;
+    a.out_obs[3] = EH;
+    a.out_obs[4] = Ex;
+    a.out_obs[5] = Je;
+    a.out_obs[6] = Nele;
+  }
+  if (!(isfinite(Etot) && isfinite(Je) && isfinite(Nele)) && a.nonfinite) *a.nonfinite = 1;
+}
+
+template <int N>
+__global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a) {
+  using TM = Team<N>;
+  constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
+  constexpr int NTEAM = SmallLayout<N>::NTEAM;
+  extern __shared__ double2 sm2[];
+  double2* tw_s = sm2;                     // N
+  double2* bufs = tw_s + N;                // NTEAM * N
+  double2* F_s = bufs + NTEAM * N;         // N
+  double* rho_s = reinterpret_cast<double*>(F_s + N);
+  double* vh_s = rho_s + N;
+  __shared__ int last_s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tl = lane % T, team = warp * PW + lane / T;
+  double2* buf = bufs + team * N;
+  const int c = blockIdx.x;                // output column (k, b)
+  const int kr = c / a.nb, ib = c % a.nb;
+  const int M = a.nk * a.nbocc;
+  const bool occupied = ib < a.nbocc;
+  const double2* wcol = a.u + (size_t)c * N;
+
+  for (int i = tid; i < N; i += kSmallThreads) tw_s[i] = a.tw[i];
+  // density of the stage input, in the reference's order (ig -> ik -> ib)
+  for (int ig = tid; ig < N; ig += kSmallThreads) {
+    double s = 0.0;
+    for (int ik = 0; ik < a.nk; ++ik)
+      for (int b = 0; b < a.nbocc; ++b) {
+        const double2 z = a.u[((size_t)ik * a.nb + b) * N + ig];
+        s += fma(a.occ * z.x, z.x, (a.occ * z.y) * z.y);
+      }
+    rho_s[ig] = s;
+  }
+  __syncthreads();
+  // Hartree potential vH = Re IFFT(vCG FFT(rho)) / N (one warp)
+  if (warp == 0) {
+    double2 x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = make_double2(rho_s[TM::pos(tl, e)], 0.0);
+    fft_team<N, -1>(x, buf, tw_s, tl);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const double v = a.vCG[TM::pos(tl, e)];
+      x[e] = make_double2(v * x[e].x, v * x[e].y);
+    }
+    fft_team<N, +1>(x, buf, tw_s, tl);
+    if (lane < T) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) vh_s[TM::pos(tl, e)] = x[e].x / (double)N;
+    }
+  }
+  __syncthreads();
+  // density scalars Nele, Eion, EH (the first CTA)
+  if (c == 0 && warp == 0) {
+    double sn = 0.0, si = 0.0, sh = 0.0;
+    for (int ig = lane; ig < N; ig += 32) {
+      sn += rho_s[ig];
+      si += a.vion[ig] * rho_s[ig];
+      sh += vh_s[ig] * rho_s[ig];
+    }
+    sn = small_warp_sum(sn);
+    si = small_warp_sum(si);
+    sh = small_warp_sum(sh);
+    if (lane == 0) {
+      a.scal[0] = sn * a.dvcell;
+      a.scal[1] = si * a.dvcell;
+      a.scal[2] = 0.5 * sh * a.dvcell;
+    }
+  }
+  // exchange of column c against every occupied orbital; teams share the pairs
+  const bool need_ex = a.hf && (a.mode != 4 || occupied);
+  if (need_ex) {
+    double2 wv[E], acc[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      wv[e] = wcol[TM::pos(tl, e)];
+      acc[e] = make_double2(0.0, 0.0);
+    }
+    // warp-uniform trip count: every team of a warp runs the same rounds
+    for (int base = warp * PW; base < M; base += NTEAM) {
+      const int p = base + lane / T;
+      const bool valid = p < M;
+      const int pp = valid ? p : 0;
+      const int kc = pp / a.nbocc, bc = pp % a.nbocc;
+      const double2* ucol = a.u + ((size_t)kc * a.nb + bc) * N;
+      const double* kern = a.kern + (size_t)(kr - kc + a.nk - 1) * N;
+      double2 x[E];
+#pragma unroll
+      for (int e = 0; e < E; ++e) x[e] = cmulc(wv[e], ucol[TM::pos(tl, e)]);
+      fft_team<N, -1>(x, buf, tw_s, tl);
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const double v = __ldg(kern + TM::pos(tl, e));
+        x[e] = make_double2(v * x[e].x, v * x[e].y);
+      }
+      fft_team<N, +1>(x, buf, tw_s, tl);
+      if (valid) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) acc[e] = cfma(x[e], ucol[TM::pos(tl, e)], acc[e]);
+      }
+    }
+    __syncthreads();  // every team is done with its transform buffer
+#pragma unroll
+    for (int e = 0; e < E; ++e) buf[TM::pos(tl, e)] = acc[e];
+    __syncthreads();
+    // fixed-order reduction over teams
+    for (int i = tid; i < N; i += kSmallThreads) {
+      double2 f = bufs[i];
+      for (int t2 = 1; t2 < NTEAM; ++t2) f = cadd(f, bufs[(size_t)t2 * N + i]);
+      F_s[i] = f;
+    }
+  } else {
+    for (int i = tid; i < N; i += kSmallThreads) F_s[i] = make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  // kinetic term, h w and the stage epilogue of column c (warp 0; its teams
+  // compute the same column, the first team writes)
+  if (warp == 0) {
+    const double A = afield_value(a.af);
+    const double kAx = a.kx[kr] + A;
+    const double kA2 = kAx * kAx;
+    const bool writer = lane < T;
+    double2 wv[E], x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      wv[e] = wcol[TM::pos(tl, e)];
+      x[e] = wv[e];
+    }
+    double exr = 0.0, exi = 0.0;
+    if (a.mode == 4) {
+      // closing pass: only <u|F> of the occupied columns
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const double2 f = F_s[TM::pos(tl, e)];
+        exr += wv[e].x * f.x + wv[e].y * f.y;
+        exi += wv[e].x * f.y - wv[e].y * f.x;
+      }
+      exr = team_sum<T>(exr);
+      exi = team_sum<T>(exi);
+      if (writer && tl == 0 && occupied) {
+        a.colbuf[(size_t)c * 4 + 2] = exr;
+        a.colbuf[(size_t)c * 4 + 3] = exi;
+      }
+    } else {
+      fft_team<N, -1>(x, buf, tw_s, tl);
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const double G = a.Gx[TM::pos(tl, e)];
+        const double m = 0.5 * (G * G + 2.0 * G * kAx + kA2);
+        x[e] = make_double2(m * x[e].x / (double)N, m * x[e].y / (double)N);
+      }
+      fft_team<N, +1>(x, buf, tw_s, tl);
+      bool bad = false;
+      double2 nx[E];
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int q = TM::pos(tl, e);
+        const double v = vh_s[q] + a.vion[q];
+        double2 h = make_double2(x[e].x + v * wv[e].x, x[e].y + v * wv[e].y);
+        const double2 f = F_s[q];
+        if (a.mode == 0) {
+          exr += wv[e].x * f.x + wv[e].y * f.y;
+          exi += wv[e].x * f.y - wv[e].y * f.x;
+        }
+        h = cadd(h, f);
+        const double2 k = make_double2(h.y, -h.x);  // -i h
+        const size_t o = (size_t)c * N + q;
+        const double2 u0 = a.u0[o];
+        if (a.mode < 3) {
+          const double cdt = (a.mode == 2) ? a.dt : 0.5 * a.dt;
+          nx[e] = make_double2(u0.x + cdt * k.x, u0.y + cdt * k.y);
+          if (writer) {
+            a.kbuf[a.mode][o] = k;
+            a.out[o] = nx[e];
+          }
+        } else {
+          const double2 k0 = a.kbuf[0][o], k1 = a.kbuf[1][o], k2 = a.kbuf[2][o];
+          double sx = k0.x + 2.0 * k1.x, sy = k0.y + 2.0 * k1.y;
+          sx = sx + 2.0 * k2.x;
+          sy = sy + 2.0 * k2.y;
+          sx = sx + k.x;
+          sy = sy + k.y;
+          sx = sx * a.dt / 6.0;
+          sy = sy * a.dt / 6.0;
+          nx[e] = make_double2(u0.x + sx, u0.y + sy);
+        }
+        bad |= !(isfinite(nx[e].x) && isfinite(nx[e].y));
+      }
+      if (a.mode == 3) {
+        // the update goes in place only after every lane has read its u0
+        __syncwarp();
+        if (writer) {
+#pragma unroll
+          for (int e = 0; e < E; ++e) a.u0[(size_t)c * N + TM::pos(tl, e)] = nx[e];
+        }
+        // Ekin and Je of the updated column at this stage's field (Parseval)
+        fft_team<N, -1>(nx, buf, tw_s, tl);
+        double ek = 0.0, je = 0.0;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          const double G = a.Gx[TM::pos(tl, e)];
+          const double m2 = nx[e].x * nx[e].x + nx[e].y * nx[e].y;
+          ek += 0.5 * (G * G + 2.0 * G * kAx + kA2) * m2;
+          je += (G + a.kx[kr] + A) * m2;
+        }
+        ek = team_sum<T>(ek) / (double)N;
+        je = team_sum<T>(je) / (double)N;
+        if (writer && tl == 0) {
+          a.colbuf[(size_t)c * 4] = ek;
+          a.colbuf[(size_t)c * 4 + 1] = je;
+        }
+      }
+      if (a.mode == 0) {
+        exr = team_sum<T>(exr);
+        exi = team_sum<T>(exi);
+        if (writer && tl == 0 && occupied) {
+          a.colbuf[(size_t)c * 4 + 2] = exr;
+          a.colbuf[(size_t)c * 4 + 3] = exi;
+        }
+      }
+      if (bad && writer && a.nonfinite) *a.nonfinite = 1;
+    }
+  }
+  // the last CTA to finish finalizes (nothing waits on another CTA)
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    const unsigned t = atomicAdd(a.ticket, 1u);
+    last_s = (t == gridDim.x - 1) ? 1 : 0;
+  }
+  __syncthreads();
+  if (last_s && warp == 0) {
+    __threadfence();
+    small_finalize(a);
+    if (lane == 0) *a.ticket = 0u;
+  }
+}
+
+template <int N>
+static cudaError_t small_impl(const SmallStageArgs& a, cudaStream_t s) {
+  const int ncols = a.nk * a.nb;
+  k_small_stage<N><<<ncols, kSmallThreads, SmallLayout<N>::bytes, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t small_configure() {
+  return cudaFuncSetAttribute(k_small_stage<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)SmallLayout<N>::bytes);
+}
+
+bool small_stage_supported(int NG) { return NG >= 16 && NG <= 256 && (NG & (NG - 1)) == 0; }
+
+cudaError_t launch_small_stage(int NG, const SmallStageArgs& a, cudaStream_t s) {
+  switch (NG) {
+    case 16: return small_impl<16>(a, s);
+    case 32: return small_impl<32>(a, s);
+    case 64: return small_impl<64>(a, s);
+    case 128: return small_impl<128>(a, s);
+    case 256: return small_impl<256>(a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t configure_small_kernels() {
+  cudaError_t e;
+  if ((e = small_configure<16>()) != cudaSuccess) return e;
+  if ((e = small_configure<32>()) != cudaSuccess) return e;
+  if ((e = small_configure<64>()) != cudaSuccess) return e;
+  if ((e = small_configure<128>()) != cudaSuccess) return e;
+  return small_configure<256>();
+}
+
+}  // namespace mattohf

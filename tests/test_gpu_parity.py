@@ -214,15 +214,24 @@ def test_observables(name):
 
 
 @pytest.mark.parametrize("name", ["ng32_nk4", "ng64_nk8", "ng16_nk3_unocc"])
-def test_rk4_run(name):
+@pytest.mark.parametrize("small", [0, 1])
+def test_rk4_run(name, small):
+    """The RT loop vs the oracle, through the tiled path (small=0) and the fused
+    one-launch-per-stage path (small=1)."""
     from oracle import mattohf_oracle as O
-    from mattohf_gb300 import define_afield
+    from mattohf_gb300 import define_afield, _capi
     cfg, ctx, S = setup(name)
+    if small and cfg.NG > 256:
+        pytest.skip("fused stages need NG <= 256")
     cfg = dataclasses.replace(cfg, dt=0.004, NT=5, field_option="LP", omegac=1.55, Tpulse=0.1, E0=20.0)
     u0 = O.gram_schmidt(S, O.init_wf(S))
     _, A, Aave, _ = define_afield(cfg)
     ctx.set_orbitals(u0)
-    E, J, N = ctx.rk4_run(A, Aave, cfg.dt)
+    ctx.set_option(_capi.OPT_SMALL_STAGES, small)
+    try:
+        E, J, N = ctx.rk4_run(A, Aave, cfg.dt)
+    finally:
+        ctx.set_option(_capi.OPT_SMALL_STAGES, 2)
     S.cfg = to_oracle_config(cfg)
     ref = O.rt_calculation(S, u0, nt=cfg.NT, A=A, Aave=Aave)
     assert rel(E, ref.Etot) <= TOL_RT
@@ -232,17 +241,26 @@ def test_rk4_run(name):
 
 
 def test_rk4_step_matches_run():
-    """mattohf_rk4_step (host fields) == one step of mattohf_rk4_run (device fields)."""
+    """mattohf_rk4_step (host fields) == one step of mattohf_rk4_run (device fields):
+    bitwise through the same tiled kernels, to rounding through the fused stages."""
     from oracle import mattohf_oracle as O
+    from mattohf_gb300 import _capi
     cfg, ctx, S = setup("ng32_nk4")
     u0 = O.gram_schmidt(S, O.init_wf(S))
     ctx.set_orbitals(u0)
     ctx.RT_RK4_ubk(0.01, 0.02, 0.005)
     a = ctx.get_orbitals()
+    ctx.set_option(_capi.OPT_SMALL_STAGES, 0)
+    try:
+        ctx.set_orbitals(u0)
+        ctx.rk4_run(np.array([0.02]), np.array([0.01]), 0.005)
+        b = ctx.get_orbitals()
+    finally:
+        ctx.set_option(_capi.OPT_SMALL_STAGES, 2)
+    assert np.array_equal(a, b)
     ctx.set_orbitals(u0)
     ctx.rk4_run(np.array([0.02]), np.array([0.01]), 0.005)
-    b = ctx.get_orbitals()
-    assert np.array_equal(a, b)
+    assert rel(ctx.get_orbitals(), a) <= 1e-14
     ref = O.rk4_step(S, u0, 0.01, 0.02, 0.005)
     assert rel(a, ref) <= TOL_OP
 
@@ -259,11 +277,13 @@ def test_taylor_propagators(variant):
     assert rel(got, ref) <= TOL_OP
 
 
-def test_graph_equals_eager():
+@pytest.mark.parametrize("small", [0, 1])
+def test_graph_equals_eager(small):
     """The graph-replayed RT loop is bitwise identical to eager launches."""
     from oracle import mattohf_oracle as O
     from mattohf_gb300 import _capi
     cfg, ctx, S = setup("ng64_nk8")
+    ctx.set_option(_capi.OPT_SMALL_STAGES, small)
     u0 = O.gram_schmidt(S, O.init_wf(S))
     A = np.linspace(0.0, 0.05, 4)
     Aave = np.concatenate([[A[0] / 2], 0.5 * (A[1:] + A[:-1])])
@@ -275,12 +295,14 @@ def test_graph_equals_eager():
     r2 = ctx.rk4_run(A, Aave, 0.005)
     u2 = ctx.get_orbitals()
     ctx.set_option(_capi.OPT_GRAPH, 1)
+    ctx.set_option(_capi.OPT_SMALL_STAGES, 2)
     assert np.array_equal(u1, u2)
     for x, y in zip(r1, r2):
         assert np.array_equal(x, y)
 
 
-def test_nonfinite_detected():
+@pytest.mark.parametrize("small", [0, 1])
+def test_nonfinite_detected(small):
     """An unstable dt overflows; the run returns ERR_NONFINITE naming the step."""
     from oracle import mattohf_oracle as O
     from mattohf_gb300 import MattohfError, _capi
@@ -289,8 +311,12 @@ def test_nonfinite_detected():
     ctx.set_orbitals(u0)
     nt = 600
     A = np.zeros(nt)
-    with pytest.raises(MattohfError) as ei:
-        ctx.rk4_run(A, A, 0.5)   # eps_max*dt ~ 100 >> 2.83
+    ctx.set_option(_capi.OPT_SMALL_STAGES, small)
+    try:
+        with pytest.raises(MattohfError) as ei:
+            ctx.rk4_run(A, A, 0.5)   # eps_max*dt ~ 100 >> 2.83
+    finally:
+        ctx.set_option(_capi.OPT_SMALL_STAGES, 2)
     assert ei.value.status == _capi.ERR_NONFINITE
     assert "step" in str(ei.value)
 
