@@ -45,6 +45,7 @@ __device__ void small_finalize(const SmallStageArgs& a) {
     if (lane == 0) *a.it = *a.it + 1;
     return;
   }
+  if (a.mode != 0 && a.mode != 4) return;  // stages 1 and 2 finalize nothing
   const int idx = *a.it - 1;
   if (idx < 0) return;
   const int ncol = a.nk * a.nb;
