@@ -104,7 +104,11 @@ struct mattohf_ctx {
   int opt_tile = 0;           // symmetric-exchange tile size (0 = automatic)
   int opt_small = 2;          // fused small-problem RK4 stages: 0 off, 1 on, 2 automatic
   bool step_small = false;    // the captured step graph uses the fused stages
-  unsigned* d_ticket = nullptr;  // CTA completion counter of the fused stages
+  unsigned* d_ticket = nullptr;  // completion counters of the fused stages [1 + NK*NB]
+  double2* d_small_part = nullptr;  // exchange partials of the fused stages
+  size_t small_part_cap = 0;
+  int small_P = 1;                // CTAs per column of the fused stages
+  int nsm = 0;                    // multiprocessors of the device
   int* d_int = nullptr;  // [0] = step counter, [1] = non-finite flag, [2] = solver flag
   // RT series
   double *d_A = nullptr, *d_Aave = nullptr, *d_sE = nullptr, *d_sJ = nullptr, *d_sN = nullptr;
@@ -552,6 +556,29 @@ bool use_small(const mattohf_ctx* ctx) {
   return ctx->NK * ctx->NB <= 256 && M * M * ctx->NG <= ((size_t)1 << 20);
 }
 
+// CTAs per column: enough to fill about two CTAs per multiprocessor, and at
+// least enough that every CTA's pairs fit one round of its pair teams.
+int small_ctas_per_column(const mattohf_ctx* ctx) {
+  const int ncols = ctx->NK * ctx->NB, M = ctx->NK * ctx->NBocc;
+  const int pt = small_pair_teams(ctx->NG);
+  int P = std::min(M, std::max(1, 2 * ctx->nsm / ncols));
+  P = std::max(P, (M + pt - 1) / pt);
+  return std::max(1, std::min(P, M));
+}
+
+// Buffers of the fused stages, sized before any capture.
+int ensure_small_buffers(mattohf_ctx* ctx) {
+  ctx->small_P = small_ctas_per_column(ctx);
+  const size_t need = (size_t)ctx->NK * ctx->NB * ctx->small_P * ctx->NG;
+  if (need > ctx->small_part_cap) {
+    if (ctx->capturing) return fail(ctx, MATTOHF_ERR_STATE, "fused-stage scratch growth during capture");
+    destroy_graph(ctx);  // a captured step holds the old pointer
+    CKR(dalloc(ctx, &ctx->d_small_part, need));
+    ctx->small_part_cap = need;
+  }
+  return MATTOHF_OK;
+}
+
 SmallStageArgs small_base(mattohf_ctx* ctx, double dt) {
   SmallStageArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -571,8 +598,9 @@ SmallStageArgs small_base(mattohf_ctx* ctx, double dt) {
   a.Gx = ctx->d_Gx;
   a.kx = ctx->d_kx;
   a.tw = ctx->tw;
+  a.P = ctx->small_P;
+  a.part = ctx->d_small_part;
   a.colbuf = ctx->d_colbuf;
-  a.scal = ctx->d_scal;
   a.series_E = ctx->d_sE;
   a.series_J = ctx->d_sJ;
   a.series_N = ctx->d_sN;
@@ -789,8 +817,10 @@ int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out) {
   for (int s = 0; s < 4; ++s)
     if ((rc = dalloc(ctx, &ctx->d_k[s], nu))) return bail(rc);
   if ((rc = dalloc(ctx, &ctx->d_hpre, nu))) return bail(rc);
-  if (cudaMalloc(&ctx->d_ticket, sizeof(unsigned)) != cudaSuccess ||
-      cudaMemset(ctx->d_ticket, 0, sizeof(unsigned)) != cudaSuccess)
+  const size_t ntick = 1 + (size_t)ctx->NK * ctx->NB;
+  if (cudaMalloc(&ctx->d_ticket, sizeof(unsigned) * ntick) != cudaSuccess ||
+      cudaMemset(ctx->d_ticket, 0, sizeof(unsigned) * ntick) != cudaSuccess ||
+      cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess)
     return bail(MATTOHF_ERR_ALLOC);
   if (cudaMemsetAsync(ctx->d_u, 0, nu * sizeof(double2), ctx->st) != cudaSuccess ||
       cudaMemsetAsync(ctx->d_int, 0, 8 * sizeof(int), ctx->st) != cudaSuccess ||
@@ -836,7 +866,8 @@ int mattohf_destroy(mattohf_ctx* ctx) {
                   ctx->d_scratch, ctx->d_colbuf, ctx->d_int, ctx->d_A, ctx->d_Aave, ctx->d_sE,
                   ctx->d_sJ, ctx->d_sN, ctx->d_work, ctx->d_hwork, ctx->d_M, ctx->d_V, ctx->d_evals,
                   ctx->d_eps, ctx->d_err, ctx->d_sym, ctx->d_symF, ctx->d_dpart,
-                  ctx->d_udf, ctx->d_kern_df, ctx->d_tw_df, ctx->d_hpre, ctx->d_ticket};
+                  ctx->d_udf, ctx->d_kern_df, ctx->d_tw_df, ctx->d_hpre, ctx->d_ticket,
+                  ctx->d_small_part};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
@@ -1174,7 +1205,8 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
   fcur.mode = ACUR;
   const bool use_graph = ctx->opt_graph && !ctx->opt_timing;
   const bool small = use_small(ctx);
-  CK(cudaMemsetAsync(ctx->d_ticket, 0, sizeof(unsigned), ctx->st));
+  if (small) CKR(ensure_small_buffers(ctx));
+  CK(cudaMemsetAsync(ctx->d_ticket, 0, sizeof(unsigned) * (1 + (size_t)ctx->NK * ctx->NB), ctx->st));
   if (use_graph && (!ctx->step_exec || ctx->step_dt != dt || ctx->step_small != small)) {
     destroy_graph(ctx);
     cudaGraph_t g;

@@ -186,9 +186,12 @@ struct CombineArgs {
   double2* hpre;            // [NK][NB][NG]
 };
 
-// Fused RK4 stage for small problems (k_small.cu): one CTA per output column
-// does the density, Hartree potential, exchange, kinetic term and the stage's
-// RK4 update of its column, so a step is 4 launches instead of about 29.
+// Fused RK4 stage for small problems (k_small.cu).  Each output column (k, b)
+// is served by P CTAs that share its exchange pairs; the last of them to
+// finish (a per-column ticket) sums the P partials in a fixed order and does
+// the density-dependent kinetic/local terms and the stage's RK4 update, and
+// the last column to finish (a global ticket) writes the observables.  A step
+// is 4 launches instead of about 29, spread over ncols * P CTAs.
 struct SmallStageArgs {
   const double2* u;         // stage input [NK][NB][NG]
   double2* u0;              // base state (updated in place by stage 3)
@@ -198,6 +201,7 @@ struct SmallStageArgs {
   double dt;
   AField af;
   int nk, nb, nbocc, hf;
+  int P;                    // CTAs per column
   double occ, dvcell, vcell;
   const double* kern;       // (2NK-1) x NG exchange kernel table
   const double* vCG;
@@ -205,18 +209,19 @@ struct SmallStageArgs {
   const double* Gx;
   const double* kx;
   const double2* tw;
+  double2* part;            // [ncols][P][NG] exchange partials
   double* colbuf;           // [ncols][4]: Ekin part, J part, Re<u|F>, Im<u|F>
-  double* scal;             // [3]: Nele, Eion, EH of the input density
   double* series_E;         // per-step observables, indexed by the step counter
   double* series_J;
   double* series_N;
   int* it;                  // step counter
   int* nonfinite;
-  unsigned* ticket;         // CTA completion counter (last CTA finalizes; reset by it)
+  unsigned* ticket;         // [1 + ncols]: global, then per-column completion counters
   double* out_obs;          // mode 4: [7] Etot, Ekin, Eion, EH, Ex, Je, Nele
 };
 cudaError_t launch_small_stage(int NG, const SmallStageArgs& a, cudaStream_t s);
 bool small_stage_supported(int NG);
+int small_pair_teams(int NG);
 cudaError_t configure_small_kernels();
 
 struct ObsReduceArgs {

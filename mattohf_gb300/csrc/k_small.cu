@@ -3,26 +3,29 @@
 // For small grids and few orbitals every kernel of the general path is
 // latency-bound, and a step of about 29 dependent launches costs more than the
 // arithmetic.  Here one launch does a whole RK4 stage (src/RT_calculation.f90:
-// 154-173), with one CTA per output column (k, b):
-//   * the density of the stage input (F:55-71, reference order ig -> ik -> ib),
-//     recomputed by every CTA, and the Hartree potential (F:147-162);
-//   * the exchange of the column against every occupied orbital (F:237-261,
-//     all ordered pairs, no symmetry: teams of the CTA share the pairs and are
-//     reduced in a fixed order);
-//   * the kinetic term (F:212-234), h w, and the stage's RK4 update of the
-//     column, into a buffer that is never the stage input (no read/write race
-//     between CTAs).
-// Observables (F:74-119, F:165-183, F:289-318) are folded in: stage 3 stores
-// Ekin and Je of each updated column; the next stage 0 (or the closing pass,
-// mode 4) recomputes the density and <u|F u>, and its last CTA to finish
-// writes Etot, Je, Nele of the previous step.  "Last CTA" is decided by an
-// atomic ticket after a fence; nothing waits on another CTA.
+// 154-173).  Output column c = (k, b) is served by P CTAs (c, chunk):
+//   * every CTA's last warp recomputes the density of the stage input (F:55-71,
+//     reference order ig -> ik -> ib) and the Hartree potential (F:147-162);
+//   * the other warps apply the exchange of column c against the CTA's chunk of
+//     the occupied orbitals (F:237-261, ordered pairs, no symmetry), one pair
+//     per team, and the CTA writes its partial sum;
+//   * the last CTA of the column (per-column ticket) adds the P partials in
+//     chunk order, then does the kinetic term (F:212-234), h w and the stage's
+//     RK4 update of the column, into a buffer that is never the stage input;
+//   * the last column (global ticket) writes the observables (F:74-119,
+//     F:165-183, F:289-318): stage 3 stores Ekin and Je of each updated column,
+//     the next stage 0 (or the closing pass, mode 4) adds <u|F u> and the
+//     density scalars of its input and writes Etot, Je, Nele of the previous
+//     step.
+// A ticket is an atomic counter taken after a fence; the CTA that draws the
+// last number does the follow-up work.  Nothing waits on another CTA.
 #include "fft.cuh"
 #include "internal.h"
 
 namespace mattohf {
 
 constexpr int kSmallThreads = 256;
+constexpr int kSmallWarps = kSmallThreads / 32;
 
 __device__ __forceinline__ double small_warp_sum(double v) {
 #pragma unroll
@@ -32,15 +35,18 @@ __device__ __forceinline__ double small_warp_sum(double v) {
 
 template <int N>
 struct SmallLayout {
-  static constexpr int NTEAM = (kSmallThreads / 32) * Team<N>::PER_WARP;
+  static constexpr int PW = Team<N>::PER_WARP;
+  static constexpr int NTEAM = kSmallWarps * PW;
+  static constexpr int PAIR_TEAMS = (kSmallWarps - 1) * PW;  // the last warp does the density
   // tw[N], bufs[NTEAM][N], F[N] (double2); rho[N], vh[N] (double)
   static constexpr size_t bytes = sizeof(double2) * (size_t)N * (2 + NTEAM) + sizeof(double) * 2 * (size_t)N;
 };
 
-// Last CTA of the launch: the observables of the stage input (mode 0 with a
-// previous step, mode 4), or the step counter (mode 3).
-__device__ void small_finalize(const SmallStageArgs& a) {
-  const int lane = threadIdx.x;
+// The global last CTA: the observables of the stage input (mode 0 with a
+// previous step, mode 4) from the column buffer and this CTA's own density,
+// or the step counter (mode 3).  Run by one warp.
+__device__ void small_finalize(const SmallStageArgs& a, const double* rho_s, const double* vh_s, int N) {
+  const int lane = threadIdx.x & 31;
   if (a.mode == 3) {
     if (lane == 0) *a.it = *a.it + 1;
     return;
@@ -58,11 +64,20 @@ __device__ void small_finalize(const SmallStageArgs& a) {
     jre += occ * __ldcg(cb + 1);
     if (ib < a.nbocc) exr += occ * __ldcg(cb + 2) * a.dvcell;
   }
+  double sn = 0.0, si = 0.0, sh = 0.0;
+  for (int ig = lane; ig < N; ig += 32) {
+    sn += rho_s[ig];
+    si += a.vion[ig] * rho_s[ig];
+    sh += vh_s[ig] * rho_s[ig];
+  }
   ekin = small_warp_sum(ekin);
   jre = small_warp_sum(jre);
   exr = small_warp_sum(exr);
+  sn = small_warp_sum(sn);
+  si = small_warp_sum(si);
+  sh = small_warp_sum(sh);
   if (lane != 0) return;
-  const double Nele = __ldcg(a.scal), Eion = __ldcg(a.scal + 1), EH = __ldcg(a.scal + 2);
+  const double Nele = sn * a.dvcell, Eion = si * a.dvcell, EH = 0.5 * sh * a.dvcell;
   const double Ex = a.hf ? 0.5 * exr : 0.0;
   const double Etot = (ekin + Eion + EH) + Ex;
   const double Je = -(jre * a.dvcell / a.vcell);
@@ -86,6 +101,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   using TM = Team<N>;
   constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
   constexpr int NTEAM = SmallLayout<N>::NTEAM;
+  constexpr int PAIR_TEAMS = SmallLayout<N>::PAIR_TEAMS;
   extern __shared__ double2 sm2[];
   double2* tw_s = sm2;                     // N
   double2* bufs = tw_s + N;                // NTEAM * N
@@ -96,26 +112,29 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tl = lane % T, team = warp * PW + lane / T;
   double2* buf = bufs + team * N;
-  const int c = blockIdx.x;                // output column (k, b)
+  const int c = blockIdx.x / a.P;          // output column (k, b)
+  const int chunk = blockIdx.x % a.P;
   const int kr = c / a.nb, ib = c % a.nb;
   const int M = a.nk * a.nbocc;
+  const int ppc = (M + a.P - 1) / a.P;     // pairs per CTA
+  const int p0 = chunk * ppc, p1 = min(M, p0 + ppc);
   const bool occupied = ib < a.nbocc;
   const double2* wcol = a.u + (size_t)c * N;
 
   for (int i = tid; i < N; i += kSmallThreads) tw_s[i] = a.tw[i];
-  // density of the stage input, in the reference's order (ig -> ik -> ib)
-  for (int ig = tid; ig < N; ig += kSmallThreads) {
-    double s = 0.0;
-    for (int ik = 0; ik < a.nk; ++ik)
-      for (int b = 0; b < a.nbocc; ++b) {
-        const double2 z = a.u[((size_t)ik * a.nb + b) * N + ig];
-        s += fma(a.occ * z.x, z.x, (a.occ * z.y) * z.y);
-      }
-    rho_s[ig] = s;
-  }
   __syncthreads();
-  // Hartree potential vH = Re IFFT(vCG FFT(rho)) / N (one warp)
-  if (warp == 0) {
+  if (warp == kSmallWarps - 1) {
+    // density of the stage input (reference order ig -> ik -> ib) and vH
+    for (int ig = lane; ig < N; ig += 32) {
+      double s = 0.0;
+      for (int ik = 0; ik < a.nk; ++ik)
+        for (int b = 0; b < a.nbocc; ++b) {
+          const double2 z = a.u[((size_t)ik * a.nb + b) * N + ig];
+          s += fma(a.occ * z.x, z.x, (a.occ * z.y) * z.y);
+        }
+      rho_s[ig] = s;
+    }
+    __syncwarp();
     double2 x[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) x[e] = make_double2(rho_s[TM::pos(tl, e)], 0.0);
@@ -130,45 +149,22 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
 #pragma unroll
       for (int e = 0; e < E; ++e) vh_s[TM::pos(tl, e)] = x[e].x / (double)N;
     }
-  }
-  __syncthreads();
-  // density scalars Nele, Eion, EH (the first CTA)
-  if (c == 0 && warp == 0) {
-    double sn = 0.0, si = 0.0, sh = 0.0;
-    for (int ig = lane; ig < N; ig += 32) {
-      sn += rho_s[ig];
-      si += a.vion[ig] * rho_s[ig];
-      sh += vh_s[ig] * rho_s[ig];
-    }
-    sn = small_warp_sum(sn);
-    si = small_warp_sum(si);
-    sh = small_warp_sum(sh);
-    if (lane == 0) {
-      a.scal[0] = sn * a.dvcell;
-      a.scal[1] = si * a.dvcell;
-      a.scal[2] = 0.5 * sh * a.dvcell;
-    }
-  }
-  // exchange of column c against every occupied orbital; teams share the pairs
-  const bool need_ex = a.hf && (a.mode != 4 || occupied);
-  if (need_ex) {
-    double2 wv[E], acc[E];
+  } else if (a.hf && (a.mode != 4 || occupied)) {
+    // this CTA's exchange pairs of column c, one pair per team per round
+    double2 acc[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-      wv[e] = wcol[TM::pos(tl, e)];
-      acc[e] = make_double2(0.0, 0.0);
-    }
+    for (int e = 0; e < E; ++e) acc[e] = make_double2(0.0, 0.0);
     // warp-uniform trip count: every team of a warp runs the same rounds
-    for (int base = warp * PW; base < M; base += NTEAM) {
+    for (int base = p0 + warp * PW; base < p1; base += PAIR_TEAMS) {
       const int p = base + lane / T;
-      const bool valid = p < M;
-      const int pp = valid ? p : 0;
+      const bool valid = p < p1;
+      const int pp = valid ? p : p0;
       const int kc = pp / a.nbocc, bc = pp % a.nbocc;
       const double2* ucol = a.u + ((size_t)kc * a.nb + bc) * N;
       const double* kern = a.kern + (size_t)(kr - kc + a.nk - 1) * N;
       double2 x[E];
 #pragma unroll
-      for (int e = 0; e < E; ++e) x[e] = cmulc(wv[e], ucol[TM::pos(tl, e)]);
+      for (int e = 0; e < E; ++e) x[e] = cmulc(wcol[TM::pos(tl, e)], ucol[TM::pos(tl, e)]);
       fft_team<N, -1>(x, buf, tw_s, tl);
 #pragma unroll
       for (int e = 0; e < E; ++e) {
@@ -181,18 +177,38 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
         for (int e = 0; e < E; ++e) acc[e] = cfma(x[e], ucol[TM::pos(tl, e)], acc[e]);
       }
     }
-    __syncthreads();  // every team is done with its transform buffer
+    __syncwarp();
 #pragma unroll
     for (int e = 0; e < E; ++e) buf[TM::pos(tl, e)] = acc[e];
-    __syncthreads();
-    // fixed-order reduction over teams
-    for (int i = tid; i < N; i += kSmallThreads) {
-      double2 f = bufs[i];
-      for (int t2 = 1; t2 < NTEAM; ++t2) f = cadd(f, bufs[(size_t)t2 * N + i]);
-      F_s[i] = f;
-    }
   } else {
-    for (int i = tid; i < N; i += kSmallThreads) F_s[i] = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int e = 0; e < E; ++e) buf[TM::pos(tl, e)] = make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  // this CTA's partial (pair teams in order) -> part[c][chunk]
+  double2* mine = a.part + ((size_t)c * a.P + chunk) * N;
+  for (int i = tid; i < N; i += kSmallThreads) {
+    double2 f = bufs[i];
+    for (int t2 = 1; t2 < PAIR_TEAMS; ++t2) f = cadd(f, bufs[(size_t)t2 * N + i]);
+    mine[i] = f;
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    const unsigned t = atomicAdd(a.ticket + 1 + c, 1u);
+    last_s = (t == (unsigned)a.P - 1) ? 1 : 0;
+  }
+  __syncthreads();
+  if (!last_s) return;
+  // ---- the last CTA of column c: ordered sum of the P partials
+  __threadfence();
+  if (tid == 0) a.ticket[1 + c] = 0u;
+  const double2* cp = a.part + (size_t)c * a.P * N;
+  for (int i = tid; i < N; i += kSmallThreads) {
+    double2 f = __ldcg(cp + i);
+    for (int ch = 1; ch < a.P; ++ch) f = cadd(f, __ldcg(cp + (size_t)ch * N + i));
+    F_s[i] = f;
   }
   __syncthreads();
   // kinetic term, h w and the stage epilogue of column c (warp 0; its teams
@@ -303,25 +319,25 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       if (bad && writer && a.nonfinite) *a.nonfinite = 1;
     }
   }
-  // the last CTA to finish finalizes (nothing waits on another CTA)
+  // the last column to finish finalizes (nothing waits on another CTA)
   __syncthreads();
   if (tid == 0) {
     __threadfence();
     const unsigned t = atomicAdd(a.ticket, 1u);
-    last_s = (t == gridDim.x - 1) ? 1 : 0;
+    last_s = (t == (unsigned)(a.nk * a.nb) - 1) ? 1 : 0;
   }
   __syncthreads();
   if (last_s && warp == 0) {
     __threadfence();
-    small_finalize(a);
+    small_finalize(a, rho_s, vh_s, N);
     if (lane == 0) *a.ticket = 0u;
   }
 }
 
 template <int N>
 static cudaError_t small_impl(const SmallStageArgs& a, cudaStream_t s) {
-  const int ncols = a.nk * a.nb;
-  k_small_stage<N><<<ncols, kSmallThreads, SmallLayout<N>::bytes, s>>>(a);
+  const int grid = a.nk * a.nb * a.P;
+  k_small_stage<N><<<grid, kSmallThreads, SmallLayout<N>::bytes, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -333,7 +349,19 @@ static cudaError_t small_configure() {
 
 bool small_stage_supported(int NG) { return NG >= 16 && NG <= 256 && (NG & (NG - 1)) == 0; }
 
+int small_pair_teams(int NG) {
+  switch (NG) {
+    case 16: return SmallLayout<16>::PAIR_TEAMS;
+    case 32: return SmallLayout<32>::PAIR_TEAMS;
+    case 64: return SmallLayout<64>::PAIR_TEAMS;
+    case 128: return SmallLayout<128>::PAIR_TEAMS;
+    case 256: return SmallLayout<256>::PAIR_TEAMS;
+    default: return 0;
+  }
+}
+
 cudaError_t launch_small_stage(int NG, const SmallStageArgs& a, cudaStream_t s) {
+  if (a.P < 1) return cudaErrorInvalidValue;
   switch (NG) {
     case 16: return small_impl<16>(a, s);
     case 32: return small_impl<32>(a, s);
