@@ -127,11 +127,13 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     // density of the stage input (reference order ig -> ik -> ib) and vH
     for (int ig = lane; ig < N; ig += 32) {
       double s = 0.0;
-      for (int ik = 0; ik < a.nk; ++ik)
-        for (int b = 0; b < a.nbocc; ++b) {
-          const double2 z = a.u[((size_t)ik * a.nb + b) * N + ig];
-          s += fma(a.occ * z.x, z.x, (a.occ * z.y) * z.y);
-        }
+      // occupied columns in (ik, ib) order; unrolled so the loads overlap
+#pragma unroll 8
+      for (int p = 0; p < M; ++p) {
+        const int ik = p / a.nbocc, b = p % a.nbocc;
+        const double2 z = a.u[((size_t)ik * a.nb + b) * N + ig];
+        s += fma(a.occ * z.x, z.x, (a.occ * z.y) * z.y);
+      }
       rho_s[ig] = s;
     }
     __syncwarp();
@@ -207,6 +209,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   const double2* cp = a.part + (size_t)c * a.P * N;
   for (int i = tid; i < N; i += kSmallThreads) {
     double2 f = __ldcg(cp + i);
+#pragma unroll 8
     for (int ch = 1; ch < a.P; ++ch) f = cadd(f, __ldcg(cp + (size_t)ch * N + i));
     F_s[i] = f;
   }
