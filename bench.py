@@ -641,9 +641,23 @@ def main():
                     help="profiling case: one ground-state SCF iteration of the workload (no timing)")
     ap.add_argument("--profile-adjoint", action="store_true",
                     help="profiling case: a 4-step adjoint on the differentiation shape (no timing)")
+    ap.add_argument("--profile-small", action="store_true",
+                    help="profiling case: 3 RK4 steps of the CPU-runnable shape through the fused stages (no timing)")
     ap.add_argument("--profile-batch", action="store_true",
                     help="profiling case: 2 batched steps of the first 32 runs of the ensemble mix (no timing)")
     args = ap.parse_args()
+    if args.profile_small:
+        from mattohf_gb300 import build, Context, RunConfig, _capi
+        build.build()
+        cfg = RunConfig(acell=10.0, NG=64, NK=8, NB=2, NBocc=2, Zeff=[2.0], alpha=[1.0], Rion=[0.5], Kion=[1])
+        with Context(cfg) as ctx:
+            ctx.Init_wf()
+            ctx.Gram_Schmidt()
+            ctx.set_option(_capi.OPT_SMALL_STAGES, 1)
+            ctx.set_option(_capi.OPT_GRAPH, 0)
+            A = np.full(3, 0.01)
+            ctx.rk4_run(A, A, 0.01)
+        return
     if args.profile_batch:
         from mattohf_gb300 import build, Batch, RunConfig
         build.build()
