@@ -209,7 +209,7 @@ struct SmallStageArgs {
   const double* Gx;
   const double* kx;
   const double2* tw;
-  double2* part;            // [ncols][P][NG] exchange partials
+  double2* part;            // [ncols][P][NG] exchange partials, then [ncols][NG] (rho, vH)
   double* colbuf;           // [ncols][4]: Ekin part, J part, Re<u|F>, Im<u|F>
   double* series_E;         // per-step observables, indexed by the step counter
   double* series_J;

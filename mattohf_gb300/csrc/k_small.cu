@@ -123,33 +123,39 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
 
   for (int i = tid; i < N; i += kSmallThreads) tw_s[i] = a.tw[i];
   __syncthreads();
+  // (rho, vH) of this stage, one copy per column: [ncols][N] after the partials
+  double2* rv_g = a.part + (size_t)a.nk * a.nb * a.P * N + (size_t)c * N;
   if (warp == kSmallWarps - 1) {
-    // density of the stage input (reference order ig -> ik -> ib) and vH
-    for (int ig = lane; ig < N; ig += 32) {
-      double s = 0.0;
-      // occupied columns in (ik, ib) order; unrolled so the loads overlap
+    if (chunk == 0) {  // the column's first CTA computes it
+      // density of the stage input (reference order ig -> ik -> ib) and vH
+      for (int ig = lane; ig < N; ig += 32) {
+        double s = 0.0;
+        // occupied columns in (ik, ib) order; unrolled so the loads overlap
 #pragma unroll 8
-      for (int p = 0; p < M; ++p) {
-        const int ik = p / a.nbocc, b = p % a.nbocc;
-        const double2 z = a.u[((size_t)ik * a.nb + b) * N + ig];
-        s += fma(a.occ * z.x, z.x, (a.occ * z.y) * z.y);
+        for (int p = 0; p < M; ++p) {
+          const int ik = p / a.nbocc, b = p % a.nbocc;
+          const double2 z = a.u[((size_t)ik * a.nb + b) * N + ig];
+          s += fma(a.occ * z.x, z.x, (a.occ * z.y) * z.y);
+        }
+        rho_s[ig] = s;
       }
-      rho_s[ig] = s;
-    }
-    __syncwarp();
-    double2 x[E];
+      __syncwarp();
+      double2 x[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) x[e] = make_double2(rho_s[TM::pos(tl, e)], 0.0);
-    fft_team<N, -1>(x, buf, tw_s, tl);
+      for (int e = 0; e < E; ++e) x[e] = make_double2(rho_s[TM::pos(tl, e)], 0.0);
+      fft_team<N, -1>(x, buf, tw_s, tl);
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const double v = a.vCG[TM::pos(tl, e)];
-      x[e] = make_double2(v * x[e].x, v * x[e].y);
-    }
-    fft_team<N, +1>(x, buf, tw_s, tl);
-    if (lane < T) {
+      for (int e = 0; e < E; ++e) {
+        const double v = a.vCG[TM::pos(tl, e)];
+        x[e] = make_double2(v * x[e].x, v * x[e].y);
+      }
+      fft_team<N, +1>(x, buf, tw_s, tl);
+      if (lane < T) {
 #pragma unroll
-      for (int e = 0; e < E; ++e) vh_s[TM::pos(tl, e)] = x[e].x / (double)N;
+        for (int e = 0; e < E; ++e) vh_s[TM::pos(tl, e)] = x[e].x / (double)N;
+      }
+      __syncwarp();
+      for (int ig = lane; ig < N; ig += 32) rv_g[ig] = make_double2(rho_s[ig], vh_s[ig]);
     }
   } else if (a.hf && (a.mode != 4 || occupied)) {
     // this CTA's exchange pairs of column c, one pair per team per round
@@ -212,6 +218,9 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
 #pragma unroll 8
     for (int ch = 1; ch < a.P; ++ch) f = cadd(f, __ldcg(cp + (size_t)ch * N + i));
     F_s[i] = f;
+    const double2 rv = __ldcg(rv_g + i);  // written by the column's first CTA
+    rho_s[i] = rv.x;
+    vh_s[i] = rv.y;
   }
   __syncthreads();
   // kinetic term, h w and the stage epilogue of column c (warp 0; its teams
