@@ -4,8 +4,9 @@
 // latency-bound, and a step of about 29 dependent launches costs more than the
 // arithmetic.  Here one launch does a whole RK4 stage (src/RT_calculation.f90:
 // 154-173).  Output column c = (k, b) is served by P CTAs (c, chunk):
-//   * every CTA's last warp recomputes the density of the stage input (F:55-71,
-//     reference order ig -> ik -> ib) and the Hartree potential (F:147-162);
+//   * the last warp of the column's first CTA computes the density of the
+//     stage input (F:55-71, reference order ig -> ik -> ib) and the Hartree
+//     potential (F:147-162) and stores them for the column's last CTA;
 //   * the other warps apply the exchange of column c against the CTA's chunk of
 //     the occupied orbitals (F:237-261, ordered pairs, no symmetry), one pair
 //     per team, and the CTA writes its partial sum;
