@@ -41,3 +41,45 @@ def test_create_rejects_bad_config_without_gpu(built_lib):
     assert built_lib.mattohf_create(ctypes.byref(c), ctypes.byref(h)) == _capi.ERR_ARG
     c.NG, c.NBocc = 64, 3                                      # NBocc > NB
     assert built_lib.mattohf_create(ctypes.byref(c), ctypes.byref(h)) == _capi.ERR_ARG
+
+
+def test_null_handles_are_rejected_without_gpu(built_lib):
+    """Every entry point checks its handle before touching the device."""
+    from mattohf_gb300 import _capi
+    D = ctypes.POINTER(ctypes.c_double)
+    x = (ctypes.c_double * 8)()
+    px = ctypes.cast(x, D)
+    assert built_lib.mattohf_destroy(None) == _capi.OK
+    assert built_lib.mattohf_last_error(None) == b"null context"
+    assert built_lib.mattohf_rk4_run(None, 1, ctypes.c_double(0.01), px, px, px, px, px) == _capi.ERR_ARG
+    assert built_lib.mattohf_hpsi(None, px, px, 1, ctypes.c_double(0.0), px) == _capi.ERR_ARG
+    assert built_lib.mattohf_set_option(None, _capi.OPT_GRAPH, 1) == _capi.ERR_ARG
+    assert built_lib.mattohf_batch_destroy(None) == _capi.OK
+    assert built_lib.mattohf_batch_set_option(None, _capi.OPT_FOCK_DF64, 1) == _capi.ERR_ARG
+    h = ctypes.c_void_p()
+    assert built_lib.mattohf_batch_create(0, None, ctypes.byref(h)) == _capi.ERR_ARG
+
+
+def test_create_validates_geometry_without_gpu(built_lib):
+    from mattohf_gb300 import _capi
+    z = (ctypes.c_double * 1)(2.0)
+    al = (ctypes.c_double * 1)(1.0)
+    R = (ctypes.c_double * 1)(0.5)
+    K = (ctypes.c_int * 1)(2)                   # species index 2 of 1
+    c = _capi.mattohf_config()
+    c.NG, c.NK, c.NB, c.NBocc, c.acell = 64, 4, 2, 2, 10.0
+    c.nspecies, c.Zeff, c.alpha = 1, ctypes.cast(z, ctypes.POINTER(ctypes.c_double)), \
+        ctypes.cast(al, ctypes.POINTER(ctypes.c_double))
+    c.nion, c.Rion, c.Kion = 1, ctypes.cast(R, ctypes.POINTER(ctypes.c_double)), \
+        ctypes.cast(K, ctypes.POINTER(ctypes.c_int))
+    h = ctypes.c_void_p()
+    assert built_lib.mattohf_create(ctypes.byref(c), ctypes.byref(h)) == _capi.ERR_ARG
+    K[0] = 1
+    c.acell = -1.0                              # non-positive cell
+    assert built_lib.mattohf_create(ctypes.byref(c), ctypes.byref(h)) == _capi.ERR_ARG
+    c.acell = 10.0
+    c.NK = 0                                    # no k-points
+    assert built_lib.mattohf_create(ctypes.byref(c), ctypes.byref(h)) == _capi.ERR_ARG
+    c.NK, c.NB, c.NBocc, c.NG = 1 << 14, 64, 64, 512   # beyond the size limit
+    assert built_lib.mattohf_create(ctypes.byref(c), ctypes.byref(h)) == _capi.ERR_ARG
+    assert not h.value
