@@ -359,3 +359,33 @@ def test_golden(case):
         assert rel(E, g["rt_Etot"]) <= TOL_RT
         assert np.max(np.abs(J - g["rt_Jtot"])) <= TOL_RT
         assert rel(ctx.get_orbitals(), g["rt_u"]) <= TOL_RT
+
+
+def test_context_usable_after_errors():
+    """Invalid calls return ERR_ARG with a message and leave the context usable; so
+    does a non-finite run once the orbitals are reset."""
+    import ctypes as C
+    from oracle import mattohf_oracle as O
+    from mattohf_gb300 import MattohfError, _capi
+    cfg, ctx, S = setup("ng32_nk4")
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    lib = ctx.lib
+    assert lib.mattohf_set_option(ctx.h, 99, 1) == _capi.ERR_ARG
+    assert b"unknown option" in lib.mattohf_last_error(ctx.h)
+    assert lib.mattohf_set_option(ctx.h, _capi.OPT_SMALL_STAGES, 5) == _capi.ERR_ARG
+    D = C.POINTER(C.c_double)
+    buf = np.zeros(8)
+    assert lib.mattohf_rk4_run(ctx.h, -1, C.c_double(0.01), buf.ctypes.data_as(D), buf.ctypes.data_as(D),
+                               None, None, None) == _capi.ERR_ARG
+    ctx.set_orbitals(u0)
+    with pytest.raises(MattohfError) as ei:
+        ctx.rk4_run(np.zeros(300), np.zeros(300), 0.5)
+    assert ei.value.status == _capi.ERR_NONFINITE
+    ctx.set_orbitals(u0)
+    A = np.array([0.01, 0.02])
+    Aave = np.array([0.005, 0.015])
+    E, J, N = ctx.rk4_run(A, Aave, 0.004)
+    S.cfg = to_oracle_config(dataclasses.replace(cfg, dt=0.004))
+    ref = O.rt_calculation(S, u0, nt=2, A=A, Aave=Aave)
+    assert rel(E, ref.Etot) <= TOL_RT
+    assert rel(ctx.get_orbitals(), ref.ubk) <= TOL_RT
