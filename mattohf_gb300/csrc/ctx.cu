@@ -571,8 +571,8 @@ int small_ctas_per_column(const mattohf_ctx* ctx) {
 // Buffers of the fused stages, sized before any capture.
 int ensure_small_buffers(mattohf_ctx* ctx) {
   ctx->small_P = small_ctas_per_column(ctx);
-  // partials [ncols][P][NG], then (rho, vH) [ncols][NG]
-  const size_t need = (size_t)ctx->NK * ctx->NB * (ctx->small_P + 1) * ctx->NG;
+  // partials [ncols][P][NG], then (rho, vH) and the kinetic term, [ncols][NG] each
+  const size_t need = (size_t)ctx->NK * ctx->NB * (ctx->small_P + 2) * ctx->NG;
   if (need > ctx->small_part_cap) {
     if (ctx->capturing) return fail(ctx, MATTOHF_ERR_STATE, "fused-stage scratch growth during capture");
     destroy_graph(ctx);  // a captured step holds the old pointer
@@ -603,6 +603,7 @@ SmallStageArgs small_base(mattohf_ctx* ctx, double dt) {
   a.tw = ctx->tw;
   a.P = ctx->small_P;
   a.part = ctx->d_small_part;
+  a.Aobs = ctx->d_A;
   a.colbuf = ctx->d_colbuf;
   a.series_E = ctx->d_sE;
   a.series_J = ctx->d_sJ;

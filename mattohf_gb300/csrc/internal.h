@@ -200,6 +200,7 @@ struct SmallStageArgs {
   int mode;                 // 0..3: RK4 stage; 4: observables of u0 only (closing pass)
   double dt;
   AField af;
+  const double* Aobs;       // A(t) samples: observables of stage 0 / mode 4 use A[it - 1]
   int nk, nb, nbocc, hf;
   int P;                    // CTAs per column
   double occ, dvcell, vcell;
@@ -209,7 +210,8 @@ struct SmallStageArgs {
   const double* Gx;
   const double* kx;
   const double2* tw;
-  double2* part;            // [ncols][P][NG] exchange partials, then [ncols][NG] (rho, vH)
+  double2* part;            // [ncols][P][NG] exchange partials, then [ncols][NG] (rho, vH),
+                            // then [ncols][NG] kinetic term T_A w
   double* colbuf;           // [ncols][4]: Ekin part, J part, Re<u|F>, Im<u|F>
   double* series_E;         // per-step observables, indexed by the step counter
   double* series_J;

@@ -10,14 +10,15 @@
 //   * the other warps apply the exchange of column c against the CTA's chunk of
 //     the occupied orbitals (F:237-261, ordered pairs, no symmetry), one pair
 //     per team, and the CTA writes its partial sum;
-//   * the last CTA of the column (per-column ticket) adds the P partials in
-//     chunk order, then does the kinetic term (F:212-234), h w and the stage's
-//     RK4 update of the column, into a buffer that is never the stage input;
-//   * the last column (global ticket) writes the observables (F:74-119,
-//     F:165-183, F:289-318): stage 3 stores Ekin and Je of each updated column,
-//     the next stage 0 (or the closing pass, mode 4) adds <u|F u> and the
-//     density scalars of its input and writes Etot, Je, Nele of the previous
-//     step.
+//   * in the column's first CTA, warp 6 does the kinetic transform of the
+//     column (F:212-234); the last CTA of the column adds the P partials in
+//     chunk order, then forms h w and the stage's RK4 update element by element
+//     into a buffer that is never the stage input;
+//   * stage 0 (or the closing pass, mode 4) also gives the observables of its
+//     input, i.e. of the previous step (F:74-119, F:165-183, F:289-318): Ekin
+//     and Je from warp 6's forward transform at the previous step's field,
+//     <u|F u> from the last CTA, and the density scalars; the last column to
+//     finish (global ticket) writes Etot, Je, Nele.
 // A ticket is an atomic counter taken after a fence; the CTA that draws the
 // last number does the follow-up work.  Nothing waits on another CTA.
 #include "fft.cuh"
@@ -38,7 +39,9 @@ template <int N>
 struct SmallLayout {
   static constexpr int PW = Team<N>::PER_WARP;
   static constexpr int NTEAM = kSmallWarps * PW;
-  static constexpr int PAIR_TEAMS = (kSmallWarps - 1) * PW;  // the last warp does the density
+  // warps 0..5 apply exchange pairs; in the column's first CTA warp 6 does the
+  // kinetic transform and warp 7 the density and Hartree potential
+  static constexpr int PAIR_TEAMS = (kSmallWarps - 2) * PW;
   // tw[N], bufs[NTEAM][N], F[N] (double2); rho[N], vh[N] (double)
   static constexpr size_t bytes = sizeof(double2) * (size_t)N * (2 + NTEAM) + sizeof(double) * 2 * (size_t)N;
 };
@@ -110,9 +113,11 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   double* rho_s = reinterpret_cast<double*>(F_s + N);
   double* vh_s = rho_s + N;
   __shared__ int last_s;
+  __shared__ double red_s[2][kSmallWarps];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tl = lane % T, team = warp * PW + lane / T;
   double2* buf = bufs + team * N;
+  const int ncols = a.nk * a.nb;
   const int c = blockIdx.x / a.P;          // output column (k, b)
   const int chunk = blockIdx.x % a.P;
   const int kr = c / a.nb, ib = c % a.nb;
@@ -120,14 +125,16 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   const int ppc = (M + a.P - 1) / a.P;     // pairs per CTA
   const int p0 = chunk * ppc, p1 = min(M, p0 + ppc);
   const bool occupied = ib < a.nbocc;
+  const bool obs = a.mode == 0 || a.mode == 4;
   const double2* wcol = a.u + (size_t)c * N;
+  // per-column results of the first CTA, after the partials
+  double2* rv_g = a.part + (size_t)ncols * a.P * N + (size_t)c * N;         // (rho, vH)
+  double2* kin_g = a.part + (size_t)ncols * (a.P + 1) * N + (size_t)c * N;  // T_A w
 
   for (int i = tid; i < N; i += kSmallThreads) tw_s[i] = a.tw[i];
   __syncthreads();
-  // (rho, vH) of this stage, one copy per column: [ncols][N] after the partials
-  double2* rv_g = a.part + (size_t)a.nk * a.nb * a.P * N + (size_t)c * N;
   if (warp == kSmallWarps - 1) {
-    if (chunk == 0) {  // the column's first CTA computes it
+    if (chunk == 0) {
       // density of the stage input (reference order ig -> ik -> ib) and vH
       for (int ig = lane; ig < N; ig += 32) {
         double s = 0.0;
@@ -157,6 +164,50 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       }
       __syncwarp();
       for (int ig = lane; ig < N; ig += 32) rv_g[ig] = make_double2(rho_s[ig], vh_s[ig]);
+    }
+  } else if (warp == kSmallWarps - 2) {
+    if (chunk == 0) {
+      // kinetic term T_A w of column c at the stage field (F:212-234) and, for
+      // stage 0 and the closing pass, Ekin and Je of the input column at the
+      // previous step's field by Parseval on the same forward transform
+      double2 x[E];
+#pragma unroll
+      for (int e = 0; e < E; ++e) x[e] = wcol[TM::pos(tl, e)];
+      fft_team<N, -1>(x, buf, tw_s, tl);
+      if (obs) {
+        const int itn = *a.it;
+        const double Ao = (itn >= 1 && a.Aobs) ? a.Aobs[itn - 1] : 0.0;
+        const double kAx = a.kx[kr] + Ao, kA2 = kAx * kAx;
+        double ek = 0.0, je = 0.0;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          const double G = a.Gx[TM::pos(tl, e)];
+          const double m2 = x[e].x * x[e].x + x[e].y * x[e].y;
+          ek += 0.5 * (G * G + 2.0 * G * kAx + kA2) * m2;
+          je += (G + a.kx[kr] + Ao) * m2;
+        }
+        ek = team_sum<T>(ek) / (double)N;
+        je = team_sum<T>(je) / (double)N;
+        if (lane == 0) {
+          a.colbuf[(size_t)c * 4] = ek;
+          a.colbuf[(size_t)c * 4 + 1] = je;
+        }
+      }
+      if (a.mode != 4) {
+        const double A = afield_value(a.af);
+        const double kAx = a.kx[kr] + A, kA2 = kAx * kAx;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          const double G = a.Gx[TM::pos(tl, e)];
+          const double m = 0.5 * (G * G + 2.0 * G * kAx + kA2);
+          x[e] = make_double2(m * x[e].x / (double)N, m * x[e].y / (double)N);
+        }
+        fft_team<N, +1>(x, buf, tw_s, tl);
+        if (lane < T) {
+#pragma unroll
+          for (int e = 0; e < E; ++e) kin_g[TM::pos(tl, e)] = x[e];
+        }
+      }
     }
   } else if (a.hf && (a.mode != 4 || occupied)) {
     // this CTA's exchange pairs of column c, one pair per team per round
@@ -207,129 +258,80 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     __threadfence();
     const unsigned t = atomicAdd(a.ticket + 1 + c, 1u);
     last_s = (t == (unsigned)a.P - 1) ? 1 : 0;
+    if (last_s) {
+      __threadfence();      // acquire: the other CTAs' partials, read below through L2
+      a.ticket[1 + c] = 0u;
+    }
   }
   __syncthreads();
   if (!last_s) return;
   // ---- the last CTA of column c: ordered sum of the P partials
-  __threadfence();
-  if (tid == 0) a.ticket[1 + c] = 0u;
   const double2* cp = a.part + (size_t)c * a.P * N;
   for (int i = tid; i < N; i += kSmallThreads) {
     double2 f = __ldcg(cp + i);
-#pragma unroll 8
+#pragma unroll 16
     for (int ch = 1; ch < a.P; ++ch) f = cadd(f, __ldcg(cp + (size_t)ch * N + i));
     F_s[i] = f;
     const double2 rv = __ldcg(rv_g + i);  // written by the column's first CTA
     rho_s[i] = rv.x;
     vh_s[i] = rv.y;
   }
-  __syncthreads();
-  // kinetic term, h w and the stage epilogue of column c (warp 0; its teams
-  // compute the same column, the first team writes)
-  if (warp == 0) {
-    const double A = afield_value(a.af);
-    const double kAx = a.kx[kr] + A;
-    const double kA2 = kAx * kAx;
-    const bool writer = lane < T;
-    double2 wv[E], x[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-      wv[e] = wcol[TM::pos(tl, e)];
-      x[e] = wv[e];
+  // h w and the stage's RK4 update, element by element over all threads (the
+  // transforms were done in the first phase), and <w|F> for the observables
+  double exr = 0.0, exi = 0.0;
+  bool bad = false;
+  for (int q = tid; q < N; q += kSmallThreads) {
+    const size_t o = (size_t)c * N + q;
+    const double2 wq = wcol[q];
+    const double2 f = F_s[q];
+    if (obs) {
+      exr += wq.x * f.x + wq.y * f.y;
+      exi += wq.x * f.y - wq.y * f.x;
     }
-    double exr = 0.0, exi = 0.0;
-    if (a.mode == 4) {
-      // closing pass: only <u|F> of the occupied columns
-#pragma unroll
-      for (int e = 0; e < E; ++e) {
-        const double2 f = F_s[TM::pos(tl, e)];
-        exr += wv[e].x * f.x + wv[e].y * f.y;
-        exi += wv[e].x * f.y - wv[e].y * f.x;
-      }
-      exr = team_sum<T>(exr);
-      exi = team_sum<T>(exi);
-      if (writer && tl == 0 && occupied) {
-        a.colbuf[(size_t)c * 4 + 2] = exr;
-        a.colbuf[(size_t)c * 4 + 3] = exi;
-      }
+    if (a.mode == 4) continue;
+    const double v = vh_s[q] + a.vion[q];
+    const double2 kin = __ldcg(kin_g + q);  // written by the column's first CTA
+    double2 h = make_double2(kin.x + v * wq.x, kin.y + v * wq.y);
+    h = cadd(h, f);
+    const double2 k = make_double2(h.y, -h.x);  // -i h
+    const double2 u0 = a.u0[o];
+    double2 nx;
+    if (a.mode < 3) {
+      const double cdt = (a.mode == 2) ? a.dt : 0.5 * a.dt;
+      nx = make_double2(u0.x + cdt * k.x, u0.y + cdt * k.y);
+      a.kbuf[a.mode][o] = k;
+      a.out[o] = nx;
     } else {
-      fft_team<N, -1>(x, buf, tw_s, tl);
-#pragma unroll
-      for (int e = 0; e < E; ++e) {
-        const double G = a.Gx[TM::pos(tl, e)];
-        const double m = 0.5 * (G * G + 2.0 * G * kAx + kA2);
-        x[e] = make_double2(m * x[e].x / (double)N, m * x[e].y / (double)N);
+      const double2 k0 = a.kbuf[0][o], k1 = a.kbuf[1][o], k2 = a.kbuf[2][o];
+      double sx = k0.x + 2.0 * k1.x, sy = k0.y + 2.0 * k1.y;
+      sx = sx + 2.0 * k2.x;
+      sy = sy + 2.0 * k2.y;
+      sx = sx + k.x;
+      sy = sy + k.y;
+      sx = sx * a.dt / 6.0;
+      sy = sy * a.dt / 6.0;
+      nx = make_double2(u0.x + sx, u0.y + sy);
+      a.u0[o] = nx;  // this element only, read just above by this thread
+    }
+    bad |= !(isfinite(nx.x) && isfinite(nx.y));
+  }
+  if (bad && a.nonfinite) *a.nonfinite = 1;
+  if (obs) {
+    exr = small_warp_sum(exr);
+    exi = small_warp_sum(exi);
+    if (lane == 0) {
+      red_s[0][warp] = exr;
+      red_s[1][warp] = exi;
+    }
+    __syncthreads();
+    if (tid == 0 && occupied) {
+      double sr = red_s[0][0], si = red_s[1][0];
+      for (int w2 = 1; w2 < kSmallWarps; ++w2) {
+        sr += red_s[0][w2];
+        si += red_s[1][w2];
       }
-      fft_team<N, +1>(x, buf, tw_s, tl);
-      bool bad = false;
-      double2 nx[E];
-#pragma unroll
-      for (int e = 0; e < E; ++e) {
-        const int q = TM::pos(tl, e);
-        const double v = vh_s[q] + a.vion[q];
-        double2 h = make_double2(x[e].x + v * wv[e].x, x[e].y + v * wv[e].y);
-        const double2 f = F_s[q];
-        if (a.mode == 0) {
-          exr += wv[e].x * f.x + wv[e].y * f.y;
-          exi += wv[e].x * f.y - wv[e].y * f.x;
-        }
-        h = cadd(h, f);
-        const double2 k = make_double2(h.y, -h.x);  // -i h
-        const size_t o = (size_t)c * N + q;
-        const double2 u0 = a.u0[o];
-        if (a.mode < 3) {
-          const double cdt = (a.mode == 2) ? a.dt : 0.5 * a.dt;
-          nx[e] = make_double2(u0.x + cdt * k.x, u0.y + cdt * k.y);
-          if (writer) {
-            a.kbuf[a.mode][o] = k;
-            a.out[o] = nx[e];
-          }
-        } else {
-          const double2 k0 = a.kbuf[0][o], k1 = a.kbuf[1][o], k2 = a.kbuf[2][o];
-          double sx = k0.x + 2.0 * k1.x, sy = k0.y + 2.0 * k1.y;
-          sx = sx + 2.0 * k2.x;
-          sy = sy + 2.0 * k2.y;
-          sx = sx + k.x;
-          sy = sy + k.y;
-          sx = sx * a.dt / 6.0;
-          sy = sy * a.dt / 6.0;
-          nx[e] = make_double2(u0.x + sx, u0.y + sy);
-        }
-        bad |= !(isfinite(nx[e].x) && isfinite(nx[e].y));
-      }
-      if (a.mode == 3) {
-        // the update goes in place only after every lane has read its u0
-        __syncwarp();
-        if (writer) {
-#pragma unroll
-          for (int e = 0; e < E; ++e) a.u0[(size_t)c * N + TM::pos(tl, e)] = nx[e];
-        }
-        // Ekin and Je of the updated column at this stage's field (Parseval)
-        fft_team<N, -1>(nx, buf, tw_s, tl);
-        double ek = 0.0, je = 0.0;
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-          const double G = a.Gx[TM::pos(tl, e)];
-          const double m2 = nx[e].x * nx[e].x + nx[e].y * nx[e].y;
-          ek += 0.5 * (G * G + 2.0 * G * kAx + kA2) * m2;
-          je += (G + a.kx[kr] + A) * m2;
-        }
-        ek = team_sum<T>(ek) / (double)N;
-        je = team_sum<T>(je) / (double)N;
-        if (writer && tl == 0) {
-          a.colbuf[(size_t)c * 4] = ek;
-          a.colbuf[(size_t)c * 4 + 1] = je;
-        }
-      }
-      if (a.mode == 0) {
-        exr = team_sum<T>(exr);
-        exi = team_sum<T>(exi);
-        if (writer && tl == 0 && occupied) {
-          a.colbuf[(size_t)c * 4 + 2] = exr;
-          a.colbuf[(size_t)c * 4 + 3] = exi;
-        }
-      }
-      if (bad && writer && a.nonfinite) *a.nonfinite = 1;
+      a.colbuf[(size_t)c * 4 + 2] = sr;
+      a.colbuf[(size_t)c * 4 + 3] = si;
     }
   }
   // the last column to finish finalizes (nothing waits on another CTA)
@@ -337,7 +339,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   if (tid == 0) {
     __threadfence();
     const unsigned t = atomicAdd(a.ticket, 1u);
-    last_s = (t == (unsigned)(a.nk * a.nb) - 1) ? 1 : 0;
+    last_s = (t == (unsigned)ncols - 1) ? 1 : 0;
   }
   __syncthreads();
   if (last_s && warp == 0) {
