@@ -558,13 +558,17 @@ bool use_small(const mattohf_ctx* ctx) {
   return ctx->NK * ctx->NB <= 64 && M * M * ctx->NG <= ((size_t)1 << 15);
 }
 
-// CTAs per column: enough to fill about two CTAs per multiprocessor, and at
-// least enough that every CTA's pairs fit one round of its pair teams.
+// CTAs per column.  A warp's teams run their pairs in the same instructions,
+// and a lone warp's FP64 work is bound by its SM sub-partition: so each CTA
+// takes as many pairs as the teams of two warps (on two sub-partitions) hold,
+// unless that needs more CTAs than there are multiprocessors.
 int small_ctas_per_column(const mattohf_ctx* ctx) {
   const int ncols = ctx->NK * ctx->NB, M = ctx->NK * ctx->NBocc;
-  const int pt = small_pair_teams(ctx->NG);
-  int P = std::min(M, std::max(1, 2 * ctx->nsm / ncols));
-  P = std::max(P, (M + pt - 1) / pt);
+  const int pair_teams = small_pair_teams(ctx->NG);   // 6 warps' teams
+  const int two_warps = std::max(1, pair_teams / 3);
+  int P = (M + two_warps - 1) / two_warps;
+  if (ncols * P > ctx->nsm) P = std::max(1, ctx->nsm / ncols);
+  P = std::max(P, (M + pair_teams - 1) / pair_teams);  // one round of all pair teams at most
   return std::max(1, std::min(P, M));
 }
 
