@@ -622,12 +622,14 @@ SmallStageArgs small_base(mattohf_ctx* ctx, double dt) {
 // One RK4 step as four fused stage launches.  Stage inputs and outputs
 // alternate between d_us and d_hpre so that no launch writes its own input.
 // Stage 0 also writes the observables of the previous step (its input).
-int enq_small_step(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt) {
+// With `store`, each stage input also goes to the adjoint's stage store.
+int enq_small_step(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt, bool store = false) {
   SmallStageArgs a = small_base(ctx, dt);
   const double2* in[4] = {ctx->d_u, ctx->d_us, ctx->d_hpre, ctx->d_us};
   double2* out[4] = {ctx->d_us, ctx->d_hpre, ctx->d_us, nullptr};
   const AField fs[4] = {f_m, f_ave, f_ave, f_cur};
   for (int s = 0; s < 4; ++s) {
+    if (store) CKR(launch_store_stage(ctx, in[s], s));
     a.u = in[s];
     a.out = out[s];
     a.mode = s;
@@ -1548,6 +1550,7 @@ namespace {
 // Recompute one forward step from d_u, storing its four stage inputs in the
 // segment store at slot (it - seg0)*4 + s.
 int enq_recompute_step(mattohf_ctx* ctx, AField fm, AField fave, AField fcur, double dt) {
+  if (use_small(ctx)) return enq_small_step(ctx, fm, fave, fcur, dt, true);  // advances the counter itself
   CKR(enq_rk4(ctx, fm, fave, fcur, dt, nullptr, true));
   CK(launch_counter_add(ctx->d_int, 1, ctx->st));
   return MATTOHF_OK;
@@ -1757,9 +1760,13 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   };
   // stage-store base step: the store slot of step it is (it - seg0)
   CK(cudaMemsetAsync(ctx->d_adj_int, 0, 4 * sizeof(int), ctx->st));
+  // small problems run their forward steps through the fused stages
+  if (use_small(ctx)) CKR(ensure_small_buffers(ctx));
+  CK(cudaMemsetAsync(ctx->d_ticket, 0, sizeof(unsigned) * (1 + (size_t)NK * NB), ctx->st));
   int rc = capture(ctx, &gfwd, [&]() {
     if (store_all) return enq_recompute_step(ctx, fm, fave, fcur, dt);
     CK(launch_checkpoint(ctx->d_ckpt, ctx->d_u, ctx->d_int, C, elems, ctx->st));
+    if (use_small(ctx)) return enq_small_step(ctx, fm, fave, fcur, dt);
     CKR(enq_rk4(ctx, fm, fave, fcur, dt, nullptr));
     CK(launch_counter_add(ctx->d_int, 1, ctx->st));
     return MATTOHF_OK;
