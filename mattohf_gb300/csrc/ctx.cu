@@ -276,6 +276,16 @@ int ensure_sym(mattohf_ctx* ctx, size_t need) {
   return MATTOHF_OK;
 }
 
+// A CUDA event destroyed on every exit path of the function that made it.
+struct ScopedEvent {
+  cudaEvent_t e = nullptr;
+  cudaError_t create() { return cudaEventCreate(&e); }
+  ~ScopedEvent() {
+    if (e) cudaEventDestroy(e);
+  }
+  operator cudaEvent_t() const { return e; }
+};
+
 int timed_begin(mattohf_ctx* ctx) {
   if (!(ctx->opt_timing && !ctx->capturing)) return MATTOHF_OK;
   if (ctx->fock_event_used == ctx->fock_events.size()) {
@@ -1258,9 +1268,9 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
       ctx->step_events.push_back(ev);
     }
   }
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  ScopedEvent e0, e1;
+  CK(e0.create());
+  CK(e1.create());
   CK(cudaEventRecord(e0, ctx->st));
   int flag = 0;
   int bad_at = -1;
@@ -1323,8 +1333,6 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
     sum += f;
     ms = (float)sum;
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   ctx->last_run_ms = ms;
   ctx->last_fock_ms = 0;
   ctx->last_fock_launches = (int)ctx->fock_event_used;
@@ -1736,10 +1744,10 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   fave.mode = AAVE;
   fcur.mode = ACUR;
 
-  cudaEvent_t e0, e1, e2;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
-  CK(cudaEventCreate(&e2));
+  ScopedEvent e0, e1, e2;
+  CK(e0.create());
+  CK(e1.create());
+  CK(e2.create());
   CK(cudaEventRecord(e0, ctx->st));
   // ---- objective at t = 0 and the forward pass with checkpoints
   double o0[8];
@@ -1749,15 +1757,15 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   CK(cudaMemcpyAsync(rho0.data(), ctx->d_rho, sizeof(double) * NG, cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaMemcpyAsync(ctx->d_u0, ctx->d_u, sizeof(double2) * elems, cudaMemcpyDeviceToDevice, ctx->st));
   CK(cudaMemsetAsync(ctx->d_int, 0, 2 * sizeof(int), ctx->st));
-  cudaGraphExec_t gfwd = nullptr, grec = nullptr, gadj = nullptr;
-  auto cleanup = [&]() {
-    if (gfwd) cudaGraphExecDestroy(gfwd);
-    if (grec) cudaGraphExecDestroy(grec);
-    if (gadj) cudaGraphExecDestroy(gadj);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaEventDestroy(e2);
-  };
+  // the three step graphs, destroyed on every exit path
+  struct Execs {
+    cudaGraphExec_t g[3] = {nullptr, nullptr, nullptr};
+    ~Execs() {
+      for (auto x : g)
+        if (x) cudaGraphExecDestroy(x);
+    }
+  } ex;
+  cudaGraphExec_t &gfwd = ex.g[0], &grec = ex.g[1], &gadj = ex.g[2];
   // stage-store base step: the store slot of step it is (it - seg0)
   CK(cudaMemsetAsync(ctx->d_adj_int, 0, 4 * sizeof(int), ctx->st));
   // small problems run their forward steps through the fused stages
@@ -1774,10 +1782,7 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   if (rc == MATTOHF_OK && !store_all)
     rc = capture(ctx, &grec, [&]() { return enq_recompute_step(ctx, fm, fave, fcur, dt); });
   if (rc == MATTOHF_OK) rc = capture(ctx, &gadj, [&]() { return enq_adjoint_step(ctx, dt, elems); });
-  if (rc != MATTOHF_OK) {
-    cleanup();
-    return rc;
-  }
+  if (rc != MATTOHF_OK) return rc;
   for (int it = 0; it < nt; ++it) CK(cudaGraphLaunch(gfwd, ctx->st));
   CK(cudaEventRecord(e1, ctx->st));
   // ---- objective at t = T and its gradient
@@ -1825,7 +1830,6 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   cudaEventElapsedTime(&tot_ms, e0, e2);
   ctx->last_adj_fwd_ms = fwd_ms;
   ctx->last_adj_ms = tot_ms;
-  cleanup();
   // ---- chain rule: stage fields (2 Aave - A, Aave, Aave, A) -> samples A[n]
   std::vector<double> gA(nt, 0.0), gAave(nt, 0.0);
   for (int i = 0; i < nt; ++i) {
@@ -2254,9 +2258,9 @@ int mattohf_batch_rk4_run(mattohf_batch* b, int nt, const double* dt, const doub
     BCK(cudaMemcpyAsync(c->d_Aave, Aave + (size_t)r * nt, sizeof(double) * nt, cudaMemcpyHostToDevice, b->st));
   }
   BCK(cudaMemsetAsync(b->d_int, 0, 2 * sizeof(int), b->st));
-  cudaEvent_t e0, e1;
-  BCK(cudaEventCreate(&e0));
-  BCK(cudaEventCreate(&e1));
+  ScopedEvent e0, e1;
+  BCK(e0.create());
+  BCK(e1.create());
   BCK(cudaEventRecord(e0, b->st));
   int flag = 0, bad_at = -1;
   for (int it = 0; it < nt; ++it) {
@@ -2280,8 +2284,6 @@ int mattohf_batch_rk4_run(mattohf_batch* b, int nt, const double* dt, const doub
   BCK(cudaEventSynchronize(e1));
   float ms = 0;
   BCK(cudaEventElapsedTime(&ms, e0, e1));
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   b->last_ms = ms;
   const int ndone = bad_at >= 0 ? bad_at + 1 : nt;
   for (int r = 0; r < b->R; ++r) {
