@@ -693,10 +693,12 @@ int compute_tables(mattohf_ctx* ctx) {
   for (int g = 0; g < NG; ++g) q[(size_t)nd * NG + g] = ctx->Gx[g];
   double* d_q = nullptr;
   double* d_all = nullptr;
+  double* d_g = nullptr;
   CKR(dalloc(ctx, &d_q, q.size()));
   CKR(dalloc(ctx, &d_all, q.size()));
+  CKR(dalloc(ctx, &d_g, (size_t)vck_points(ctx->acell, NG, NK)));
   CK(cudaMemcpyAsync(d_q, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-  CK(launch_vck_table(NG, NK, ctx->acell, d_q, (int)q.size(), d_all, ctx->st));
+  CK(launch_vck_table(NG, NK, ctx->acell, d_q, (int)q.size(), d_g, d_all, ctx->st));
   CKR(dalloc(ctx, &ctx->d_vcq, (size_t)nd * NG));
   CKR(dalloc(ctx, &ctx->d_vCG, NG));
   CKR(dalloc(ctx, &ctx->d_kern, (size_t)nd * NG));
@@ -708,6 +710,7 @@ int compute_tables(mattohf_ctx* ctx) {
   CK(cudaStreamSynchronize(ctx->st));
   cudaFree(d_q);
   cudaFree(d_all);
+  cudaFree(d_g);
   return MATTOHF_OK;
 }
 
@@ -958,10 +961,11 @@ int mattohf_vck(mattohf_ctx* ctx, const double* q, int n, double* out) {
   if (n < 0 || (n > 0 && (!q || !out))) return fail(ctx, MATTOHF_ERR_ARG, "bad vck arguments");
   if (n == 0) return MATTOHF_OK;
   double* d = nullptr;
-  CKR(dalloc(ctx, &d, 2 * (size_t)n));
+  const size_t ng = (size_t)vck_points(ctx->acell, ctx->NG, ctx->NK);
+  CKR(dalloc(ctx, &d, 2 * (size_t)n + ng));
   int rc = MATTOHF_OK;
   if (cudaMemcpyAsync(d, q, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->st) != cudaSuccess ||
-      launch_vck_table(ctx->NG, ctx->NK, ctx->acell, d, n, d + n, ctx->st) != cudaSuccess ||
+      launch_vck_table(ctx->NG, ctx->NK, ctx->acell, d, n, d + 2 * (size_t)n, d + n, ctx->st) != cudaSuccess ||
       cudaMemcpyAsync(out, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->st) != cudaSuccess ||
       cudaStreamSynchronize(ctx->st) != cudaSuccess)
     rc = fail(ctx, MATTOHF_ERR_CUDA, "k_vCk evaluation failed");

@@ -331,7 +331,9 @@ cudaError_t launch_te_update(double2* w, const double2* h0, const double2* h1, d
 cudaError_t launch_half_sum(double2* out, const double2* a, const double2* b, size_t n, cudaStream_t s);
 
 // Tables (k_table.cu)
-cudaError_t launch_vck_table(int NG, int NK, double acell, const double* d_q, int nq,
+// k_vCk (F:33-52) at nq arguments; d_g: scratch of vck_points(acell, NG, NK) doubles
+long long vck_points(double acell, int NG, int NK);
+cudaError_t launch_vck_table(int NG, int NK, double acell, const double* d_q, int nq, double* d_g,
                              double* d_out, cudaStream_t s);
 cudaError_t launch_make_kern(int NG, int NK, const double* vcq, double* kern, cudaStream_t s);
 

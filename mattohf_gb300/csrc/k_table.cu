@@ -3,33 +3,49 @@
 //
 // vCk(k) = 2*dx*sum_{ix=0}^{n-1} 0.5*(f(ix*dx) + f((ix+1)*dx)),
 // f(x) = cos(k*x)/sqrt(x*x + 1), dx = acell/NG/20, n = trip count of
-// `Do While (ix*dx < NK*acell)`.  One CTA per k value; each thread walks a
-// contiguous ix range in order (reusing f at the shared end point), then the
-// CTA reduces the per-thread sums in a fixed tree order.  cos/sqrt are CUDA's
-// library functions.
+// `Do While (ix*dx < NK*acell)`.  The trapezoid sum is the same as
+// 0.5 f_0 + f_1 + ... + f_{n-1} + 0.5 f_n.  g(x) = 1/sqrt(x*x + 1) does not
+// depend on k and is tabulated once (k_vck_g).  One CTA per k value; thread t
+// takes the points t, t + 256, t + 512, ... and advances cos(k x) and sin(k x)
+// between them by a rotation through the angle 256 k dx (angle addition),
+// recomputing both from x with sincos every kReseed points so that the
+// recurrence's rounding never builds up over more than kReseed steps.  The
+// CTA then reduces the per-thread sums in a fixed tree order.
 #include "internal.h"
 
 namespace mattohf {
 
 constexpr int kTableThreads = 256;
+constexpr int kReseed = 32;
+
+__global__ void k_vck_g(double dx, long long n, double* __restrict__ g) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  const double x = (double)i * dx;
+  g[i] = 1.0 / sqrt(x * x + 1.0);
+}
 
 __global__ void __launch_bounds__(kTableThreads) k_vck(const double* __restrict__ q, double dx,
-                                                       long long n, double* __restrict__ out) {
+                                                       long long n, const double* __restrict__ g,
+                                                       double* __restrict__ out) {
   __shared__ double red[kTableThreads];
   const double k = q[blockIdx.x];
-  const long long per = (n + kTableThreads - 1) / kTableThreads;
-  const long long i0 = (long long)threadIdx.x * per;
-  const long long i1 = min(n, i0 + per);
-  double s = 0.0;
-  if (i0 < i1) {
-    double x = (double)i0 * dx;
-    double f0 = cos(k * x) / sqrt(x * x + 1.0);
-    for (long long i = i0; i < i1; ++i) {
-      const double x1 = (double)(i + 1) * dx;
-      const double f1 = cos(k * x1) / sqrt(x1 * x1 + 1.0);
-      s += 0.5 * (f0 + f1);
-      f0 = f1;
+  double wc, ws;  // rotation by kTableThreads points
+  sincos(k * ((double)kTableThreads * dx), &ws, &wc);
+  double s = 0.0, c = 0.0, sn = 0.0;
+  int since = kReseed;
+  for (long long i = threadIdx.x; n > 0 && i <= n; i += kTableThreads) {
+    if (since == kReseed) {
+      sincos(k * ((double)i * dx), &sn, &c);
+      since = 0;
+    } else {
+      const double c2 = fma(c, wc, -(sn * ws));
+      sn = fma(sn, wc, c * ws);
+      c = c2;
     }
+    ++since;
+    const double f = c * g[i];
+    s += (i == 0 || i == n) ? 0.5 * f : f;
   }
   red[threadIdx.x] = s;
   __syncthreads();
@@ -59,12 +75,20 @@ static long long vck_count(double acell, int NG, int NK, double* dx_out) {
   return n;
 }
 
-cudaError_t launch_vck_table(int NG, int NK, double acell, const double* d_q, int nq,
+long long vck_points(double acell, int NG, int NK) {
+  double dx;
+  return vck_count(acell, NG, NK, &dx) + 1;
+}
+
+cudaError_t launch_vck_table(int NG, int NK, double acell, const double* d_q, int nq, double* d_g,
                              double* d_out, cudaStream_t s) {
   double dx;
   const long long n = vck_count(acell, NG, NK, &dx);
   if (nq <= 0) return cudaSuccess;
-  k_vck<<<nq, kTableThreads, 0, s>>>(d_q, dx, n, d_out);
+  k_vck_g<<<(unsigned)((n + 1 + 255) / 256), 256, 0, s>>>(dx, n, d_g);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_vck<<<nq, kTableThreads, 0, s>>>(d_q, dx, n, d_g, d_out);
   return cudaGetLastError();
 }
 
