@@ -3,7 +3,7 @@
 The reference ships no golden vectors and cannot be built here, so these
 fixtures are the oracle's own outputs on small seeded inputs (``parity
 unpinned``: they pin the CUDA path to the oracle and the oracle to itself
-across changes; the oracle is pinned to physics by tests/test_oracle_physics.py).
+across changes; the oracle is pinned to physics by tests/test_oracle.py).
 
 Run:  python tests/golden/make_golden.py
 """
@@ -57,7 +57,35 @@ def run_case(name, kw):
         json.dump(dataclasses.asdict(cfg), fh, indent=1, sort_keys=True)
 
 
+# long real-time runs: error accumulation over hundreds of steps
+LONG_CASES = {
+    # the CPU-runnable configuration's shape, pulse and step count, at a stable dt
+    "rt2000_ng64_nk8": dict(acell=10.0, NG=64, NK=8, NB=2, NBocc=2, Zeff=[2.0], alpha=[1.0],
+                           Rion=[0.5], Kion=[1], dt=0.01, NT=2000,
+                           field_option="LP", omegac=0.057 * O.HARTREE, Tpulse=100 * O.ATOMTIME,
+                           E0=0.05 * 0.057 * O.ATOMFIELD, nenvelope=2,
+                           phiCEP=0.057 * 100 / (4 * O.PI) % 1.0),
+}
+
+
+def run_long(name, kw):
+    cfg = O.Config(**kw)
+    S = O.make_system(cfg)
+    u = O.gram_schmidt(S, O.init_wf(S))
+    rt = O.rt_calculation(S, u, nt=cfg.NT)
+    out = dict(u0=u, rt_A=rt.A, rt_Etot=rt.Etot, rt_Jtot=rt.Jtot, rt_Nele=rt.Nele, rt_u=rt.ubk)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    with open(os.path.join(HERE, f"{name}.json"), "w") as fh:
+        json.dump(dataclasses.asdict(cfg), fh, indent=1, sort_keys=True)
+
+
 if __name__ == "__main__":
+    only = sys.argv[1:]
     for n, kw in CASES.items():
-        run_case(n, kw)
-        print("wrote", n)
+        if not only or n in only:
+            run_case(n, kw)
+            print("wrote", n)
+    for n, kw in LONG_CASES.items():
+        if not only or n in only:
+            run_long(n, kw)
+            print("wrote", n)

@@ -389,3 +389,25 @@ def test_context_usable_after_errors():
     ref = O.rt_calculation(S, u0, nt=2, A=A, Aave=Aave)
     assert rel(E, ref.Etot) <= TOL_RT
     assert rel(ctx.get_orbitals(), ref.ubk) <= TOL_RT
+
+
+@pytest.mark.parametrize("small", [0, 1])
+def test_long_golden_run(small):
+    """The full 2000-step run of the CPU-runnable shape (stable dt) against the oracle's
+    committed series, through the tiled path and through the fused stages: relative
+    errors of Etot, Je, Nele and the final orbitals stay within the 1e-10 bound."""
+    from mattohf_gb300 import Context, RunConfig, aave_from_samples, _capi
+    g = np.load(os.path.join(GOLD, "rt2000_ng64_nk8.npz"))
+    with open(os.path.join(GOLD, "rt2000_ng64_nk8.json")) as fh:
+        d = json.load(fh)
+    cfg = RunConfig(**{f.name: d[f.name] for f in dataclasses.fields(RunConfig)})
+    A = g["rt_A"]
+    with Context(cfg) as ctx:
+        ctx.set_option(_capi.OPT_SMALL_STAGES, small)
+        ctx.set_orbitals(g["u0"])
+        E, J, N = ctx.rk4_run(A, aave_from_samples(A), cfg.dt)
+        u = ctx.get_orbitals()
+    assert rel(E, g["rt_Etot"]) <= TOL_RT
+    assert np.max(np.abs(J - g["rt_Jtot"])) <= TOL_RT * max(1.0, np.max(np.abs(g["rt_Jtot"])))
+    assert rel(N, g["rt_Nele"]) <= TOL_RT
+    assert rel(u, g["rt_u"]) <= TOL_RT

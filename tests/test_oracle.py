@@ -205,3 +205,34 @@ def test_oracle_adjoint_matches_finite_differences(objective):
         S.vion = vp
         fd = (Lp - Lm) / (2 * h)
         assert abs(gv[x] - fd) <= 1e-5 * np.max(np.abs(gv)) + 1e-9  # FD round-off ~ 1e-16*|E|/h
+
+
+def test_c_port_matches_long_golden_run():
+    """The C restatement over the full 2000-step run of the CPU-runnable shape
+    reproduces the oracle's committed series (tests/golden/rt2000_ng64_nk8)."""
+    import json
+    import os
+    import ctypes as C
+    from oracle import build_cref
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    g = np.load(os.path.join(here, "rt2000_ng64_nk8.npz"))
+    with open(os.path.join(here, "rt2000_ng64_nk8.json")) as fh:
+        cfg = O.Config(**json.load(fh))
+    S = O.make_system(cfg)
+    lib = build_cref.load()
+    D = C.POINTER(C.c_double)
+    h = lib.cref_create(cfg.NG, cfg.NK, cfg.NB, cfg.NBocc, cfg.acell, 1, S.vion.ctypes.data_as(D), None, None)
+    try:
+        A = np.ascontiguousarray(g["rt_A"])
+        Aave = np.concatenate([[0.5 * A[0]], 0.5 * (A[1:] + A[:-1])])
+        u = np.ascontiguousarray(g["u0"]).copy()
+        nt = A.size
+        E, J, N = np.empty(nt), np.empty(nt), np.empty(nt)
+        lib.cref_rk4_run(h, u.view(np.float64).ctypes.data_as(D), nt, C.c_double(cfg.dt), A.ctypes.data_as(D),
+                         Aave.ctypes.data_as(D), E.ctypes.data_as(D), J.ctypes.data_as(D), N.ctypes.data_as(D))
+    finally:
+        lib.cref_destroy(h)
+    assert np.max(np.abs(E - g["rt_Etot"])) <= 1e-10 * np.max(np.abs(g["rt_Etot"]))
+    assert np.max(np.abs(J - g["rt_Jtot"])) <= 1e-10 * max(1.0, np.max(np.abs(g["rt_Jtot"])))
+    assert np.max(np.abs(N - g["rt_Nele"])) <= 1e-10 * np.max(np.abs(g["rt_Nele"]))
+    assert np.max(np.abs(u - g["rt_u"])) <= 1e-10 * np.max(np.abs(g["rt_u"]))
