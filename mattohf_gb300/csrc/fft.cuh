@@ -14,9 +14,11 @@
 // exp(+2*pi*i*n*k/N), both unnormalised.
 //
 // The FP64 pipe bounds this code on GB300, so the butterflies are written to
-// minimise DADD/DMUL/DFMA count (radix-8/4 with FMA-folded sqrt(1/2) terms,
-// first-pass twiddles skipped); index arithmetic and shared-memory traffic are
-// off the critical pipe.
+// minimise DADD/DMUL/DFMA count: radix-8/4 with FMA-folded sqrt(1/2) terms,
+// first-pass twiddles skipped, and every multiplication in front of a
+// butterfly (twiddles, a G-space kernel, a pair product) folded into its first
+// level with FMA.  Index arithmetic and shared-memory traffic are off the
+// critical pipe.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -31,6 +33,20 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 w) {
 // a * conj(b)
 __device__ __forceinline__ double2 cmulc(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, a.y * b.y), fma(a.y, b.x, -(a.x * b.y)));
+}
+// a + b * w, accumulated into a (4 FMA)
+__device__ __forceinline__ double2 cmadd(double2 b, double2 w, double2 a) {
+  return make_double2(fma(-b.y, w.y, fma(b.x, w.x, a.x)), fma(b.y, w.x, fma(b.x, w.y, a.y)));
+}
+// a + b * conj(c), accumulated into a (4 FMA)
+__device__ __forceinline__ double2 cmaddc(double2 b, double2 c, double2 a) {
+  return make_double2(fma(b.y, c.y, fma(b.x, c.x, a.x)), fma(-b.x, c.y, fma(b.y, c.x, a.y)));
+}
+// 2a - s.  For s = a + t this is the partner output a - t of a butterfly, in
+// 2 FMA instead of the 4 that recomputing a - t from a and t's factors costs.
+// The extra rounding is that of s, the size of the butterfly's own rounding.
+__device__ __forceinline__ double2 cmirror(double2 a, double2 s) {
+  return make_double2(fma(2.0, a.x, -s.x), fma(2.0, a.y, -s.y));
 }
 // acc += a * b
 __device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 acc) {
@@ -48,43 +64,87 @@ __device__ __forceinline__ double2 rot4(double2 a) {
   return DIR < 0 ? make_double2(a.y, -a.x) : make_double2(-a.y, a.x);
 }
 
+// Inputs of a butterfly's first level.  pair(i, j, s, d) forms s = X_i + X_j
+// and d = X_i - X_j, where X is what the butterfly transforms: a register
+// slot as is, or a slot times a twiddle, a real scale or a conjugate product.
+// Folding that multiplication into the sum with FMA and taking the difference
+// as 2*first - s saves 2 FP64 instructions per slot pair over multiplying
+// first.  Slot indices are compile-time constants after unrolling.
+struct InPlain {
+  const double2* x;
+  __device__ __forceinline__ void pair(int i, int j, double2& s, double2& d) const {
+    s = cadd(x[i], x[j]);
+    d = csub(x[i], x[j]);
+  }
+};
+
+// X_r = x_r * w_r with w_0 = 1 (Stockham passes after the first)
+struct InTwiddled {
+  const double2* x;
+  const double2* w;
+  __device__ __forceinline__ void pair(int i, int j, double2& s, double2& d) const {
+    const double2 t = (i == 0) ? x[0] : cmul(x[i], w[i]);
+    s = cmadd(x[j], w[j], t);
+    d = cmirror(t, s);
+  }
+};
+
+// X_e = f[pos(e)] * x_e for a real per-point factor f (a kernel in G space)
+template <int N>
+struct InScaled;
+
+// X_e = a[pos(e)] * conj(b[pos(e)]) for two columns read from memory (pair densities)
+template <int N>
+struct InConjProduct;
+
 template <int R, int DIR> struct Dft;
 
 template <int DIR> struct Dft<2, DIR> {
-  __device__ __forceinline__ static void run(double2* x) {
-    double2 a = x[0], b = x[1];
-    x[0] = cadd(a, b);
-    x[1] = csub(a, b);
+  template <class In>
+  __device__ __forceinline__ static void run_from(const In& in, int b, double2* y) {
+    double2 s, d;
+    in.pair(b, b + 1, s, d);
+    y[0] = s;
+    y[1] = d;
   }
+  __device__ __forceinline__ static void run(double2* x) { run_from(InPlain{x}, 0, x); }
 };
 
 template <int DIR> struct Dft<4, DIR> {
-  __device__ __forceinline__ static void run(double2* x) {
-    double2 e0 = cadd(x[0], x[2]), e1 = csub(x[0], x[2]);
-    double2 e2 = cadd(x[1], x[3]), e3 = rot4<DIR>(csub(x[1], x[3]));
-    x[0] = cadd(e0, e2);
-    x[2] = csub(e0, e2);
-    x[1] = cadd(e1, e3);
-    x[3] = csub(e1, e3);
+  template <class In>
+  __device__ __forceinline__ static void run_from(const In& in, int b, double2* y) {
+    double2 e0, e1, e2, e3;
+    in.pair(b + 0, b + 2, e0, e1);
+    in.pair(b + 1, b + 3, e2, e3);
+    e3 = rot4<DIR>(e3);
+    y[0] = cadd(e0, e2);
+    y[2] = csub(e0, e2);
+    y[1] = cadd(e1, e3);
+    y[3] = csub(e1, e3);
   }
+  __device__ __forceinline__ static void run(double2* x) { run_from(InPlain{x}, 0, x); }
 };
 
 template <int DIR> struct Dft<8, DIR> {
-  __device__ __forceinline__ static void run(double2* x) {
+  template <class In>
+  __device__ __forceinline__ static void run_from(const In& in, int b, double2* y) {
     constexpr double c = 0.70710678118654752440084436210485;
     // even / odd halves as two 4-point DFTs
-    double2 a0 = cadd(x[0], x[4]), a1 = csub(x[0], x[4]);
-    double2 a2 = cadd(x[2], x[6]), a3 = rot4<DIR>(csub(x[2], x[6]));
-    double2 a4 = cadd(x[1], x[5]), a5 = csub(x[1], x[5]);
-    double2 a6 = cadd(x[3], x[7]), a7 = rot4<DIR>(csub(x[3], x[7]));
+    double2 a0, a1, a2, a3, a4, a5, a6, a7;
+    in.pair(b + 0, b + 4, a0, a1);
+    in.pair(b + 2, b + 6, a2, a3);
+    in.pair(b + 1, b + 5, a4, a5);
+    in.pair(b + 3, b + 7, a6, a7);
+    a3 = rot4<DIR>(a3);
+    a7 = rot4<DIR>(a7);
     double2 b0 = cadd(a0, a2), b2 = csub(a0, a2);
     double2 b1 = cadd(a1, a3), b3 = csub(a1, a3);
     double2 b4 = cadd(a4, a6), b6 = rot4<DIR>(csub(a4, a6));
     double2 b5 = cadd(a5, a7), b7 = csub(a5, a7);
-    x[0] = cadd(b0, b4);
-    x[4] = csub(b0, b4);
-    x[2] = cadd(b2, b6);
-    x[6] = csub(b2, b6);
+    y[0] = cadd(b0, b4);
+    y[4] = csub(b0, b4);
+    y[2] = cadd(b2, b6);
+    y[6] = csub(b2, b6);
     // b5 * W8^1 and b7 * W8^3, folded into the final butterflies with FMA
     double s5, t5, s7, t7;
     if (DIR < 0) {            // W8 = (1-i)/sqrt2, W8^3 = (-1-i)/sqrt2
@@ -94,11 +154,12 @@ template <int DIR> struct Dft<8, DIR> {
       s5 = b5.x - b5.y;  t5 = b5.x + b5.y;
       s7 = -(b7.x + b7.y); t7 = b7.x - b7.y;
     }
-    x[1] = make_double2(fma(c, s5, b1.x), fma(c, t5, b1.y));
-    x[5] = make_double2(fma(-c, s5, b1.x), fma(-c, t5, b1.y));
-    x[3] = make_double2(fma(c, s7, b3.x), fma(c, t7, b3.y));
-    x[7] = make_double2(fma(-c, s7, b3.x), fma(-c, t7, b3.y));
+    y[1] = make_double2(fma(c, s5, b1.x), fma(c, t5, b1.y));
+    y[5] = make_double2(fma(-c, s5, b1.x), fma(-c, t5, b1.y));
+    y[3] = make_double2(fma(c, s7, b3.x), fma(c, t7, b3.y));
+    y[7] = make_double2(fma(-c, s7, b3.x), fma(-c, t7, b3.y));
   }
+  __device__ __forceinline__ static void run(double2* x) { run_from(InPlain{x}, 0, x); }
 };
 
 // Pass plans: radices with equal first and last radix.
@@ -124,6 +185,32 @@ template <int N> struct Team {
   __device__ __forceinline__ static int pos(int tl, int e) { return pos(tl, e / R0, e % R0); }
 };
 
+template <int N>
+struct InScaled {
+  const double2* x;
+  const double* f;  // global memory, read-only for the kernel's lifetime
+  int tl;
+  __device__ __forceinline__ void pair(int i, int j, double2& s, double2& d) const {
+    const double fi = __ldg(f + Team<N>::pos(tl, i)), fj = __ldg(f + Team<N>::pos(tl, j));
+    const double2 t = make_double2(fi * x[i].x, fi * x[i].y);
+    s = make_double2(fma(fj, x[j].x, t.x), fma(fj, x[j].y, t.y));
+    d = make_double2(fma(-fj, x[j].x, t.x), fma(-fj, x[j].y, t.y));
+  }
+};
+
+template <int N>
+struct InConjProduct {
+  const double2* a;
+  const double2* b;
+  int tl;
+  __device__ __forceinline__ void pair(int i, int j, double2& s, double2& d) const {
+    const int qi = Team<N>::pos(tl, i), qj = Team<N>::pos(tl, j);
+    const double2 t = cmulc(a[qi], b[qi]);
+    s = cmaddc(a[qj], b[qj], t);
+    d = cmirror(t, s);
+  }
+};
+
 // One Stockham pass reading and writing the team buffer.
 template <int N, int R, int NS, int DIR, int T>
 __device__ __forceinline__ void fft_mid_pass(double2* buf, const double2* __restrict__ tw, int tl) {
@@ -135,15 +222,15 @@ __device__ __forceinline__ void fft_mid_pass(double2* buf, const double2* __rest
   for (int p = 0; p < PER; ++p) {
     const int j = tl + T * p;
     const int k = j % NS;
+    double2 w[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[p][r] = buf[j + r * NBF];
 #pragma unroll
     for (int r = 1; r < R; ++r) {
-      double2 w = tw[(r * k) * (N / (NS * R))];
-      if (DIR > 0) w.y = -w.y;
-      v[p][r] = cmul(v[p][r], w);
+      w[r] = tw[(r * k) * (N / (NS * R))];
+      if (DIR > 0) w[r].y = -w[r].y;
     }
-    Dft<R, DIR>::run(v[p]);
+    Dft<R, DIR>::run_from(InTwiddled{v[p], w}, 0, v[p]);
   }
   __syncwarp();
 #pragma unroll
@@ -156,19 +243,20 @@ __device__ __forceinline__ void fft_mid_pass(double2* buf, const double2* __rest
   __syncwarp();
 }
 
-// Transform x (register slots at Team<N>::pos) in place.  buf: N double2 of
-// team-private shared memory; tw: N forward twiddles exp(-2 pi i m / N).
-template <int N, int DIR>
-__device__ __forceinline__ void fft_team(double2 (&x)[Team<N>::E], double2* buf,
-                                         const double2* __restrict__ tw, int tl) {
+// Transform the input policy's values X (register slots at Team<N>::pos) into
+// x.  buf: N double2 of team-private shared memory; tw: N forward twiddles
+// exp(-2 pi i m / N).
+template <int N, int DIR, class In>
+__device__ __forceinline__ void fft_team_in(const In& in, double2 (&x)[Team<N>::E], double2* buf,
+                                            const double2* __restrict__ tw, int tl) {
   using TM = Team<N>;
   constexpr int R0 = FftPlan<N>::R[0];
   constexpr int NP = FftPlan<N>::NP;
   constexpr int T = TM::T;
-  // first pass (NS = 1, no twiddles), from registers to the buffer
+  // first pass (NS = 1, no twiddles), from the inputs to the buffer
 #pragma unroll
   for (int p = 0; p < TM::PER; ++p) {
-    Dft<R0, DIR>::run(&x[p * R0]);
+    Dft<R0, DIR>::run_from(in, p * R0, &x[p * R0]);
   }
   __syncwarp();
 #pragma unroll
@@ -191,17 +279,24 @@ __device__ __forceinline__ void fft_team(double2 (&x)[Team<N>::E], double2* buf,
   for (int p = 0; p < TM::PER; ++p) {
     const int j = tl + T * p;
     const int k = j;  // j < NS
+    double2 w[RL];
 #pragma unroll
     for (int r = 0; r < RL; ++r) x[p * RL + r] = buf[j + r * NS];
 #pragma unroll
     for (int r = 1; r < RL; ++r) {
-      double2 w = tw[r * k];  // N/(NS*RL) == 1
-      if (DIR > 0) w.y = -w.y;
-      x[p * RL + r] = cmul(x[p * RL + r], w);
+      w[r] = tw[r * k];  // N/(NS*RL) == 1
+      if (DIR > 0) w[r].y = -w[r].y;
     }
-    Dft<RL, DIR>::run(&x[p * RL]);
+    Dft<RL, DIR>::run_from(InTwiddled{&x[p * RL], w}, 0, &x[p * RL]);
   }
   __syncwarp();
+}
+
+// Transform x (register slots at Team<N>::pos) in place.
+template <int N, int DIR>
+__device__ __forceinline__ void fft_team(double2 (&x)[Team<N>::E], double2* buf,
+                                         const double2* __restrict__ tw, int tl) {
+  fft_team_in<N, DIR>(InPlain{x}, x, buf, tw, tl);
 }
 
 // Team-wide sum of one double; team lanes are contiguous within a warp.

@@ -70,20 +70,10 @@ __global__ void __launch_bounds__(kThreads) k_fock_adj(AdjFockArgs a) {
     const double2* mB = a.mu + ob;
     double2 x[E];
     // ---- pass A: phi_ab = Phi_ab[v_a conj(v_b)]
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const int q = TM::pos(tl, e);
-      x[e] = cmulc(vA[q], vB[q]);
-    }
-    fft_team<N, -1>(x, buf, tw_s, tl);
+    fft_team_in<N, -1>(InConjProduct<N>{vA, vB, tl}, x, buf, tw_s, tl);
     double rnx = __shfl_sync(0xffffffffu, x[TM::R0 / 2].x, team_lane0);
     double rny = __shfl_sync(0xffffffffu, x[TM::R0 / 2].y, team_lane0);
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const double kv = __ldg(kab + TM::pos(tl, e));
-      x[e] = make_double2(kv * x[e].x, kv * x[e].y);
-    }
-    fft_team<N, +1>(x, buf, tw_s, tl);
+    fft_team_in<N, +1>(InScaled<N>{x, kab, tl}, x, buf, tw_s, tl);
     if (valid) {
       if (self) {
         // out_a += i conj(phi_aa) mu_a
@@ -113,12 +103,7 @@ __global__ void __launch_bounds__(kThreads) k_fock_adj(AdjFockArgs a) {
     fft_team<N, -1>(x, buf, tw_s, tl);
     rnx = __shfl_sync(0xffffffffu, x[TM::R0 / 2].x, team_lane0);
     rny = __shfl_sync(0xffffffffu, x[TM::R0 / 2].y, team_lane0);
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const double kv = __ldg(kab + TM::pos(tl, e));
-      x[e] = make_double2(kv * x[e].x, kv * x[e].y);
-    }
-    fft_team<N, +1>(x, buf, tw_s, tl);
+    fft_team_in<N, +1>(InScaled<N>{x, kab, tl}, x, buf, tw_s, tl);
     if (valid) {
       // out_a += i v_b phi'_ab
 #pragma unroll

@@ -184,18 +184,8 @@ __global__ void __launch_bounds__(kThreads) k_fock(FockArgs a) {
     const double2* ucol = a.u.p + (size_t)kc * a.u.kstride + (size_t)ibc * N;
     const double* kern = a.kern + (size_t)(kr - kc + a.nk - 1) * N;
     double2 x[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const int q = TM::pos(tl, e);
-      x[e] = cmulc(wcol[q], ucol[q]);
-    }
-    fft_team<N, -1>(x, buf, tw_s, tl);
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const double v = __ldg(kern + TM::pos(tl, e));
-      x[e] = make_double2(v * x[e].x, v * x[e].y);
-    }
-    fft_team<N, +1>(x, buf, tw_s, tl);
+    fft_team_in<N, -1>(InConjProduct<N>{wcol, ucol, tl}, x, buf, tw_s, tl);
+    fft_team_in<N, +1>(InScaled<N>{x, kern, tl}, x, buf, tw_s, tl);
     if (valid) {
 #pragma unroll
       for (int e = 0; e < E; ++e) acc[e] = cfma(x[e], ucol[TM::pos(tl, e)], acc[e]);
@@ -271,24 +261,14 @@ __device__ __forceinline__ void fock_sym_body(const FockSymArgs& a, const int ti
     const int kb = (ib < M ? ib : 0) / a.nbocc, bb = (ib < M ? ib : 0) % a.nbocc;
     const double2* ucol_b = a.u.p + (size_t)kb * a.u.kstride + (size_t)bb * N;
     double2 x[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const int q = TM::pos(tl, e);
-      x[e] = cmulc(ucol_a[q], ucol_b[q]);
-    }
-    fft_team<N, -1>(x, buf, tw_s, tl);
+    fft_team_in<N, -1>(InConjProduct<N>{ucol_a, ucol_b, tl}, x, buf, tw_s, tl);
     // Nyquist coefficient R_ab[N/2] lives in slot (p=0, r=R0/2) of the team's lane 0
     const double2 rn_own = x[TM::R0 / 2];
     const double rnx = __shfl_sync(0xffffffffu, rn_own.x, team_lane0);
     const double rny = __shfl_sync(0xffffffffu, rn_own.y, team_lane0);
     const int dab = ka - kb + a.nk - 1, dba = kb - ka + a.nk - 1;
     const double* kab = a.kern + (size_t)dab * N;
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const double v = __ldg(kab + TM::pos(tl, e));
-      x[e] = make_double2(v * x[e].x, v * x[e].y);
-    }
-    fft_team<N, +1>(x, buf, tw_s, tl);
+    fft_team_in<N, +1>(InScaled<N>{x, kab, tl}, x, buf, tw_s, tl);
     if (valid) {
 #pragma unroll
       for (int e = 0; e < E; ++e) racc[e] = cfma(x[e], ucol_b[TM::pos(tl, e)], racc[e]);

@@ -223,15 +223,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       const double2* ucol = a.u + ((size_t)kc * a.nb + bc) * N;
       const double* kern = a.kern + (size_t)(kr - kc + a.nk - 1) * N;
       double2 x[E];
-#pragma unroll
-      for (int e = 0; e < E; ++e) x[e] = cmulc(wcol[TM::pos(tl, e)], ucol[TM::pos(tl, e)]);
-      fft_team<N, -1>(x, buf, tw_s, tl);
-#pragma unroll
-      for (int e = 0; e < E; ++e) {
-        const double v = __ldg(kern + TM::pos(tl, e));
-        x[e] = make_double2(v * x[e].x, v * x[e].y);
-      }
-      fft_team<N, +1>(x, buf, tw_s, tl);
+      fft_team_in<N, -1>(InConjProduct<N>{wcol, ucol, tl}, x, buf, tw_s, tl);
+      fft_team_in<N, +1>(InScaled<N>{x, kern, tl}, x, buf, tw_s, tl);
       if (valid) {
 #pragma unroll
         for (int e = 0; e < E; ++e) acc[e] = cfma(x[e], ucol[TM::pos(tl, e)], acc[e]);
