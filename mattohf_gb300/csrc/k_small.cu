@@ -4,9 +4,13 @@
 // latency-bound, and a step of about 29 dependent launches costs more than the
 // arithmetic.  Here one launch does a whole RK4 stage (src/RT_calculation.f90:
 // 154-173).  Output column c = (k, b) is served by P CTAs (c, chunk):
-//   * the last warp of the column's first CTA computes the density of the
-//     stage input (F:55-71, reference order ig -> ik -> ib) and the Hartree
-//     potential (F:147-162) and stores them for the column's last CTA;
+//   * the column's first CTA computes the density of the stage input
+//     (F:55-71): all its threads first sum |u|^2 over slices of the occupied
+//     orbitals (in ik -> ib order within a slice, the uniform occupation
+//     applied once); then its last warp adds the slices, forms the Hartree
+//     potential (F:147-162) and stores both for the column's last CTA.  One
+//     warp alone would queue about 4 us of FP64 work on its SM sub-partition
+//     for the sum, and that backlog held up the whole CTA after the phase;
 //   * the other warps apply the exchange of column c against the CTA's chunk of
 //     the occupied orbitals (F:237-261, ordered pairs, no symmetry), one pair
 //     per team, and the CTA writes its partial sum;
@@ -132,20 +136,34 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   double2* kin_g = a.part + (size_t)ncols * (a.P + 1) * N + (size_t)c * N;  // T_A w
 
   for (int i = tid; i < N; i += kSmallThreads) tw_s[i] = a.tw[i];
+  // density, first part: sum of |u|^2 over slice j of the occupied orbitals at
+  // point ig, one (j, ig) per thread.  F_s, rho_s and vh_s (4N contiguous
+  // doubles) are free until the epilogue and hold the slices.
+  constexpr int NSUB = (kSmallThreads / N) < 4 ? (kSmallThreads / N) : 4;
+  double* dslice = reinterpret_cast<double*>(F_s);  // [NSUB][N]
+  if (chunk == 0 && tid < NSUB * N) {
+    const int ig = tid % N, j = tid / N;
+    const int per = (M + NSUB - 1) / NSUB;
+    const int q1 = min(M, (j + 1) * per);
+    double s = 0.0;
+#pragma unroll 4
+    for (int p = j * per; p < q1; ++p) {
+      const int ik = p / a.nbocc, b = p % a.nbocc;
+      const double2 z = a.u[((size_t)ik * a.nb + b) * N + ig];
+      s = fma(z.y, z.y, fma(z.x, z.x, s));
+    }
+    dslice[j * N + ig] = s;
+  }
   __syncthreads();
   if (warp == kSmallWarps - 1) {
     if (chunk == 0) {
-      // density of the stage input (reference order ig -> ik -> ib) and vH
+      // density (slices in order; with 3 or more slices rho_s[ig] is slice
+      // 2's entry for ig, read by this lane before it is overwritten) and vH
       for (int ig = lane; ig < N; ig += 32) {
-        double s = 0.0;
-        // occupied columns in (ik, ib) order; unrolled so the loads overlap
-#pragma unroll 8
-        for (int p = 0; p < M; ++p) {
-          const int ik = p / a.nbocc, b = p % a.nbocc;
-          const double2 z = a.u[((size_t)ik * a.nb + b) * N + ig];
-          s += fma(a.occ * z.x, z.x, (a.occ * z.y) * z.y);
-        }
-        rho_s[ig] = s;
+        double s = dslice[ig];
+#pragma unroll
+        for (int j = 1; j < NSUB; ++j) s += dslice[j * N + ig];
+        rho_s[ig] = a.occ * s;
       }
       __syncwarp();
       double2 x[E];
