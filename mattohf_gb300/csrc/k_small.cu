@@ -50,16 +50,11 @@ struct SmallLayout {
   static constexpr size_t bytes = sizeof(double2) * (size_t)N * (2 + NTEAM) + sizeof(double) * 2 * (size_t)N;
 };
 
-// The global last CTA: the observables of the stage input (mode 0 with a
-// previous step, mode 4) from the column buffer and this CTA's own density,
-// or the step counter (mode 3).  Run by one warp.
+// The global last CTA of an observable stage: the observables of the stage
+// input (mode 0 with a previous step, mode 4) from the column buffer and this
+// CTA's own density.  Run by one warp.
 __device__ void small_finalize(const SmallStageArgs& a, const double* rho_s, const double* vh_s, int N) {
   const int lane = threadIdx.x & 31;
-  if (a.mode == 3) {
-    if (lane == 0) *a.it = *a.it + 1;
-    return;
-  }
-  if (a.mode != 0 && a.mode != 4) return;  // stages 1 and 2 finalize nothing
   const int idx = *a.it - 1;
   if (idx < 0) return;
   const int ncol = a.nk * a.nb;
@@ -136,6 +131,13 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   double2* kin_g = a.part + (size_t)ncols * (a.P + 1) * N + (size_t)c * N;  // T_A w
 
   for (int i = tid; i < N; i += kSmallThreads) tw_s[i] = a.tw[i];
+  // Launched as a programmatic dependent of the previous stage: everything
+  // above reads only constant tables.  Wait for the previous grid to complete
+  // (and its writes to be visible) before touching the state or the scratch,
+  // then let the next stage's grid start its own prologue.  Both are no-ops
+  // without a programmatic dependency.
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;");
   // density, first part: sum of |u|^2 over slice j of the occupied orbitals at
   // point ig, one (j, ig) per thread.  F_s, rho_s and vh_s (4N contiguous
   // doubles) are free until the epilogue and hold the slices.
@@ -345,7 +347,10 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       a.colbuf[(size_t)c * 4 + 3] = si;
     }
   }
-  // the last column to finish finalizes (nothing waits on another CTA)
+  // stage 3 advances the step counter (one CTA); stages 1 and 2 finish here
+  if (a.mode == 3 && c == 0 && tid == 0) *a.it = *a.it + 1;
+  if (!obs) return;
+  // the last column to finish finalizes the observables (nothing waits on another CTA)
   __syncthreads();
   if (tid == 0) {
     __threadfence();
@@ -362,9 +367,17 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
 
 template <int N>
 static cudaError_t small_impl(const SmallStageArgs& a, cudaStream_t s) {
-  const int grid = a.nk * a.nb * a.P;
-  k_small_stage<N><<<grid, kSmallThreads, SmallLayout<N>::bytes, s>>>(a);
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(a.nk * a.nb * a.P);
+  cfg.blockDim = dim3(kSmallThreads);
+  cfg.dynamicSmemBytes = SmallLayout<N>::bytes;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_small_stage<N>, a);
 }
 
 template <int N>
