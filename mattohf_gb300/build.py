@@ -20,7 +20,7 @@ LIB = os.path.join(OUT_DIR, "libmattohf.so")
 DRIVER = os.path.join(OUT_DIR, "mattohf")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["ctx.cu", "k_hpsi.cu", "k_gs.cu", "k_table.cu", "noalloc.cu", "k_adjoint.cu", "k_spectra.cu", "k_fock_df.cu",
-           "k_small.cu"]
+           "k_small.cu", "k_small_adj.cu"]
 
 
 def nvcc() -> str:

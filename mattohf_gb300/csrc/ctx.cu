@@ -108,6 +108,7 @@ struct mattohf_ctx {
   double2* d_small_part = nullptr;  // exchange partials of the fused stages
   size_t small_part_cap = 0;
   int small_P = 1;                // CTAs per column of the fused stages
+  int small_P_adj = 1;            // CTAs per column of the fused reverse stages
   int nsm = 0;                    // multiprocessors of the device
   int* d_int = nullptr;  // [0] = step counter, [1] = non-finite flag, [2] = solver flag
   // RT series
@@ -583,11 +584,23 @@ int small_ctas_per_column(const mattohf_ctx* ctx) {
   return std::max(1, std::min(P, M));
 }
 
+// CTAs per column of the fused reverse stages: one round of the pass teams
+// (each orbital b takes a pass-A and a pass-B team), unless that needs more
+// CTAs than there are multiprocessors.
+int small_adj_ctas_per_column(const mattohf_ctx* ctx) {
+  const int ncols = ctx->NK * ctx->NB, M = ncols;
+  const int per_round = std::max(1, small_adj_pair_warps_teams(ctx->NG));
+  int P = (M + per_round - 1) / per_round;
+  if (ncols * P > ctx->nsm) P = std::max(1, ctx->nsm / ncols);
+  return std::max(1, std::min(P, M));
+}
+
 // Buffers of the fused stages, sized before any capture.
 int ensure_small_buffers(mattohf_ctx* ctx) {
   ctx->small_P = small_ctas_per_column(ctx);
+  ctx->small_P_adj = small_adj_ctas_per_column(ctx);
   // partials [ncols][P][NG], then (rho, vH) and the kinetic term, [ncols][NG] each
-  const size_t need = (size_t)ctx->NK * ctx->NB * (ctx->small_P + 2) * ctx->NG;
+  const size_t need = (size_t)ctx->NK * ctx->NB * (std::max(ctx->small_P, ctx->small_P_adj) + 2) * ctx->NG;
   if (need > ctx->small_part_cap) {
     if (ctx->capturing) return fail(ctx, MATTOHF_ERR_STATE, "fused-stage scratch growth during capture");
     destroy_graph(ctx);  // a captured step holds the old pointer
@@ -828,6 +841,7 @@ int mattohf_create(const mattohf_config* cfg, mattohf_ctx** out) {
     if (e == cudaSuccess) e = configure_adjoint_kernels();
     if (e == cudaSuccess) e = configure_df_kernels();
     if (e == cudaSuccess) e = configure_small_kernels();
+    if (e == cudaSuccess) e = configure_small_adj_kernels();
     if (e != cudaSuccess) return bail(MATTOHF_ERR_CUDA);
   }
   const size_t nu = orb_elems(ctx, ctx->NB);
@@ -1576,6 +1590,44 @@ int enq_adjoint_step(mattohf_ctx* ctx, double dt, size_t elems) {
   CK(launch_adj_init(ctx->d_lam, ctx->d_lamu, ctx->d_lamk, dt, elems, ctx->st));
   const double cst[3] = {0.5 * dt, 0.5 * dt, dt};
   const int amodes[4] = {AM, AAVE, AAVE, ACUR};
+  if (use_small(ctx)) {
+    // one fused launch per reverse stage; stage 0 also copies lam = lam_u and
+    // steps the counter back
+    SmallAdjArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.store = ctx->d_store;
+    a.n = n;
+    a.seg0 = seg0;
+    a.lam_u = ctx->d_lamu;
+    a.lam = ctx->d_lam;
+    a.af.A = ctx->d_A;
+    a.af.Aave = ctx->d_Aave;
+    a.af.it = n;
+    a.nk = NK;
+    a.nb = NB;
+    a.P = ctx->small_P_adj;
+    a.occ = ctx->occ;
+    a.kern = ctx->d_kern;
+    a.vCG = ctx->d_vCG;
+    a.vion = ctx->d_vion;
+    a.Gx = ctx->d_Gx;
+    a.kx = ctx->d_kx;
+    a.tw = ctx->tw;
+    a.part = ctx->d_small_part;
+    a.gcol = ctx->d_gcol;
+    a.gstage = ctx->d_gstage;
+    a.gvion = ctx->d_gvion;
+    a.ticket = ctx->d_ticket;
+    for (int s = 3; s >= 0; --s) {
+      a.slot = s;
+      a.mu = ctx->d_lamk[s];
+      a.lam_prev = s > 0 ? ctx->d_lamk[s - 1] : nullptr;
+      a.cprev = s > 0 ? cst[s - 1] : 0.0;
+      a.af.mode = amodes[s];
+      CK(launch_small_adj(NG, a, ctx->st));
+    }
+    return MATTOHF_OK;
+  }
   const int M = NK * ctx->NBocc;
   const int S = sym_tile(ctx);
   const int T = (M + S - 1) / S;

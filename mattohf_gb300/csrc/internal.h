@@ -226,6 +226,42 @@ bool small_stage_supported(int NG);
 int small_pair_teams(int NG);
 cudaError_t configure_small_kernels();
 
+// Fused reverse RK4 stage for small problems (all bands occupied): the
+// adjoint of one stage as enq_adjoint_step forms it, in one launch over
+// ncols * P CTAs.  Column a's CTAs split the ordered pairs (a, b) of the
+// adjoint exchange; the column's first CTA also forms vloc = vH[rho(v)] + vion,
+// psi = vH[sigma] and the kinetic term and field-gradient partial of column a;
+// the column's last CTA does the stage bookkeeping, the last column the
+// ordered field-gradient sum.
+struct SmallAdjArgs {
+  const double2* store;     // stage-input store; v = store[(n - seg0) * 4 + slot]
+  int* n;                   // backward step (device); stage 0 decrements it
+  const int* seg0;          // first step of the stored segment (device)
+  int slot;                 // RK4 stage 0..3
+  const double2* mu;        // this stage's adjoint lam_k[slot]
+  double2* lam_u;           // += J^T mu
+  double2* lam_prev;        // += cprev * J^T mu (lam_k[slot - 1]), or null
+  double cprev;
+  double2* lam;             // stage 0: lam = lam_u after the update
+  AField af;                // stage field (it = n)
+  int nk, nb, P;
+  double occ;
+  const double* kern;
+  const double* vCG;
+  const double* vion;
+  const double* Gx;
+  const double* kx;
+  const double2* tw;
+  double2* part;            // [ncols][P][NG] partials, then [ncols][NG] (vloc, psi), then [ncols][NG] T_A mu
+  double* gcol;             // [ncols] field-gradient partials
+  double* gstage;           // [nt][4]
+  double* gvion;            // += sigma
+  unsigned* ticket;         // [1 + ncols], as for the forward stages
+};
+cudaError_t launch_small_adj(int NG, const SmallAdjArgs& a, cudaStream_t s);
+int small_adj_pair_warps_teams(int NG);
+cudaError_t configure_small_adj_kernels();
+
 struct ObsReduceArgs {
   const double* colbuf;     // [nk*nb][4]
   const double* scal;       // dens scalars: Nele, Eion, EH

@@ -16,8 +16,10 @@ def _cfg(**kw):
 
 @pytest.mark.parametrize("objective", ["energy", "current"])
 @pytest.mark.parametrize("ckpt", [0, 2])
-def test_adjoint_matches_oracle(built_lib, objective, ckpt):
-    from mattohf_gb300 import Context
+@pytest.mark.parametrize("small", [0, 1])
+def test_adjoint_matches_oracle(built_lib, objective, ckpt, small):
+    """Both the separate-launch path and the fused forward/reverse stages."""
+    from mattohf_gb300 import Context, _capi
     from oracle import mattohf_oracle as O
     from conftest import to_oracle_config
     cfg = _cfg()
@@ -28,6 +30,7 @@ def test_adjoint_matches_oracle(built_lib, objective, ckpt):
     dt = 0.004
     Lr, gr, gvr = O.rt_adjoint(S, u0, A, dt, objective)
     with Context(cfg) as ctx:
+        ctx.set_option(_capi.OPT_SMALL_STAGES, small)
         ctx.set_orbitals(u0)
         L, g, gv = ctx.adjoint(A, dt, objective, ckpt_every=ckpt)
     assert abs(L - Lr) <= 1e-10 * max(1.0, abs(Lr))
@@ -60,3 +63,36 @@ def test_adjoint_finite_differences_gpu(built_lib):
             Am[n] -= h
             fd = (obj(Ap) - obj(Am)) / (2 * h)
             assert abs(g[n] - fd) <= 1e-6 * np.max(np.abs(g)) + 2e-10, (n, g[n], fd)
+
+
+@pytest.mark.parametrize("NG,NK,NB", [(16, 3, 2), (32, 5, 1), (64, 4, 2), (128, 8, 2), (256, 3, 3)])
+@pytest.mark.parametrize("objective", ["energy", "current"])
+def test_fused_reverse_stages_match_separate_launches(built_lib, NG, NK, NB, objective):
+    """The fused reverse stage (ordered exchange pairs, one launch per stage) gives
+    the gradients of the separate-launch backward step (symmetric exchange) to
+    round-off, for every team width of the transforms."""
+    from mattohf_gb300 import Context, _capi
+    cfg = _cfg(NG=NG, NK=NK, NB=NB, NBocc=NB, acell=9.0)
+    rng = np.random.default_rng(6)
+    nt = 7
+    A = 0.05 * np.sin(0.4 * np.arange(nt)) + 1e-2 * rng.standard_normal(nt)
+    dt = 2e-4          # RK4-stable up to NG = 256 at a = 9 (|E_max| dt < 1)
+    out = {}
+    with Context(cfg) as ctx:
+        ctx.Init_wf()
+        ctx.Gram_Schmidt()
+        u0 = ctx.get_orbitals()
+        for small in (0, 1):
+            for ckpt in (0, 3):
+                ctx.set_option(_capi.OPT_SMALL_STAGES, small)
+                ctx.set_orbitals(u0)
+                out[small, ckpt] = ctx.adjoint(A, dt, objective, ckpt_every=ckpt)
+    for ckpt in (0, 3):
+        L0, g0, v0 = out[0, ckpt]
+        L1, g1, v1 = out[1, ckpt]
+        assert np.isfinite(L0) and np.all(np.isfinite(g0))
+        assert abs(L1 - L0) <= 1e-12 * max(1.0, abs(L0))
+        assert np.max(np.abs(g1 - g0)) <= 1e-11 * np.max(np.abs(g0))
+        assert np.max(np.abs(v1 - v0)) <= 1e-11 * np.max(np.abs(v0))
+    # the checkpoint modes of the fused path agree bitwise
+    assert np.array_equal(out[1, 0][1], out[1, 3][1])
