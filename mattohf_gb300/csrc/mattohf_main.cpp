@@ -13,6 +13,7 @@
 //   <sys>_DoS.out, _band.out band energies and broadened DoS (src/GS_calculation.f90:93-118, 239-265)
 //   <sys>_EtotNJEAt.out      time, Etot, dEtot, Nele, dNele, J, E, A (src/RT_calculation.f90:22-24, 52-53)
 //   <sys>_JEAF.out, _sigmaeps.out (LR) or _JEAF_window.out (LP)   (src/RT_calculation.f90:246-351)
+//   <sys>_dipole.out         time, P = -int J dt (extension; trapezoid from J(0))
 //
 // Usage: `echo '"input.dat"' | mattohf [output directory]`.  An empty name
 // keeps every default of src/Global_variables.f90:7-26.  Exit status 0 on
@@ -544,6 +545,17 @@ int run(const Config& c, const std::string& dir) {
     f << "#time(it), Etot(it)-Etot0, N(it)-N0, J(it), E(it), A(it)\n";
     for (int it = 0; it < NT; ++it)
       f << row({time[it], Et[it], Et[it] - ini.Etot, Ne[it], Ne[it] - ini.Nele, Je[it], E[it], A[it]}) << "\n";
+  }
+  {
+    // extension (no reference counterpart): dipole P = -int J dt, trapezoid from J(0)
+    std::ofstream f = open_out(dir, sysn + "_dipole.out");
+    f << "#time(it), P(it)\n";
+    double acc = 0.0, prev = ini.Je;
+    for (int it = 0; it < NT; ++it) {
+      acc -= 0.5 * c.dt * (prev + Je[it]);
+      prev = Je[it];
+      f << row({time[it], acc}) << "\n";
+    }
   }
   const double t_rt = seconds_since(t_rt0);
 

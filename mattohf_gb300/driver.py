@@ -12,6 +12,7 @@ and writes the reference's output files in its formats:
   <sys>_DoS.out, _band.out band energies and broadened DoS (src/GS_calculation.f90:93-118, 239-265)
   <sys>_EtotNJEAt.out      time, Etot, dEtot, Nele, dNele, J, E, A  (src/RT_calculation.f90:22-24, 52-53)
   <sys>_JEAF.out, _sigmaeps.out, _JEAF_window.out     (src/RT_calculation.f90:246-351)
+  <sys>_dipole.out         time, P = -int J dt (extension; trapezoid from J(0))
 
 Only the hot path runs on the GPU (all through ``libmattohf.so``); the files
 are written on the host.
@@ -28,7 +29,7 @@ import numpy as np
 
 from . import _capi
 from .api import Context
-from .inputs import ATOMFLUENCE, ATOMTIME, HARTREE, PI, RunConfig, define_afield, read_input, _powi
+from .inputs import ATOMFLUENCE, ATOMTIME, HARTREE, PI, RunConfig, define_afield, dipole_from_current, read_input, _powi
 
 _D = C.POINTER(C.c_double)
 
@@ -197,6 +198,12 @@ def run(cfg: RunConfig, out_dir: str = ".", rt_chunk: int = 1000, log=print) -> 
         fh.write("#time(it), Etot(it)-Etot0, N(it)-N0, J(it), E(it), A(it)\n")
         for it in range(NT):
             fh.write(_row([time_[it], Et[it], Et[it] - Etotm1, Ne[it], Ne[it] - Nelem1, Je[it], E[it], A[it]]) + "\n")
+    # extension (no reference counterpart): dipole P = -int J dt, trapezoid from J(0)
+    P = dipole_from_current(Je, Jtotm1, cfg.dt)
+    with open(p(f"{sysn}_dipole.out"), "w") as fh:
+        fh.write("#time(it), P(it)\n")
+        for it in range(NT):
+            fh.write(_row([time_[it], P[it]]) + "\n")
     t_rt = time.perf_counter() - t_rt
     # ---- spectra (RT:64-65)
     ft = fourier(cfg, time_, Je, Jtotm1, E, A, window=False)
@@ -223,7 +230,7 @@ def run(cfg: RunConfig, out_dir: str = ".", rt_chunk: int = 1000, log=print) -> 
     log(f"Time for an interaction in RT ={t_rt / max(NT, 1):12.4E} [sec]")
     log(f"Fluence of the field: {float(np.sum(E ** 2) * cfg.dt * ATOMFLUENCE)!r} J/cm^2")
     ctx.close()
-    return {"Etot": Et, "Je": Je, "Nele": Ne, "A": A, "E": E, "time": time_, "t_rt": t_rt,
+    return {"Etot": Et, "Je": Je, "Nele": Ne, "P": P, "J0": Jtotm1, "A": A, "E": E, "time": time_, "t_rt": t_rt,
             "t_total": time.perf_counter() - t_all}
 
 

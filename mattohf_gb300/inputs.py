@@ -200,3 +200,21 @@ def aave_from_samples(A: np.ndarray) -> np.ndarray:
         Aave[0] = 0.5 * (A[0] + 0.0)
         Aave[1:] = 0.5 * (A[1:] + A[:-1])
     return Aave
+
+
+def dipole_from_current(J: np.ndarray, J0: float, dt: float) -> np.ndarray:
+    """Dipole P(t_i) = -int_0^{t_i} J dt' by the trapezoid rule on the RT time
+    grid t_i = (i+1) dt, with J(0) = J0 (the current of the initial state).
+
+    An extension: the reference writes Etot, Nele, Jtot, E and A
+    (src/RT_calculation.f90:52-53) and no dipole, so P is pinned only through J.
+    """
+    J = np.asarray(J, dtype=np.float64)
+    P = np.empty_like(J)
+    acc = 0.0
+    prev = float(J0)
+    for i in range(J.size):
+        acc -= 0.5 * dt * (prev + J[i])
+        P[i] = acc
+        prev = J[i]
+    return P

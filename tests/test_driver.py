@@ -98,12 +98,20 @@ def test_driver_end_to_end(tmp_path, built_lib):
     cfg = read_input(str(p))
     res = run(cfg, out_dir=str(tmp_path), log=lambda *a: None)
     for f in ("potential.out", "vk.out", "tiny_GSinfo.out", "tiny_DoS.out", "tiny_band.out",
-              "tiny_EtotNJEAt.out", "tiny_JEAF.out", "tiny_JEAF_window.out"):
+              "tiny_EtotNJEAt.out", "tiny_JEAF.out", "tiny_JEAF_window.out", "tiny_dipole.out"):
         assert os.path.exists(tmp_path / f), f
     rows = [l for l in open(tmp_path / "tiny_EtotNJEAt.out") if not l.startswith("#")]
     assert len(rows) == cfg.NT and len(rows[0]) == 8 * 20 + 1
     vals = np.array([[float(l[i * 20:(i + 1) * 20].replace("E", "e")) for i in range(8)] for l in rows])
     assert np.allclose(vals[:, 1], res["Etot"], rtol=1e-11, atol=0)
+    # the dipole extension: -int J dt by the trapezoid rule from the initial current
+    from oracle import mattohf_oracle as O
+    prow = [l for l in open(tmp_path / "tiny_dipole.out") if not l.startswith("#")]
+    P = np.array([float(l[20:40].replace("E", "e")) for l in prow])
+    assert len(prow) == cfg.NT
+    Pref = O.dipole_from_current(res["time"], res["Je"], res["J0"], cfg.dt)
+    assert np.allclose(P, Pref, rtol=1e-11, atol=1e-13 * np.max(np.abs(Pref)))
+    assert np.allclose(res["P"], Pref, rtol=1e-12, atol=0)
 
 
 @pytest.mark.gpu

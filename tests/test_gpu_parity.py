@@ -394,9 +394,13 @@ def test_context_usable_after_errors():
 @pytest.mark.parametrize("small", [0, 1])
 def test_long_golden_run(small):
     """The full 2000-step run of the CPU-runnable shape (stable dt) against the oracle's
-    committed series, through the tiled path and through the fused stages: relative
-    errors of Etot, Je, Nele and the final orbitals stay within the 1e-10 bound."""
-    from mattohf_gb300 import Context, RunConfig, aave_from_samples, _capi
+    committed series, through the tiled path and through the fused stages.  The
+    relative error of each result (Etot, Je, Nele, the dipole, the final orbitals)
+    is printed and stays within the 1e-10 bound.  Je crosses zero, so its error is
+    relative to max |Je| (at least 1); the dipole is -int Je dt from the initial
+    current by the trapezoid rule, pinned only through Je."""
+    from mattohf_gb300 import Context, RunConfig, aave_from_samples, dipole_from_current, _capi
+    from oracle import mattohf_oracle as O
     g = np.load(os.path.join(GOLD, "rt2000_ng64_nk8.npz"))
     with open(os.path.join(GOLD, "rt2000_ng64_nk8.json")) as fh:
         d = json.load(fh)
@@ -405,9 +409,18 @@ def test_long_golden_run(small):
     with Context(cfg) as ctx:
         ctx.set_option(_capi.OPT_SMALL_STAGES, small)
         ctx.set_orbitals(g["u0"])
+        J0 = ctx.observables(0.0)["Je"]
         E, J, N = ctx.rk4_run(A, aave_from_samples(A), cfg.dt)
         u = ctx.get_orbitals()
-    assert rel(E, g["rt_Etot"]) <= TOL_RT
-    assert np.max(np.abs(J - g["rt_Jtot"])) <= TOL_RT * max(1.0, np.max(np.abs(g["rt_Jtot"])))
-    assert rel(N, g["rt_Nele"]) <= TOL_RT
-    assert rel(u, g["rt_u"]) <= TOL_RT
+    S = O.make_system(to_oracle_config(cfg))
+    J0r = O.ubk_Je(S, g["u0"], 0.0)
+    P = dipole_from_current(J, J0, cfg.dt)
+    Pr = O.dipole_from_current(None, g["rt_Jtot"], J0r, cfg.dt)
+    err = {"Etot": rel(E, g["rt_Etot"]),
+           "Je": np.max(np.abs(J - g["rt_Jtot"])) / max(1.0, np.max(np.abs(g["rt_Jtot"]))),
+           "Nele": rel(N, g["rt_Nele"]),
+           "dipole": rel(P, Pr),
+           "orbitals": rel(u, g["rt_u"])}
+    print("golden 2000-step run, small=%d: " % small + ", ".join(f"{k} {v:.2e}" for k, v in err.items()))
+    for k, v in err.items():
+        assert v <= TOL_RT, (k, v)

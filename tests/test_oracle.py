@@ -236,3 +236,20 @@ def test_c_port_matches_long_golden_run():
     assert np.max(np.abs(J - g["rt_Jtot"])) <= 1e-10 * max(1.0, np.max(np.abs(g["rt_Jtot"])))
     assert np.max(np.abs(N - g["rt_Nele"])) <= 1e-10 * np.max(np.abs(g["rt_Nele"]))
     assert np.max(np.abs(u - g["rt_u"])) <= 1e-10 * np.max(np.abs(g["rt_u"]))
+
+
+def test_dipole_helper_matches_oracle_quadrature():
+    """The product's dipole (P = -int J dt, trapezoid from J(0)) is the oracle's
+    quadrature, bitwise, on the golden 2000-step current."""
+    import json
+    import os
+    from mattohf_gb300 import dipole_from_current
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    g = np.load(os.path.join(here, "rt2000_ng64_nk8.npz"))
+    with open(os.path.join(here, "rt2000_ng64_nk8.json")) as fh:
+        cfg = O.Config(**json.load(fh))
+    S = O.make_system(cfg)
+    J0 = O.ubk_Je(S, g["u0"], 0.0)
+    P = dipole_from_current(g["rt_Jtot"], J0, cfg.dt)
+    assert np.array_equal(P, O.dipole_from_current(None, g["rt_Jtot"], J0, cfg.dt))
+    assert P.shape == g["rt_Jtot"].shape and np.all(np.isfinite(P))
