@@ -49,6 +49,8 @@ extern "C" {
                                       column; for small problems): 0 off, 1 on, 2 automatic (default) */
 #define MATTOHF_OPT_L2_FLUSH 5     /* >0: bytes written between RK4 steps of mattohf_rk4_run, which then
                                       reports the summed per-step device time (benchmarking) */
+#define MATTOHF_OPT_SMALL_CTAS 9   /* CTAs per output column of the fused stages (the exchange pairs of a
+                                      column are split over them); 0 = automatic (default) */
 
 typedef struct mattohf_ctx mattohf_ctx;
 
@@ -160,6 +162,17 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
  * MATTOHF_OPT_KERNEL_TIMING) the summed device time and launch count of the
  * Fock pair kernel inside it. */
 int mattohf_last_run_timing(mattohf_ctx* ctx, double* run_ms, double* fock_ms, int* fock_launches);
+/* Autotuner (no reference counterpart; the reference has no launch shapes).
+ * Times, on the context's current orbitals, (1) the symmetric-exchange tile
+ * size for one h[u]u exchange apply, (2) the CTAs per column of the fused
+ * small-problem stages and (3) fused stages against the tiled step, with
+ * `steps` graph-replayed mattohf_rk4_run steps (dt = 1e-4, A = 0) per
+ * candidate, then keeps the fastest as MATTOHF_OPT_SYM_TILE,
+ * MATTOHF_OPT_SMALL_CTAS and MATTOHF_OPT_SMALL_STAGES (0 or 1).  The orbitals
+ * are restored.  out[3] (may be NULL): tile, CTAs per column (0 if the fused
+ * stages do not apply), 1 if the fused stages won; us[3] (may be NULL):
+ * microseconds of the exchange apply, of a tiled step and of a fused step. */
+int mattohf_autotune(mattohf_ctx* ctx, int steps, int* out, double* us);
 
 /* GS_calculation (src/GS_calculation.f90:2-121) SCF loop: per iteration
  * Gram_Schmidt, KS_ubk2_SVD (Krylov block of NB*ncg columns, GS:124-194),
@@ -215,8 +228,14 @@ mattohf_ctx* mattohf_batch_run(mattohf_batch* b, int run);
 int mattohf_batch_rk4_run(mattohf_batch* b, int nt, const double* dt, const double* A,
                           const double* Aave, double* Etot, double* Je, double* Nele);
 int mattohf_batch_last_run_ms(mattohf_batch* b, double* ms);
-/* Batch options: MATTOHF_OPT_FOCK_DF64 only. */
+/* Batch options: MATTOHF_OPT_FOCK_DF64, and MATTOHF_OPT_SYM_TILE (the exchange
+ * tile of every run's tile pairs; 0 = a CTA's teams, the default). */
 int mattohf_batch_set_option(mattohf_batch* b, int option, long long value);
+/* Batch autotuner: times every exchange tile (a CTA's teams, then halves down
+ * to 1) over `steps` graph-replayed ensemble steps (dt = 1e-4, A = 0) on the
+ * runs' current orbitals, restores them and keeps the fastest tile.  tile,
+ * us (may be NULL): the tile kept and an ensemble step's time in microseconds. */
+int mattohf_batch_autotune(mattohf_batch* b, int steps, int* tile, double* us);
 
 /* Diagnostic (no reference counterpart): measured FP64 FMA throughput of
  * `device` in TFLOP/s (2 flops per DFMA), the roofline denominator of the

@@ -30,6 +30,7 @@ OPT_L2_FLUSH = 5
 OPT_FOCK_DF64 = 6
 OPT_SYM_TILE = 7
 OPT_SMALL_STAGES = 8
+OPT_SMALL_CTAS = 9
 
 # every symbol include/mattohf.h declares
 EXPORTS = [
@@ -43,7 +44,8 @@ EXPORTS = [
     "mattohf_synchronize", "mattohf_diag_fp64_peak", "mattohf_diag_dmma_peak", "mattohf_fock_noalloc",
     "mattohf_batch_create", "mattohf_batch_destroy", "mattohf_batch_last_error", "mattohf_batch_run",
     "mattohf_batch_rk4_run", "mattohf_batch_last_run_ms", "mattohf_adjoint", "mattohf_adjoint_timing",
-    "mattohf_fourier", "mattohf_vck", "mattohf_te_step", "mattohf_batch_set_option",
+    "mattohf_fourier", "mattohf_vck", "mattohf_te_step", "mattohf_batch_set_option", "mattohf_autotune",
+    "mattohf_batch_autotune",
 ]
 
 
@@ -97,6 +99,8 @@ def load(path: str = LIB_PATH):
         "mattohf_rk4_step": ([P, C.c_double, C.c_double, C.c_double], I),
         "mattohf_rk4_run": ([P, I, C.c_double, D, D, D, D, D], I),
         "mattohf_last_run_timing": ([P, D, D, C.POINTER(C.c_int)], I),
+        "mattohf_autotune": ([P, I, C.POINTER(C.c_int), D], I),
+        "mattohf_batch_autotune": ([P, I, C.POINTER(C.c_int), D], I),
         "mattohf_gs_run": ([P, I, I, D, D, D, D, D], I),
         "mattohf_eps": ([P, D, D], I),
         "mattohf_synchronize": ([P], I),

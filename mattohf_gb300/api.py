@@ -219,6 +219,16 @@ class Context:
         self._check(st)
         return E, J, N
 
+    def autotune(self, steps: int = 20) -> dict:
+        """Time the tunable launch shapes on the current orbitals and keep the
+        fastest (exchange tile, fused-stage CTAs per column, fused vs tiled
+        stepping); the orbitals are restored.  Returns the choices and times."""
+        out = (C.c_int * 3)()
+        us = (C.c_double * 3)()
+        self._check(self.lib.mattohf_autotune(self.h, int(steps), out, us))
+        return {"sym_tile": out[0], "small_ctas": out[1], "small_stages": bool(out[2]),
+                "exchange_us": us[0], "tiled_step_us": us[1], "fused_step_us": us[2]}
+
     def last_run_timing(self):
         r, f = C.c_double(), C.c_double()
         n = C.c_int()
@@ -315,6 +325,14 @@ class Batch:
     def _check(self, st):
         if st != _capi.OK:
             raise MattohfError(st, self.lib.mattohf_batch_last_error(self.h).decode())
+
+    def autotune(self, steps: int = 10) -> dict:
+        """Time every exchange tile over ensemble steps on the runs' current
+        orbitals (restored afterwards) and keep the fastest."""
+        tile = C.c_int()
+        us = C.c_double()
+        self._check(self.lib.mattohf_batch_autotune(self.h, int(steps), C.byref(tile), C.byref(us)))
+        return {"sym_tile": tile.value, "step_us": us.value}
 
     def rk4_run(self, A, Aave, dt):
         """A, Aave: (nruns, nt); dt: scalar or (nruns,).  Returns (Etot, Je, Nele), each (nruns, nt)."""

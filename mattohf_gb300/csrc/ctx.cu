@@ -103,6 +103,7 @@ struct mattohf_ctx {
   int opt_df = 0;             // exchange transforms in double-float arithmetic
   int opt_tile = 0;           // symmetric-exchange tile size (0 = automatic)
   int opt_small = 2;          // fused small-problem RK4 stages: 0 off, 1 on, 2 automatic
+  int opt_small_ctas = 0;     // CTAs per column of the fused stages (0 = automatic)
   bool step_small = false;    // the captured step graph uses the fused stages
   unsigned* d_ticket = nullptr;  // completion counters of the fused stages [1 + NK*NB]
   double2* d_small_part = nullptr;  // exchange partials of the fused stages
@@ -577,6 +578,8 @@ bool use_small(const mattohf_ctx* ctx) {
 int small_ctas_per_column(const mattohf_ctx* ctx) {
   const int ncols = ctx->NK * ctx->NB, M = ctx->NK * ctx->NBocc;
   const int pair_teams = small_pair_teams(ctx->NG);   // 6 warps' teams
+  if (ctx->opt_small_ctas > 0)  // set (or tuned): at least one round of all pair teams, at most M
+    return std::max(std::max(1, (M + pair_teams - 1) / pair_teams), std::min(ctx->opt_small_ctas, std::max(1, M)));
   const int two_warps = std::max(1, pair_teams / 3);
   int P = (M + two_warps - 1) / two_warps;
   if (ncols * P > ctx->nsm) P = std::max(1, ctx->nsm / ncols);
@@ -941,6 +944,10 @@ int mattohf_set_option(mattohf_ctx* ctx, int option, long long value) {
     case MATTOHF_OPT_L2_FLUSH:
       if (value < 0 || value > (4LL << 30)) return fail(ctx, MATTOHF_ERR_ARG, "flush bytes out of range");
       ctx->opt_flush = value;
+      break;
+    case MATTOHF_OPT_SMALL_CTAS:
+      if (value < 0 || value > 4096) return fail(ctx, MATTOHF_ERR_ARG, "CTAs per column must be 0..4096");
+      ctx->opt_small_ctas = (int)value;
       break;
     default: return fail(ctx, MATTOHF_ERR_ARG, "unknown option");
   }
@@ -1380,6 +1387,137 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
     std::snprintf(buf, sizeof(buf), "non-finite state at RK4 step %d (1-based it=%d); %d steps run",
                   first, first + 1, ndone);
     return fail(ctx, MATTOHF_ERR_NONFINITE, buf);
+  }
+  return MATTOHF_OK;
+}
+
+// Autotuner: times the context's tunable launch shapes on its own orbitals
+// and keeps the fastest.  The orbitals (and the step counter) are restored.
+//   * symmetric-exchange tile S: one exchange apply h[u]u (k_fock_sym +
+//     k_sym_reduce, or the double-float kernels) for S = 1, 2, 4, ... up to the
+//     teams of a CTA;
+//   * fused-stage CTAs per column P, for the grids the fused stages support:
+//     graph-replayed mattohf_rk4_run steps for P from one round of all pair
+//     teams up to the multiprocessors (powers of two and the default);
+//   * fused stages vs the tiled step: the faster of the best of each.
+// out: [0] S, [1] P (0 when the fused stages do not apply), [2] 1 when the
+// fused stages won; us: [0] exchange apply at S, [1] step of the tiled path,
+// [2] step of the fused path (0 when not timed), in microseconds.
+extern "C" int mattohf_autotune(mattohf_ctx* ctx, int steps, int* out, double* us) {
+  CKR(check_ctx(ctx));
+  if (steps < 1 || steps > 100000) return fail(ctx, MATTOHF_ERR_ARG, "autotune steps must be 1..100000");
+  if (ctx->capturing) return fail(ctx, MATTOHF_ERR_STATE, "autotune during capture");
+  const int NG = ctx->NG, NB = ctx->NB, NK = ctx->NK;
+  const size_t elems = orb_elems(ctx, NB);
+  struct DevBuf {
+    double2* p = nullptr;
+    ~DevBuf() {
+      if (p) cudaFree(p);
+    }
+  } saved;
+  CK(cudaMalloc((void**)&saved.p, sizeof(double2) * elems));
+  CK(cudaMemcpyAsync(saved.p, ctx->d_u, sizeof(double2) * elems, cudaMemcpyDeviceToDevice, ctx->st));
+  ScopedEvent e0, e1;
+  CK(e0.create());
+  CK(e1.create());
+  auto restore = [&]() -> int {
+    CK(cudaMemcpyAsync(ctx->d_u, saved.p, sizeof(double2) * elems, cudaMemcpyDeviceToDevice, ctx->st));
+    CK(cudaMemsetAsync(ctx->d_int, 0, 2 * sizeof(int), ctx->st));
+    return MATTOHF_OK;
+  };
+  // ---- exchange tile
+  int bestS = sym_tile(ctx);
+  double tS = 0.0;
+  if (ctx->hf && ctx->opt_sym && ctx->NBocc > 0) {
+    const int reps = std::max(2, std::min(steps, 20));
+    double best = 1e300;
+    const int M = NK * ctx->NBocc, Smax = fock_sym_teams(NG);
+    for (int S = 1; S <= Smax; S <<= 1) {
+      // tiles far beyond a few waves only add partial-sum traffic (and scratch)
+      const long long T = (M + S - 1) / S;
+      if (S < Smax && T * (T + 1) / 2 > 32LL * ctx->nsm) continue;
+      ctx->opt_tile = S;
+      CKR(ensure_fock_buffers(ctx));
+      const Block ub = blk(ctx->d_u, NB, NG, NB);
+      FockPlan fp;
+      CKR(enq_fock(ctx, ub, ub, &fp));  // warm-up
+      CK(cudaEventRecord(e0, ctx->st));
+      for (int r = 0; r < reps; ++r) CKR(enq_fock(ctx, ub, ub, &fp));
+      CK(cudaEventRecord(e1, ctx->st));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      const double t = 1e3 * ms / reps;
+      if (t < best) {
+        best = t;
+        bestS = S;
+      }
+    }
+    ctx->opt_tile = bestS;
+    tS = best;
+  }
+  // ---- stepping: tiled, then the fused stages for each P
+  std::vector<double> A(steps, 0.0), h1(steps), h2(steps), h3(steps);
+  auto time_steps = [&](double* t_us) -> int {
+    destroy_graph(ctx);
+    CKR(restore());
+    int rc = mattohf_rk4_run(ctx, steps, 1e-4, A.data(), A.data(), h1.data(), h2.data(), h3.data());
+    if (rc != MATTOHF_OK) return rc;  // first call captures the graph
+    CKR(restore());
+    rc = mattohf_rk4_run(ctx, steps, 1e-4, A.data(), A.data(), h1.data(), h2.data(), h3.data());
+    if (rc != MATTOHF_OK) return rc;
+    *t_us = 1e3 * ctx->last_run_ms / steps;
+    return MATTOHF_OK;
+  };
+  const int opt_small0 = ctx->opt_small, opt_ctas0 = ctx->opt_small_ctas;
+  double t_tiled = 0.0, t_fused = 0.0;
+  int bestP = 0;
+  ctx->opt_small = 0;
+  int rc = time_steps(&t_tiled);
+  const bool fused_ok = small_stage_supported(NG) && !ctx->opt_df && !ctx->opt_timing && ctx->NBocc > 0;
+  if (rc == MATTOHF_OK && fused_ok) {
+    const int ncols = NK * NB, M = NK * ctx->NBocc;
+    const int lo = std::max(1, (M + small_pair_teams(NG) - 1) / small_pair_teams(NG));
+    const int hi = std::max(lo, std::min(M, std::max(1, 2 * ctx->nsm / ncols)));
+    ctx->opt_small = 1;
+    ctx->opt_small_ctas = 0;
+    std::vector<int> cand{small_ctas_per_column(ctx)};
+    for (int P = 1; P <= hi; P <<= 1)
+      if (P >= lo && P != cand[0]) cand.push_back(P);
+    double best = 1e300;
+    for (int P : cand) {
+      ctx->opt_small_ctas = P;
+      double t = 0.0;
+      if ((rc = time_steps(&t)) != MATTOHF_OK) break;
+      if (t < best) {
+        best = t;
+        bestP = P;
+      }
+    }
+    t_fused = best;
+  }
+  // restore the state whatever happened, then keep the winners
+  const int rr = restore();
+  destroy_graph(ctx);
+  if (rc != MATTOHF_OK) {
+    ctx->opt_small = opt_small0;
+    ctx->opt_small_ctas = opt_ctas0;
+    return rc;
+  }
+  if (rr != MATTOHF_OK) return rr;
+  const bool fused_wins = bestP > 0 && t_fused < t_tiled;
+  ctx->opt_small = fused_wins ? 1 : 0;
+  ctx->opt_small_ctas = bestP;
+  CK(cudaStreamSynchronize(ctx->st));
+  if (out) {
+    out[0] = bestS;
+    out[1] = bestP;
+    out[2] = fused_wins ? 1 : 0;
+  }
+  if (us) {
+    us[0] = tS;
+    us[1] = t_tiled;
+    us[2] = bestP > 0 ? t_fused : 0.0;
   }
   return MATTOHF_OK;
 }
@@ -1983,6 +2121,7 @@ struct mattohf_batch {
   cudaStream_t st_side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int opt_df = 0;  // exchange transforms in double-float arithmetic
+  int opt_tile = 0;  // symmetric-exchange tile of every run (0 = the CTA's teams)
   ObsReduceArgs* d_obs = nullptr;
   ExArgs* d_ex = nullptr;
   ExArgs* d_exf = nullptr;
@@ -2045,7 +2184,9 @@ int batch_prepare(mattohf_batch* b, int nt) {
   std::vector<ExArgs> ex(R), exf(R);
   std::vector<int> tile_pre(R + 1, 0), elem_pre(R + 1, 0), cta_pre(R + 1, 0);
   const int cpc = combine_cols_per_cta(NG);
-  const int S = fock_sym_teams(NG);
+  // one launch shape (a CTA's teams) for every run; a smaller tile leaves
+  // teams idle but gives small runs more CTAs
+  const int S = b->opt_tile > 0 ? b->opt_tile : fock_sym_teams(NG);
   for (int r = 0; r < R; ++r) {
     mattohf_ctx* ctx = b->runs[r];
     int rc;
@@ -2356,13 +2497,88 @@ int mattohf_batch_rk4_run(mattohf_batch* b, int nt, const double* dt, const doub
 
 int mattohf_batch_set_option(mattohf_batch* b, int option, long long value) {
   if (!b) return MATTOHF_ERR_ARG;
-  if (option != MATTOHF_OPT_FOCK_DF64) return bfail(b, MATTOHF_ERR_ARG, "unsupported batch option");
-  b->opt_df = value ? 1 : 0;
+  if (option == MATTOHF_OPT_FOCK_DF64) {
+    b->opt_df = value ? 1 : 0;
+  } else if (option == MATTOHF_OPT_SYM_TILE) {
+    if (value < 0 || value > fock_sym_teams(b->NG) || (value & (value - 1)))
+      return bfail(b, MATTOHF_ERR_ARG, "tile size must be 0 or a power of two up to the CTA's teams");
+    b->opt_tile = (int)value;
+  } else {
+    return bfail(b, MATTOHF_ERR_ARG, "unsupported batch option");
+  }
   if (b->exec) {
     cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
   }
   b->built_nt = -1;
+  return MATTOHF_OK;
+}
+
+// Batch autotuner: the exchange tile shared by every run's tile pairs, timed
+// over `steps` graph-replayed ensemble steps (dt = 1e-4, A = 0) per
+// candidate on the runs' current orbitals, which are restored.  out: the tile
+// kept; us: microseconds of an ensemble step at that tile.
+int mattohf_batch_autotune(mattohf_batch* b, int steps, int* tile, double* us) {
+  if (!b || steps < 1 || steps > 100000) return MATTOHF_ERR_ARG;
+  BCK(cudaSetDevice(b->device));
+  for (auto* c : b->runs) BCK(cudaStreamSynchronize(c->st));
+  std::vector<double2*> saved(b->R, nullptr);
+  struct Free {
+    std::vector<double2*>& v;
+    ~Free() {
+      for (auto* p : v)
+        if (p) cudaFree(p);
+    }
+  } guard{saved};
+  for (int r = 0; r < b->R; ++r) {
+    mattohf_ctx* c = b->runs[r];
+    const size_t n = orb_elems(c, c->NB);
+    BCK(cudaMalloc((void**)&saved[r], sizeof(double2) * n));
+    BCK(cudaMemcpyAsync(saved[r], c->d_u, sizeof(double2) * n, cudaMemcpyDeviceToDevice, b->st));
+  }
+  auto restore = [&]() -> int {
+    for (int r = 0; r < b->R; ++r) {
+      mattohf_ctx* c = b->runs[r];
+      BCK(cudaMemcpyAsync(c->d_u, saved[r], sizeof(double2) * orb_elems(c, c->NB), cudaMemcpyDeviceToDevice,
+                          b->st));
+    }
+    BCK(cudaStreamSynchronize(b->st));
+    return MATTOHF_OK;
+  };
+  const std::vector<double> dts0 = b->dts;
+  const int tile0 = b->opt_tile;
+  std::vector<double> A((size_t)b->R * steps, 0.0), dt(b->R, 1e-4);
+  double best = 1e300;
+  int bestS = 0, rc = MATTOHF_OK;
+  for (int S = fock_sym_teams(b->NG); S >= 1 && rc == MATTOHF_OK; S >>= 1) {
+    b->opt_tile = S;
+    b->built_nt = -1;
+    double t = 0.0;
+    for (int pass = 0; pass < 2 && rc == MATTOHF_OK; ++pass) {  // the first pass builds the graph
+      if ((rc = restore()) != MATTOHF_OK) break;
+      rc = mattohf_batch_rk4_run(b, steps, dt.data(), A.data(), A.data(), nullptr, nullptr, nullptr);
+      t = 1e3 * b->last_ms / steps;
+    }
+    if (rc == MATTOHF_OK && t < best) {
+      best = t;
+      bestS = S;
+    }
+  }
+  const int rr = restore();
+  b->dts = dts0;
+  b->built_nt = -1;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  if (rc != MATTOHF_OK) {
+    b->opt_tile = tile0;
+    return rc;
+  }
+  if (rr != MATTOHF_OK) return rr;
+  b->opt_tile = bestS;
+  if (tile) *tile = bestS;
+  if (us) *us = best;
   return MATTOHF_OK;
 }
 

@@ -23,6 +23,8 @@
 //     and Je from warp 6's forward transform at the previous step's field,
 //     <u|F u> from the last CTA, and the density scalars; the last column to
 //     finish (global ticket) writes Etot, Je, Nele.
+//     In stage 3 the last column to finish advances the step counter (the
+//     columns' first CTAs read it for the stage field until then).
 // A ticket is an atomic counter taken after a fence; the CTA that draws the
 // last number does the follow-up work.  Nothing waits on another CTA.
 #include "fft.cuh"
@@ -347,10 +349,11 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       a.colbuf[(size_t)c * 4 + 3] = si;
     }
   }
-  // stage 3 advances the step counter (one CTA); stages 1 and 2 finish here
-  if (a.mode == 3 && c == 0 && tid == 0) *a.it = *a.it + 1;
-  if (!obs) return;
-  // the last column to finish finalizes the observables (nothing waits on another CTA)
+  // stages 1 and 2 finish here.  Stage 3 advances the step counter, but the
+  // first CTA of every column reads it (the stage field A[it]): only the last
+  // column to finish, when every column has passed its ticket, may change it.
+  if (!obs && a.mode != 3) return;
+  // the last column to finish finalizes (nothing waits on another CTA)
   __syncthreads();
   if (tid == 0) {
     __threadfence();
@@ -360,7 +363,11 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   __syncthreads();
   if (last_s && warp == 0) {
     __threadfence();
-    small_finalize(a, rho_s, vh_s, N);
+    if (a.mode == 3) {
+      if (lane == 0) *a.it = *a.it + 1;
+    } else {
+      small_finalize(a, rho_s, vh_s, N);
+    }
     if (lane == 0) *a.ticket = 0u;
   }
 }

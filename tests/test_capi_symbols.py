@@ -56,6 +56,8 @@ def test_null_handles_are_rejected_without_gpu(built_lib):
     assert built_lib.mattohf_set_option(None, _capi.OPT_GRAPH, 1) == _capi.ERR_ARG
     assert built_lib.mattohf_batch_destroy(None) == _capi.OK
     assert built_lib.mattohf_batch_set_option(None, _capi.OPT_FOCK_DF64, 1) == _capi.ERR_ARG
+    assert built_lib.mattohf_autotune(None, 4, None, None) == _capi.ERR_ARG
+    assert built_lib.mattohf_batch_autotune(None, 4, None, None) == _capi.ERR_ARG
     h = ctypes.c_void_p()
     assert built_lib.mattohf_batch_create(0, None, ctypes.byref(h)) == _capi.ERR_ARG
 

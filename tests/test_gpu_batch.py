@@ -103,3 +103,38 @@ def test_batch_double_float_matches_single_runs(built_lib):
         assert np.max(np.abs(j - J[r])) <= 1e-12 * max(1.0, np.max(np.abs(j))), r
         assert np.max(np.abs(n - N[r])) <= 1e-12 * np.max(np.abs(n)), r
         assert np.max(np.abs(us - ub[r])) <= 1e-11 * np.max(np.abs(us)), r
+
+
+def test_batch_autotune_restores_state_and_keeps_results(built_lib):
+    """The batch autotuner restores every run's orbitals bitwise; every tile it
+    may pick (and the tuned one) gives the ensemble's results to rounding."""
+    from mattohf_gb300 import Batch, _capi
+    cfgs = _cfgs()
+    nt = 4
+    rng = np.random.default_rng(3)
+    A = 0.02 * rng.standard_normal((len(cfgs), nt))
+    Aave = np.concatenate([0.5 * A[:, :1], 0.5 * (A[:, 1:] + A[:, :-1])], axis=1)
+    dts = np.array([0.004, 0.003, 0.002, 0.004, 0.005])
+    with Batch(cfgs) as b:
+        u0 = []
+        for r in range(len(cfgs)):
+            b[r].Init_wf()
+            b[r].Gram_Schmidt()
+            u0.append(b[r].get_orbitals())
+        E0, J0, N0 = b.rk4_run(A, Aave, dts)
+        for r in range(len(cfgs)):
+            b[r].set_orbitals(u0[r])
+        res = b.autotune(steps=3)
+        assert res["sym_tile"] >= 1 and res["step_us"] > 0
+        for r in range(len(cfgs)):
+            assert np.array_equal(b[r].get_orbitals(), u0[r]), r
+        E, J, N = b.rk4_run(A, Aave, dts)
+        assert np.max(np.abs(E - E0)) <= 1e-13 * np.max(np.abs(E0))
+        assert np.max(np.abs(N - N0)) <= 1e-13 * np.max(np.abs(N0))
+        for tile in (1, 2, 4):
+            b.set_option(_capi.OPT_SYM_TILE, tile)
+            for r in range(len(cfgs)):
+                b[r].set_orbitals(u0[r])
+            E, J, N = b.rk4_run(A, Aave, dts)
+            assert np.max(np.abs(E - E0)) <= 1e-13 * np.max(np.abs(E0)), tile
+            assert np.max(np.abs(J - J0)) <= 1e-13 * max(1.0, np.max(np.abs(J0))), tile

@@ -424,3 +424,38 @@ def test_long_golden_run(small):
     print("golden 2000-step run, small=%d: " % small + ", ".join(f"{k} {v:.2e}" for k, v in err.items()))
     for k, v in err.items():
         assert v <= TOL_RT, (k, v)
+
+
+@pytest.mark.parametrize("NG,NK,NB", [(64, 8, 2), (128, 16, 2), (256, 8, 4)])
+def test_autotune_restores_state_and_keeps_results(NG, NK, NB):
+    """The autotuner times its candidates on the context's own orbitals, restores
+    them bitwise, and the tuned launch shapes give the same run (1e-12)."""
+    from mattohf_gb300 import Context, RunConfig, _capi
+    cfg = RunConfig(acell=10.0, NG=NG, NK=NK, NB=NB, NBocc=NB, Zeff=[2.0], alpha=[1.0], Rion=[0.5], Kion=[1])
+    A = 0.02 * np.sin(0.3 * np.arange(1, 9))
+    Aave = np.concatenate([0.5 * A[:1], 0.5 * (A[1:] + A[:-1])])
+    dt = 2e-4
+    with Context(cfg) as ctx:
+        ctx.Init_wf()
+        ctx.Gram_Schmidt()
+        u0 = ctx.get_orbitals()
+        E0, J0, N0 = ctx.rk4_run(A, Aave, dt)
+        ctx.set_orbitals(u0)
+        res = ctx.autotune(steps=8)
+        assert np.array_equal(ctx.get_orbitals(), u0)
+        assert res["sym_tile"] >= 1 and res["sym_tile"] & (res["sym_tile"] - 1) == 0
+        assert res["exchange_us"] > 0 and res["tiled_step_us"] > 0
+        if res["small_ctas"]:
+            assert res["fused_step_us"] > 0
+        E, J, N = ctx.rk4_run(A, Aave, dt)
+        assert rel(E, E0) <= 1e-12 and rel(N, N0) <= 1e-12
+        assert np.max(np.abs(J - J0)) <= 1e-12 * max(1.0, np.max(np.abs(J0)))
+        # every CTAs-per-column setting of the fused stages gives the same run,
+        # including grids far beyond one wave (the stage field is read by each
+        # column's first CTA while other columns finish)
+        for P in (1, 2, 3, 8, 12, 24):
+            ctx.set_option(_capi.OPT_SMALL_STAGES, 1)
+            ctx.set_option(_capi.OPT_SMALL_CTAS, P)
+            ctx.set_orbitals(u0)
+            E, J, N = ctx.rk4_run(A, Aave, dt)
+            assert rel(E, E0) <= 1e-12 and rel(N, N0) <= 1e-12, P
