@@ -652,9 +652,66 @@ def main():
                     help="profiling case: a 4-step adjoint on the differentiation shape (no timing)")
     ap.add_argument("--profile-small", action="store_true",
                     help="profiling case: 3 RK4 steps of the CPU-runnable shape through the fused stages (no timing)")
+    ap.add_argument("--profile-extras", action="store_true",
+                    help="profiling case: spectra, propagators, allocation-free exchange, double-float "
+                         "ensemble step, separate-launch adjoint and the peak probes (no timing)")
     ap.add_argument("--profile-batch", action="store_true",
                     help="profiling case: 2 batched steps of the first 32 runs of the ensemble mix (no timing)")
     args = ap.parse_args()
+    if args.profile_extras:
+        # the kernels outside the RK4 step: spectra at the exchange-dominated
+        # workload's sizes, the Taylor / predictor-corrector propagators, the
+        # allocation-free exchange, a double-float ensemble step, the separate-
+        # launch adjoint with the current objective, and the two peak probes
+        import ctypes as C
+        import dataclasses
+        import torch
+        from mattohf_gb300 import build, Batch, Context, RunConfig, _capi
+        from mattohf_gb300.driver import fourier
+        build.build()
+        lib = _capi.load()
+        pk = C.c_double()
+        lib.mattohf_diag_fp64_peak(0, C.byref(pk))
+        lib.mattohf_diag_dmma_peak(0, C.byref(pk))
+        cfg = dataclasses.replace(make_cfg(), NT=20000, Nomega=4000, omegaM=4.0)
+        nt = cfg.NT
+        t = cfg.dt * np.arange(nt)
+        J = 1e-3 * np.sin(0.05 * np.arange(nt))
+        Ef = 1e-2 * np.cos(0.05 * np.arange(nt))
+        for window in (False, True):
+            fourier(cfg, t, J, 0.0, Ef, Ef, window)
+        small = RunConfig(acell=10.0, NG=64, NK=8, NB=2, NBocc=2, Zeff=[2.0], alpha=[1.0], Rion=[0.5], Kion=[1])
+        with Context(small) as ctx:
+            ctx.Init_wf()
+            ctx.Gram_Schmidt()
+            for v in ("TE", "TEPC", "TEPC2"):
+                ctx.RT_TE_ubk(0.01, 0.002, v)
+            ctx.set_option(_capi.OPT_SMALL_STAGES, 0)
+            ctx.adjoint(0.01 * np.sin(0.3 * np.arange(1, 4)), 0.002, "current", ckpt_every=2)
+            _, vCq = ctx.coulomb()
+        noa = RunConfig(acell=9.0, NG=128, NK=8, NB=3, NBocc=2, Zeff=[2.0], alpha=[1.0], Rion=[0.5], Kion=[1])
+        with Context(noa) as ctx:
+            _, vCq = ctx.coulomb()
+        rng = np.random.default_rng(9)
+        u = rng.standard_normal((8, 3, 128, 2))
+        w = rng.standard_normal((8, 4, 128, 2))
+        d_vcq = torch.from_numpy(np.ascontiguousarray(vCq)).cuda()
+        d_u, d_w = torch.from_numpy(u).cuda(), torch.from_numpy(w).cuda()
+        d_out = torch.empty_like(d_w)
+        torch.cuda.synchronize()
+        lib.mattohf_fock_noalloc(128, 8, 3, 2, 4, d_vcq.data_ptr(), d_u.data_ptr(), d_w.data_ptr(),
+                                 d_out.data_ptr(), None)
+        torch.cuda.synchronize()
+        cfgs = [RunConfig(acell=10.0, NG=64, NK=k, NB=b, NBocc=b, Zeff=[2.0], alpha=[1.0], Rion=[0.5],
+                          Kion=[1]) for k, b in [(8, 2), (16, 1), (4, 4)]]
+        with Batch(cfgs) as bt:
+            for r in range(len(cfgs)):
+                bt[r].Init_wf()
+                bt[r].Gram_Schmidt()
+            bt.set_option(_capi.OPT_FOCK_DF64, 1)
+            A = np.full((len(cfgs), 2), 0.01)
+            bt.rk4_run(A, A, 0.002)
+        return
     if args.profile_small:
         from mattohf_gb300 import build, Context, RunConfig, _capi
         build.build()

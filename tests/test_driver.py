@@ -133,6 +133,20 @@ def test_fourier_matches_oracle(built_lib):
     w2, JF2, _, _ = O.window_fourier_tr(oc, t, J, 0.3, E, A)
     fw = fourier(cfg, t, J, 0.3, E, A, window=True)
     assert np.max(np.abs(fw[:, 1] + 1j * fw[:, 2] - JF2)) <= 1e-12 * np.max(np.abs(JF2))
+    # a time grid that is not uniform takes a sincos per term instead of the
+    # rotation recurrence; longer series span several time chunks
+    for tt in (t + 1e-3 * rng.standard_normal(cfg.NT), None):
+        if tt is None:
+            cfg2 = dataclasses.replace(cfg, NT=3000)
+            tt = cfg2.dt * np.arange(cfg2.NT)
+            J3, E3, A3 = rng.standard_normal((3, cfg2.NT))
+        else:
+            cfg2, J3, E3, A3 = cfg, J, E, A
+        oc2 = O.Config(**{f.name: getattr(cfg2, f.name) for f in dataclasses.fields(O.Config)})
+        _, JF3, EF3, AF3, _, _ = O.fourier_tr(oc2, tt, J3, 0.3, E3, A3)
+        f3 = fourier(cfg2, tt, J3, 0.3, E3, A3, window=False)
+        for col, ref in ((1, JF3), (3, EF3), (5, AF3)):
+            assert np.max(np.abs(f3[:, col] + 1j * f3[:, col + 1] - ref)) <= 1e-12 * np.max(np.abs(ref))
 
 
 # ---------------------------------------------------------------------------
