@@ -578,13 +578,13 @@ bool use_small(const mattohf_ctx* ctx) {
 int small_ctas_per_column(const mattohf_ctx* ctx) {
   const int ncols = ctx->NK * ctx->NB, M = ctx->NK * ctx->NBocc;
   const int pair_teams = small_pair_teams(ctx->NG);   // 6 warps' teams
-  if (ctx->opt_small_ctas > 0)  // set (or tuned): at least one round of all pair teams, at most M
-    return std::max(std::max(1, (M + pair_teams - 1) / pair_teams), std::min(ctx->opt_small_ctas, std::max(1, M)));
+  if (ctx->opt_small_ctas > 0)  // set (or tuned): at most M and a cluster's CTAs
+    return std::max(1, std::min(std::min(ctx->opt_small_ctas, std::max(1, M)), kSmallMaxCtas));
   const int two_warps = std::max(1, pair_teams / 3);
   int P = (M + two_warps - 1) / two_warps;
   if (ncols * P > ctx->nsm) P = std::max(1, ctx->nsm / ncols);
   P = std::max(P, (M + pair_teams - 1) / pair_teams);  // one round of all pair teams at most
-  return std::max(1, std::min(P, M));
+  return std::max(1, std::min(std::min(P, M), kSmallMaxCtas));  // one cluster per column
 }
 
 // CTAs per column of the fused reverse stages: one round of the pass teams
@@ -1477,8 +1477,8 @@ extern "C" int mattohf_autotune(mattohf_ctx* ctx, int steps, int* out, double* u
   const bool fused_ok = small_stage_supported(NG) && !ctx->opt_df && !ctx->opt_timing && ctx->NBocc > 0;
   if (rc == MATTOHF_OK && fused_ok) {
     const int ncols = NK * NB, M = NK * ctx->NBocc;
-    const int lo = std::max(1, (M + small_pair_teams(NG) - 1) / small_pair_teams(NG));
-    const int hi = std::max(lo, std::min(M, std::max(1, 2 * ctx->nsm / ncols)));
+    const int lo = std::min(kSmallMaxCtas, std::max(1, (M + small_pair_teams(NG) - 1) / small_pair_teams(NG)));
+    const int hi = std::min(kSmallMaxCtas, std::max(lo, std::min(M, std::max(1, 2 * ctx->nsm / ncols))));
     ctx->opt_small = 1;
     ctx->opt_small_ctas = 0;
     std::vector<int> cand{small_ctas_per_column(ctx)};

@@ -221,6 +221,9 @@ struct SmallStageArgs {
   unsigned* ticket;         // [1 + ncols]: global, then per-column completion counters
   double* out_obs;          // mode 4: [7] Etot, Ekin, Eion, EH, Ex, Je, Nele
 };
+// CTAs per column of the fused stages: one thread-block cluster per column
+// (the portable cluster size)
+constexpr int kSmallMaxCtas = 8;
 cudaError_t launch_small_stage(int NG, const SmallStageArgs& a, cudaStream_t s);
 bool small_stage_supported(int NG);
 int small_pair_teams(int NG);

@@ -3,30 +3,36 @@
 // For small grids and few orbitals every kernel of the general path is
 // latency-bound, and a step of about 29 dependent launches costs more than the
 // arithmetic.  Here one launch does a whole RK4 stage (src/RT_calculation.f90:
-// 154-173).  Output column c = (k, b) is served by P CTAs (c, chunk):
+// 154-173).  Output column c = (k, b) is served by P CTAs (c, chunk) that form
+// one thread-block cluster:
 //   * the column's first CTA computes the density of the stage input
 //     (F:55-71): all its threads first sum |u|^2 over slices of the occupied
 //     orbitals (in ik -> ib order within a slice, the uniform occupation
-//     applied once); then its last warp adds the slices, forms the Hartree
-//     potential (F:147-162) and stores both for the column's last CTA.  One
-//     warp alone would queue about 4 us of FP64 work on its SM sub-partition
-//     for the sum, and that backlog held up the whole CTA after the phase;
+//     applied once); then its last warp adds the slices and forms the Hartree
+//     potential (F:147-162).  One warp alone would queue about 4 us of FP64
+//     work on its SM sub-partition for the sum, and that backlog held up the
+//     whole CTA after the phase;
 //   * the other warps apply the exchange of column c against the CTA's chunk of
 //     the occupied orbitals (F:237-261, ordered pairs, no symmetry), one pair
-//     per team, and the CTA writes its partial sum;
+//     per team, and the CTA keeps its partial sum in shared memory;
 //   * in the column's first CTA, warp 6 does the kinetic transform of the
-//     column (F:212-234); the last CTA of the column adds the P partials in
-//     chunk order, then forms h w and the stage's RK4 update element by element
-//     into a buffer that is never the stage input;
+//     column (F:212-234);
+//   * after a cluster barrier each CTA of the column adds the P partials in
+//     chunk order for its share of the grid points (distributed shared
+//     memory), takes vH and T_A w from the first CTA the same way, and forms
+//     h w and the stage's RK4 update element by element, into a buffer that is
+//     never the stage input;
 //   * stage 0 (or the closing pass, mode 4) also gives the observables of its
 //     input, i.e. of the previous step (F:74-119, F:165-183, F:289-318): Ekin
 //     and Je from warp 6's forward transform at the previous step's field,
-//     <u|F u> from the last CTA, and the density scalars; the last column to
-//     finish (global ticket) writes Etot, Je, Nele.
+//     <u|F u> from the CTAs' shares, and the density scalars; the last column
+//     to finish (global ticket) writes Etot, Je, Nele.
 //     In stage 3 the last column to finish advances the step counter (the
 //     columns' first CTAs read it for the stage field until then).
 // A ticket is an atomic counter taken after a fence; the CTA that draws the
-// last number does the follow-up work.  Nothing waits on another CTA.
+// last number does the follow-up work.  No CTA waits on another column.
+#include <cooperative_groups.h>
+
 #include "fft.cuh"
 #include "internal.h"
 
@@ -48,8 +54,8 @@ struct SmallLayout {
   // warps 0..5 apply exchange pairs; in the column's first CTA warp 6 does the
   // kinetic transform and warp 7 the density and Hartree potential
   static constexpr int PAIR_TEAMS = (kSmallWarps - 2) * PW;
-  // tw[N], bufs[NTEAM][N], F[N] (double2); rho[N], vh[N] (double)
-  static constexpr size_t bytes = sizeof(double2) * (size_t)N * (2 + NTEAM) + sizeof(double) * 2 * (size_t)N;
+  // tw[N], bufs[NTEAM][N], F[N] (double2); rho[N], vh[N] (double); K[N] (double2)
+  static constexpr size_t bytes = sizeof(double2) * (size_t)N * (3 + NTEAM) + sizeof(double) * 2 * (size_t)N;
 };
 
 // The global last CTA of an observable stage: the observables of the stage
@@ -107,20 +113,23 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
   constexpr int NTEAM = SmallLayout<N>::NTEAM;
   constexpr int PAIR_TEAMS = SmallLayout<N>::PAIR_TEAMS;
+  namespace cg = cooperative_groups;
   extern __shared__ double2 sm2[];
   double2* tw_s = sm2;                     // N
   double2* bufs = tw_s + N;                // NTEAM * N
-  double2* F_s = bufs + NTEAM * N;         // N
+  double2* F_s = bufs + NTEAM * N;         // N: this CTA's exchange partial
   double* rho_s = reinterpret_cast<double*>(F_s + N);
   double* vh_s = rho_s + N;
+  double2* K_s = reinterpret_cast<double2*>(vh_s + N);  // N: T_A w (the column's first CTA)
   __shared__ int last_s;
   __shared__ double red_s[2][kSmallWarps];
+  __shared__ double ex_s[2];               // this CTA's share of <w|F>
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tl = lane % T, team = warp * PW + lane / T;
   double2* buf = bufs + team * N;
   const int ncols = a.nk * a.nb;
   const int c = blockIdx.x / a.P;          // output column (k, b)
-  const int chunk = blockIdx.x % a.P;
+  const int chunk = blockIdx.x % a.P;      // rank in the column's cluster
   const int kr = c / a.nb, ib = c % a.nb;
   const int M = a.nk * a.nbocc;
   const int ppc = (M + a.P - 1) / a.P;     // pairs per CTA
@@ -128,9 +137,6 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   const bool occupied = ib < a.nbocc;
   const bool obs = a.mode == 0 || a.mode == 4;
   const double2* wcol = a.u + (size_t)c * N;
-  // per-column results of the first CTA, after the partials
-  double2* rv_g = a.part + (size_t)ncols * a.P * N + (size_t)c * N;         // (rho, vH)
-  double2* kin_g = a.part + (size_t)ncols * (a.P + 1) * N + (size_t)c * N;  // T_A w
 
   for (int i = tid; i < N; i += kSmallThreads) tw_s[i] = a.tw[i];
   // Launched as a programmatic dependent of the previous stage: everything
@@ -142,7 +148,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   asm volatile("griddepcontrol.launch_dependents;");
   // density, first part: sum of |u|^2 over slice j of the occupied orbitals at
   // point ig, one (j, ig) per thread.  F_s, rho_s and vh_s (4N contiguous
-  // doubles) are free until the epilogue and hold the slices.
+  // doubles) are free during the first phase and hold the slices.
   constexpr int NSUB = (kSmallThreads / N) < 4 ? (kSmallThreads / N) : 4;
   double* dslice = reinterpret_cast<double*>(F_s);  // [NSUB][N]
   if (chunk == 0 && tid < NSUB * N) {
@@ -184,8 +190,6 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
 #pragma unroll
         for (int e = 0; e < E; ++e) vh_s[TM::pos(tl, e)] = x[e].x / (double)N;
       }
-      __syncwarp();
-      for (int ig = lane; ig < N; ig += 32) rv_g[ig] = make_double2(rho_s[ig], vh_s[ig]);
     }
   } else if (warp == kSmallWarps - 2) {
     if (chunk == 0) {
@@ -227,7 +231,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
         fft_team<N, +1>(x, buf, tw_s, tl);
         if (lane < T) {
 #pragma unroll
-          for (int e = 0; e < E; ++e) kin_g[TM::pos(tl, e)] = x[e];
+          for (int e = 0; e < E; ++e) K_s[TM::pos(tl, e)] = x[e];
         }
       }
     }
@@ -260,78 +264,61 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     for (int e = 0; e < E; ++e) buf[TM::pos(tl, e)] = make_double2(0.0, 0.0);
   }
   __syncthreads();
-  // this CTA's partial (pair teams in order) -> part[c][chunk]
-  double2* mine = a.part + ((size_t)c * a.P + chunk) * N;
+  // this CTA's partial (pair teams in order), kept in its shared memory
   for (int i = tid; i < N; i += kSmallThreads) {
     double2 f = bufs[i];
     for (int t2 = 1; t2 < PAIR_TEAMS; ++t2) f = cadd(f, bufs[(size_t)t2 * N + i]);
-    mine[i] = f;
-  }
-  __threadfence();
-  __syncthreads();
-  if (tid == 0) {
-    __threadfence();
-    const unsigned t = atomicAdd(a.ticket + 1 + c, 1u);
-    last_s = (t == (unsigned)a.P - 1) ? 1 : 0;
-    if (last_s) {
-      __threadfence();      // acquire: the other CTAs' partials, read below through L2
-      a.ticket[1 + c] = 0u;
-    }
-  }
-  __syncthreads();
-  if (!last_s) return;
-  // ---- the last CTA of column c: ordered sum of the P partials
-  const double2* cp = a.part + (size_t)c * a.P * N;
-  for (int i = tid; i < N; i += kSmallThreads) {
-    double2 f = __ldcg(cp + i);
-#pragma unroll 16
-    for (int ch = 1; ch < a.P; ++ch) f = cadd(f, __ldcg(cp + (size_t)ch * N + i));
     F_s[i] = f;
-    const double2 rv = __ldcg(rv_g + i);  // written by the column's first CTA
-    rho_s[i] = rv.x;
-    vh_s[i] = rv.y;
   }
-  // h w and the stage's RK4 update, element by element over all threads (the
-  // transforms were done in the first phase), and <w|F> for the observables
+  // the column's P CTAs form a cluster: after this barrier every CTA reads the
+  // P partials and the first CTA's vH and T_A w through distributed shared
+  // memory, and does h w and the RK4 update for its own share of the grid
+  cg::cluster_group cluster = cg::this_cluster();
+  cluster.sync();
+  const int per = (N + a.P - 1) / a.P;
+  const int q = chunk * per + tid;
   double exr = 0.0, exi = 0.0;
   bool bad = false;
-  for (int q = tid; q < N; q += kSmallThreads) {
+  if (tid < per && q < N) {
+    double2 f = cluster.map_shared_rank(F_s, 0)[q];
+    for (int r = 1; r < a.P; ++r) f = cadd(f, cluster.map_shared_rank(F_s, r)[q]);
     const size_t o = (size_t)c * N + q;
     const double2 wq = wcol[q];
-    const double2 f = F_s[q];
     if (obs) {
-      exr += wq.x * f.x + wq.y * f.y;
-      exi += wq.x * f.y - wq.y * f.x;
+      exr = wq.x * f.x + wq.y * f.y;
+      exi = wq.x * f.y - wq.y * f.x;
     }
-    if (a.mode == 4) continue;
-    const double v = vh_s[q] + a.vion[q];
-    const double2 kin = __ldcg(kin_g + q);  // written by the column's first CTA
-    double2 h = make_double2(kin.x + v * wq.x, kin.y + v * wq.y);
-    h = cadd(h, f);
-    const double2 k = make_double2(h.y, -h.x);  // -i h
-    const double2 u0 = a.u0[o];
-    double2 nx;
-    if (a.mode < 3) {
-      const double cdt = (a.mode == 2) ? a.dt : 0.5 * a.dt;
-      nx = make_double2(u0.x + cdt * k.x, u0.y + cdt * k.y);
-      a.kbuf[a.mode][o] = k;
-      a.out[o] = nx;
-    } else {
-      const double2 k0 = a.kbuf[0][o], k1 = a.kbuf[1][o], k2 = a.kbuf[2][o];
-      double sx = k0.x + 2.0 * k1.x, sy = k0.y + 2.0 * k1.y;
-      sx = sx + 2.0 * k2.x;
-      sy = sy + 2.0 * k2.y;
-      sx = sx + k.x;
-      sy = sy + k.y;
-      sx = sx * a.dt / 6.0;
-      sy = sy * a.dt / 6.0;
-      nx = make_double2(u0.x + sx, u0.y + sy);
-      a.u0[o] = nx;  // this element only, read just above by this thread
+    if (a.mode != 4) {
+      const double v = cluster.map_shared_rank(vh_s, 0)[q] + a.vion[q];
+      const double2 kin = cluster.map_shared_rank(K_s, 0)[q];
+      double2 h = make_double2(kin.x + v * wq.x, kin.y + v * wq.y);
+      h = cadd(h, f);
+      const double2 k = make_double2(h.y, -h.x);  // -i h
+      const double2 u0 = a.u0[o];
+      double2 nx;
+      if (a.mode < 3) {
+        const double cdt = (a.mode == 2) ? a.dt : 0.5 * a.dt;
+        nx = make_double2(u0.x + cdt * k.x, u0.y + cdt * k.y);
+        a.kbuf[a.mode][o] = k;
+        a.out[o] = nx;
+      } else {
+        const double2 k0 = a.kbuf[0][o], k1 = a.kbuf[1][o], k2 = a.kbuf[2][o];
+        double sx = k0.x + 2.0 * k1.x, sy = k0.y + 2.0 * k1.y;
+        sx = sx + 2.0 * k2.x;
+        sy = sy + 2.0 * k2.y;
+        sx = sx + k.x;
+        sy = sy + k.y;
+        sx = sx * a.dt / 6.0;
+        sy = sy * a.dt / 6.0;
+        nx = make_double2(u0.x + sx, u0.y + sy);
+        a.u0[o] = nx;  // this element only, read just above by this thread
+      }
+      bad = !(isfinite(nx.x) && isfinite(nx.y));
     }
-    bad |= !(isfinite(nx.x) && isfinite(nx.y));
   }
   if (bad && a.nonfinite) *a.nonfinite = 1;
   if (obs) {
+    // <w|F>: this CTA's elements in thread order (warp tree, then warps in order)
     exr = small_warp_sum(exr);
     exi = small_warp_sum(exi);
     if (lane == 0) {
@@ -339,21 +326,35 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       red_s[1][warp] = exi;
     }
     __syncthreads();
-    if (tid == 0 && occupied) {
+    if (tid == 0) {
       double sr = red_s[0][0], si = red_s[1][0];
       for (int w2 = 1; w2 < kSmallWarps; ++w2) {
         sr += red_s[0][w2];
         si += red_s[1][w2];
       }
+      ex_s[0] = sr;
+      ex_s[1] = si;
+    }
+  }
+  // every read of another CTA's shared memory above is done after this barrier
+  cluster.sync();
+  if (obs) {
+    if (chunk == 0 && tid == 0 && occupied) {
+      double sr = ex_s[0], si = ex_s[1];
+      for (int r = 1; r < a.P; ++r) {
+        sr += cluster.map_shared_rank(ex_s, r)[0];
+        si += cluster.map_shared_rank(ex_s, r)[1];
+      }
       a.colbuf[(size_t)c * 4 + 2] = sr;
       a.colbuf[(size_t)c * 4 + 3] = si;
     }
+    cluster.sync();  // the other CTAs stay until their shares are read
   }
-  // stages 1 and 2 finish here.  Stage 3 advances the step counter, but the
+  // stages 1 and 2 end here.  Stage 3 advances the step counter, but the
   // first CTA of every column reads it (the stage field A[it]): only the last
-  // column to finish, when every column has passed its ticket, may change it.
-  if (!obs && a.mode != 3) return;
-  // the last column to finish finalizes (nothing waits on another CTA)
+  // column to finish, when every column has passed this point, may change it.
+  if ((!obs && a.mode != 3) || chunk != 0) return;
+  // the last column to finish finalizes (nothing waits on another column)
   __syncthreads();
   if (tid == 0) {
     __threadfence();
@@ -379,11 +380,15 @@ static cudaError_t small_impl(const SmallStageArgs& a, cudaStream_t s) {
   cfg.blockDim = dim3(kSmallThreads);
   cfg.dynamicSmemBytes = SmallLayout<N>::bytes;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
+  attr[1].id = cudaLaunchAttributeClusterDimension;  // one cluster per output column
+  attr[1].val.clusterDim.x = a.P;
+  attr[1].val.clusterDim.y = 1;
+  attr[1].val.clusterDim.z = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = 2;
   return cudaLaunchKernelEx(&cfg, k_small_stage<N>, a);
 }
 
@@ -407,7 +412,7 @@ int small_pair_teams(int NG) {
 }
 
 cudaError_t launch_small_stage(int NG, const SmallStageArgs& a, cudaStream_t s) {
-  if (a.P < 1) return cudaErrorInvalidValue;
+  if (a.P < 1 || a.P > kSmallMaxCtas) return cudaErrorInvalidValue;
   switch (NG) {
     case 16: return small_impl<16>(a, s);
     case 32: return small_impl<32>(a, s);
