@@ -564,11 +564,12 @@ int enq_rk4(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt,
 bool use_small(const mattohf_ctx* ctx) {
   if (ctx->opt_small == 0 || ctx->opt_df || ctx->opt_timing || !small_stage_supported(ctx->NG)) return false;
   if (ctx->opt_small == 1) return true;
-  // measured on GB300 (us per step, fused vs tiled): NG=64 NK=8 Nocc=2 100 vs 199;
-  // NG=128 NK=16 Nocc=2 215 vs 243; NG=64 NK=16 Nocc=4 311 vs 353; NG=64 NK=32
-  // Nocc=2 310 vs 350 (M^2 NG = 2^18); NG=128 NK=32 Nocc=2 529 vs 402 (2^19)
+  // measured on GB300 with mattohf_autotune (us per step, fused vs tiled):
+  // NG=128 NK=16 Nocc=2 126 vs 238 and NG=128 NK=8 Nocc=4 125 vs 242 (M^2 NG =
+  // 2^17); NG=64 NK=16 Nocc=4 196 vs 158, NG=64 NK=32 Nocc=2 196 vs 159 (2^18);
+  // NG=256 NK=8 Nocc=4 249 vs 262 (2^18); NG=128 NK=32 Nocc=2 451 vs 283 (2^19)
   const size_t M = (size_t)ctx->NK * ctx->NBocc;
-  return ctx->NK * ctx->NB <= 64 && M * M * ctx->NG <= ((size_t)1 << 18);
+  return ctx->NK * ctx->NB <= 64 && M * M * ctx->NG <= ((size_t)1 << 17);
 }
 
 // CTAs per column.  A warp's teams run their pairs in the same instructions,
