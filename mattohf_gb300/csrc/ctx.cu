@@ -136,6 +136,7 @@ struct mattohf_ctx {
   double last_adj_ms = 0, last_adj_fwd_ms = 0;
   // graph of one RK4 step
   cudaGraphExec_t step_exec = nullptr;
+  cudaGraphExec_t multi_exec = nullptr;  // kGraphSteps steps in one graph
   double step_dt = 0;
   // timing
   double last_run_ms = 0, last_fock_ms = 0;
@@ -306,6 +307,9 @@ int timed_end(mattohf_ctx* ctx) {
   ctx->fock_event_used++;
   return MATTOHF_OK;
 }
+
+// RK4 steps captured in one graph for mattohf_rk4_run (divides 256)
+constexpr int kGraphSteps = 8;
 
 int sym_tile(const mattohf_ctx* ctx) {
   return ctx->opt_tile > 0 ? ctx->opt_tile : choose_sym_tile(ctx->NG, ctx->NK * ctx->NBocc);
@@ -694,6 +698,10 @@ void destroy_graph(mattohf_ctx* c) {
   if (c->step_exec) {
     cudaGraphExecDestroy(c->step_exec);
     c->step_exec = nullptr;
+  }
+  if (c->multi_exec) {
+    cudaGraphExecDestroy(c->multi_exec);
+    c->multi_exec = nullptr;
   }
 }
 
@@ -1256,23 +1264,30 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
   CK(cudaMemsetAsync(ctx->d_ticket, 0, sizeof(unsigned) * (1 + (size_t)ctx->NK * ctx->NB), ctx->st));
   if (use_graph && (!ctx->step_exec || ctx->step_dt != dt || ctx->step_small != small)) {
     destroy_graph(ctx);
-    cudaGraph_t g;
-    ctx->capturing = true;
-    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
-    int rc = MATTOHF_OK;
-    if (small) {
-      rc = enq_small_step(ctx, fm, fave, fcur, dt);
-    } else {
-      rc = enq_rk4(ctx, fm, fave, fcur, dt, ctx->d_sE);
-      if (rc == MATTOHF_OK) rc = enq_observables(ctx, ctx->d_u, fcur, true, true);
+    // one step, and kGraphSteps steps in one graph: the launch of a graph is a
+    // full dependency, while within it consecutive stages overlap
+    // (programmatic dependent launches)
+    for (int steps : {1, kGraphSteps}) {
+      cudaGraph_t g;
+      ctx->capturing = true;
+      CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+      int rc = MATTOHF_OK;
+      for (int s = 0; s < steps && rc == MATTOHF_OK; ++s) {
+        if (small) {
+          rc = enq_small_step(ctx, fm, fave, fcur, dt);
+        } else {
+          rc = enq_rk4(ctx, fm, fave, fcur, dt, ctx->d_sE);
+          if (rc == MATTOHF_OK) rc = enq_observables(ctx, ctx->d_u, fcur, true, true);
+        }
+      }
+      cudaError_t ec = cudaStreamEndCapture(ctx->st, &g);
+      ctx->capturing = false;
+      if (rc != MATTOHF_OK) return rc;
+      CK(ec);
+      cudaError_t ei = cudaGraphInstantiate(steps == 1 ? &ctx->step_exec : &ctx->multi_exec, g, 0);
+      cudaGraphDestroy(g);
+      CK(ei);
     }
-    cudaError_t ec = cudaStreamEndCapture(ctx->st, &g);
-    ctx->capturing = false;
-    if (rc != MATTOHF_OK) return rc;
-    CK(ec);
-    cudaError_t ei = cudaGraphInstantiate(&ctx->step_exec, g, 0);
-    cudaGraphDestroy(g);
-    CK(ei);
     ctx->step_dt = dt;
     ctx->step_small = small;
   }
@@ -1305,7 +1320,10 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
       CK(cudaMemsetAsync(ctx->d_flush, it & 0xff, (size_t)ctx->opt_flush, ctx->st));
       CK(cudaEventRecord(ctx->step_events[2 * it], ctx->st));
     }
-    if (use_graph) {
+    if (use_graph && !stepwise && it % kGraphSteps == 0 && nt - it >= kGraphSteps) {
+      CK(cudaGraphLaunch(ctx->multi_exec, ctx->st));  // steps it .. it + kGraphSteps - 1
+      it += kGraphSteps - 1;
+    } else if (use_graph) {
       CK(cudaGraphLaunch(ctx->step_exec, ctx->st));
     } else if (small) {
       CKR(enq_small_step(ctx, fm, fave, fcur, dt));
@@ -1315,6 +1333,7 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
     }
     if (stepwise) CK(cudaEventRecord(ctx->step_events[2 * it + 1], ctx->st));
     // bounded detection of a blow-up: poll the flag every 256 steps
+    // (kGraphSteps divides 256, so a multi-step launch ends on each check)
     if ((it & 255) == 255 && it + 1 < nt) {
       CK(cudaMemcpyAsync(&flag, ctx->d_int + 1, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
       CK(cudaStreamSynchronize(ctx->st));
