@@ -579,13 +579,16 @@ bool use_small(const mattohf_ctx* ctx) {
 // CTAs per column.  A warp's teams run their pairs in the same instructions,
 // and a lone warp's FP64 work is bound by its SM sub-partition: so each CTA
 // takes as many pairs as the teams of two warps (on two sub-partitions) hold,
-// unless that needs more CTAs than there are multiprocessors.
+// at least 4, unless that needs more CTAs than there are multiprocessors.
 int small_ctas_per_column(const mattohf_ctx* ctx) {
   const int ncols = ctx->NK * ctx->NB, M = ctx->NK * ctx->NBocc;
   const int pair_teams = small_pair_teams(ctx->NG);   // 6 warps' teams
   if (ctx->opt_small_ctas > 0)  // set (or tuned): at most M and a cluster's CTAs
     return std::max(1, std::min(std::min(ctx->opt_small_ctas, std::max(1, M)), kSmallMaxCtas));
-  const int two_warps = std::max(1, pair_teams / 3);
+  // two warps' teams, and at least 4 pairs (with one team per warp, as in the
+  // 32-lane transforms, fewer pairs per CTA only add CTAs: measured with
+  // mattohf_autotune at NG=64, NK=8, Nocc=2)
+  const int two_warps = std::max(4, pair_teams / 3);
   int P = (M + two_warps - 1) / two_warps;
   if (ncols * P > ctx->nsm) P = std::max(1, ctx->nsm / ncols);
   P = std::max(P, (M + pair_teams - 1) / pair_teams);  // one round of all pair teams at most

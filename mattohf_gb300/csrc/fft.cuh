@@ -90,11 +90,11 @@ struct InTwiddled {
 };
 
 // X_e = f[pos(e)] * x_e for a real per-point factor f (a kernel in G space)
-template <int N>
+template <int N, int L = 0>
 struct InScaled;
 
 // X_e = a[pos(e)] * conj(b[pos(e)]) for two columns read from memory (pair densities)
-template <int N>
+template <int N, int L = 0>
 struct InConjProduct;
 
 template <int R, int DIR> struct Dft;
@@ -162,23 +162,39 @@ template <int DIR> struct Dft<8, DIR> {
   __device__ __forceinline__ static void run(double2* x) { run_from(InPlain{x}, 0, x); }
 };
 
-// Pass plans: radices with equal first and last radix.
-template <int N> struct FftPlan;
-template <> struct FftPlan<16>  { static constexpr int NP = 2; static constexpr int R[4] = {4, 4, 0, 0}; };
-template <> struct FftPlan<32>  { static constexpr int NP = 3; static constexpr int R[4] = {4, 2, 4, 0}; };
+// Pass plans: radices with equal first and last radix (NP passes, NP <= 8).
+// L = 0: the throughput plans, used by every kernel unless it asks otherwise.
+template <int N, int L = 0> struct FftPlan;
+template <> struct FftPlan<16, 0>  { static constexpr int NP = 2; static constexpr int R[8] = {4, 4}; };
+template <> struct FftPlan<32, 0>  { static constexpr int NP = 3; static constexpr int R[8] = {4, 2, 4}; };
 // N = 64 takes three radix-4 passes on 16 lanes rather than two radix-8 passes
 // on 8: 3 % more FP64 instructions in total, but half as many per lane.  Each
 // FP64 warp instruction occupies an SM sub-partition for ~64 cycles, so the
 // small grids, which run few transforms at a time, finish a transform in about
 // half the time.
-template <> struct FftPlan<64>  { static constexpr int NP = 3; static constexpr int R[4] = {4, 4, 4, 0}; };
-template <> struct FftPlan<128> { static constexpr int NP = 3; static constexpr int R[4] = {4, 8, 4, 0}; };
-template <> struct FftPlan<256> { static constexpr int NP = 3; static constexpr int R[4] = {8, 4, 8, 0}; };
-template <> struct FftPlan<512> { static constexpr int NP = 3; static constexpr int R[4] = {8, 8, 8, 0}; };
+template <> struct FftPlan<64, 0>  { static constexpr int NP = 3; static constexpr int R[8] = {4, 4, 4}; };
+template <> struct FftPlan<128, 0> { static constexpr int NP = 3; static constexpr int R[8] = {4, 8, 4}; };
+template <> struct FftPlan<256, 0> { static constexpr int NP = 3; static constexpr int R[8] = {8, 4, 8}; };
+template <> struct FftPlan<512, 0> { static constexpr int NP = 3; static constexpr int R[8] = {8, 8, 8}; };
+// L = 1: latency plans for kernels that run few transforms at a time (the
+// fused small-problem stages): radix-2 passes with two values per lane, so a
+// warp's dependent FP64 chain is about half that of the L = 0 plan for a few
+// percent more instructions in total.  Sizes without one use the L = 0 plan.
+template <int N> struct FftPlan<N, 1> : FftPlan<N, 0> {};
+template <> struct FftPlan<16, 1> { static constexpr int NP = 4; static constexpr int R[8] = {2, 2, 2, 2}; };
+template <> struct FftPlan<32, 1> { static constexpr int NP = 5; static constexpr int R[8] = {2, 2, 2, 2, 2}; };
+template <> struct FftPlan<64, 1> { static constexpr int NP = 6; static constexpr int R[8] = {2, 2, 2, 2, 2, 2}; };
 
-template <int N> struct Team {
-  static constexpr int R0 = FftPlan<N>::R[0];
-  static constexpr int RMAX = FftPlan<N>::R[1] > R0 ? FftPlan<N>::R[1] : R0;
+template <int N, int L>
+constexpr int fft_max_radix() {
+  int m = 0;
+  for (int p = 0; p < FftPlan<N, L>::NP; ++p) m = FftPlan<N, L>::R[p] > m ? FftPlan<N, L>::R[p] : m;
+  return m;
+}
+
+template <int N, int L = 0> struct Team {
+  static constexpr int R0 = FftPlan<N, L>::R[0];
+  static constexpr int RMAX = fft_max_radix<N, L>();
   // lanes per transform: every lane owns >= 1 butterfly in every pass
   static constexpr int T = (N / RMAX) < 32 ? (N / RMAX) : 32;
   static constexpr int PER = (N / R0) / T;     // butterflies per lane, first/last pass
@@ -190,26 +206,26 @@ template <int N> struct Team {
   __device__ __forceinline__ static int pos(int tl, int e) { return pos(tl, e / R0, e % R0); }
 };
 
-template <int N>
+template <int N, int L>
 struct InScaled {
   const double2* x;
   const double* f;  // global memory, read-only for the kernel's lifetime
   int tl;
   __device__ __forceinline__ void pair(int i, int j, double2& s, double2& d) const {
-    const double fi = __ldg(f + Team<N>::pos(tl, i)), fj = __ldg(f + Team<N>::pos(tl, j));
+    const double fi = __ldg(f + Team<N, L>::pos(tl, i)), fj = __ldg(f + Team<N, L>::pos(tl, j));
     const double2 t = make_double2(fi * x[i].x, fi * x[i].y);
     s = make_double2(fma(fj, x[j].x, t.x), fma(fj, x[j].y, t.y));
     d = make_double2(fma(-fj, x[j].x, t.x), fma(-fj, x[j].y, t.y));
   }
 };
 
-template <int N>
+template <int N, int L>
 struct InConjProduct {
   const double2* a;
   const double2* b;
   int tl;
   __device__ __forceinline__ void pair(int i, int j, double2& s, double2& d) const {
-    const int qi = Team<N>::pos(tl, i), qj = Team<N>::pos(tl, j);
+    const int qi = Team<N, L>::pos(tl, i), qj = Team<N, L>::pos(tl, j);
     const double2 t = cmulc(a[qi], b[qi]);
     s = cmaddc(a[qj], b[qj], t);
     d = cmirror(t, s);
@@ -248,15 +264,26 @@ __device__ __forceinline__ void fft_mid_pass(double2* buf, const double2* __rest
   __syncwarp();
 }
 
-// Transform the input policy's values X (register slots at Team<N>::pos) into
-// x.  buf: N double2 of team-private shared memory; tw: N forward twiddles
-// exp(-2 pi i m / N).
-template <int N, int DIR, class In>
-__device__ __forceinline__ void fft_team_in(const In& in, double2 (&x)[Team<N>::E], double2* buf,
+// The middle passes P = 1 .. NP-2 of plan (N, L); NS is the product of the
+// radices before pass P.
+template <int N, int L, int DIR, int T, int P, int NS>
+__device__ __forceinline__ void fft_mid_passes(double2* buf, const double2* __restrict__ tw, int tl) {
+  if constexpr (P < FftPlan<N, L>::NP - 1) {
+    constexpr int R = FftPlan<N, L>::R[P];
+    fft_mid_pass<N, R, NS, DIR, T>(buf, tw, tl);
+    fft_mid_passes<N, L, DIR, T, P + 1, NS * R>(buf, tw, tl);
+  }
+}
+
+// Transform the input policy's values X (register slots at Team<N, L>::pos)
+// into x.  buf: N double2 of team-private shared memory; tw: N forward
+// twiddles exp(-2 pi i m / N).
+template <int N, int DIR, int L = 0, class In>
+__device__ __forceinline__ void fft_team_in(const In& in, double2 (&x)[Team<N, L>::E], double2* buf,
                                             const double2* __restrict__ tw, int tl) {
-  using TM = Team<N>;
-  constexpr int R0 = FftPlan<N>::R[0];
-  constexpr int NP = FftPlan<N>::NP;
+  using TM = Team<N, L>;
+  constexpr int R0 = FftPlan<N, L>::R[0];
+  constexpr int NP = FftPlan<N, L>::NP;
   constexpr int T = TM::T;
   // first pass (NS = 1, no twiddles), from the inputs to the buffer
 #pragma unroll
@@ -271,13 +298,9 @@ __device__ __forceinline__ void fft_team_in(const In& in, double2 (&x)[Team<N>::
     for (int r = 0; r < R0; ++r) buf[j * R0 + r] = x[p * R0 + r];
   }
   __syncwarp();
-  // middle passes
-  if constexpr (NP == 3) {
-    constexpr int R1 = FftPlan<N>::R[1];
-    fft_mid_pass<N, R1, R0, DIR, T>(buf, tw, tl);
-  }
+  fft_mid_passes<N, L, DIR, T, 1, R0>(buf, tw, tl);
   // last pass: NS = N / RL, outputs land at j + r*N/RL = register slot positions
-  constexpr int RL = FftPlan<N>::R[NP - 1];
+  constexpr int RL = FftPlan<N, L>::R[NP - 1];
   static_assert(RL == R0, "plan must be symmetric");
   constexpr int NS = N / RL;
 #pragma unroll
@@ -297,11 +320,11 @@ __device__ __forceinline__ void fft_team_in(const In& in, double2 (&x)[Team<N>::
   __syncwarp();
 }
 
-// Transform x (register slots at Team<N>::pos) in place.
-template <int N, int DIR>
-__device__ __forceinline__ void fft_team(double2 (&x)[Team<N>::E], double2* buf,
+// Transform x (register slots at Team<N, L>::pos) in place.
+template <int N, int DIR, int L = 0>
+__device__ __forceinline__ void fft_team(double2 (&x)[Team<N, L>::E], double2* buf,
                                          const double2* __restrict__ tw, int tl) {
-  fft_team_in<N, DIR>(InPlain{x}, x, buf, tw, tl);
+  fft_team_in<N, DIR, L>(InPlain{x}, x, buf, tw, tl);
 }
 
 // Team-wide sum of one double; team lanes are contiguous within a warp.

@@ -40,6 +40,8 @@ namespace mattohf {
 
 constexpr int kSmallThreads = 256;
 constexpr int kSmallWarps = kSmallThreads / 32;
+// the latency FFT plans: few transforms run at a time, so a warp's chain counts
+constexpr int kSmallPlan = 1;
 
 __device__ __forceinline__ double small_warp_sum(double v) {
 #pragma unroll
@@ -49,7 +51,7 @@ __device__ __forceinline__ double small_warp_sum(double v) {
 
 template <int N>
 struct SmallLayout {
-  static constexpr int PW = Team<N>::PER_WARP;
+  static constexpr int PW = Team<N, kSmallPlan>::PER_WARP;
   static constexpr int NTEAM = kSmallWarps * PW;
   // warps 0..5 apply exchange pairs; in the column's first CTA warp 6 does the
   // kinetic transform and warp 7 the density and Hartree potential
@@ -109,7 +111,7 @@ __device__ void small_finalize(const SmallStageArgs& a, const double* rho_s, con
 
 template <int N>
 __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a) {
-  using TM = Team<N>;
+  using TM = Team<N, kSmallPlan>;
   constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
   constexpr int NTEAM = SmallLayout<N>::NTEAM;
   constexpr int PAIR_TEAMS = SmallLayout<N>::PAIR_TEAMS;
@@ -179,13 +181,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       double2 x[E];
 #pragma unroll
       for (int e = 0; e < E; ++e) x[e] = make_double2(rho_s[TM::pos(tl, e)], 0.0);
-      fft_team<N, -1>(x, buf, tw_s, tl);
-#pragma unroll
-      for (int e = 0; e < E; ++e) {
-        const double v = a.vCG[TM::pos(tl, e)];
-        x[e] = make_double2(v * x[e].x, v * x[e].y);
-      }
-      fft_team<N, +1>(x, buf, tw_s, tl);
+      fft_team<N, -1, kSmallPlan>(x, buf, tw_s, tl);
+      fft_team_in<N, +1, kSmallPlan>(InScaled<N, kSmallPlan>{x, a.vCG, tl}, x, buf, tw_s, tl);
       if (lane < T) {
 #pragma unroll
         for (int e = 0; e < E; ++e) vh_s[TM::pos(tl, e)] = x[e].x / (double)N;
@@ -199,7 +196,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       double2 x[E];
 #pragma unroll
       for (int e = 0; e < E; ++e) x[e] = wcol[TM::pos(tl, e)];
-      fft_team<N, -1>(x, buf, tw_s, tl);
+      fft_team<N, -1, kSmallPlan>(x, buf, tw_s, tl);
       if (obs) {
         const int itn = *a.it;
         const double Ao = (itn >= 1 && a.Aobs) ? a.Aobs[itn - 1] : 0.0;
@@ -228,7 +225,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
           const double m = 0.5 * (G * G + 2.0 * G * kAx + kA2);
           x[e] = make_double2(m * x[e].x / (double)N, m * x[e].y / (double)N);
         }
-        fft_team<N, +1>(x, buf, tw_s, tl);
+        fft_team<N, +1, kSmallPlan>(x, buf, tw_s, tl);
         if (lane < T) {
 #pragma unroll
           for (int e = 0; e < E; ++e) K_s[TM::pos(tl, e)] = x[e];
@@ -249,8 +246,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       const double2* ucol = a.u + ((size_t)kc * a.nb + bc) * N;
       const double* kern = a.kern + (size_t)(kr - kc + a.nk - 1) * N;
       double2 x[E];
-      fft_team_in<N, -1>(InConjProduct<N>{wcol, ucol, tl}, x, buf, tw_s, tl);
-      fft_team_in<N, +1>(InScaled<N>{x, kern, tl}, x, buf, tw_s, tl);
+      fft_team_in<N, -1, kSmallPlan>(InConjProduct<N, kSmallPlan>{wcol, ucol, tl}, x, buf, tw_s, tl);
+      fft_team_in<N, +1, kSmallPlan>(InScaled<N, kSmallPlan>{x, kern, tl}, x, buf, tw_s, tl);
       if (valid) {
 #pragma unroll
         for (int e = 0; e < E; ++e) acc[e] = cfma(x[e], ucol[TM::pos(tl, e)], acc[e]);
