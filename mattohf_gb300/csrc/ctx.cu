@@ -1975,20 +1975,38 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   CK(cudaMemcpyAsync(ctx->d_u0, ctx->d_u, sizeof(double2) * elems, cudaMemcpyDeviceToDevice, ctx->st));
   CK(cudaMemsetAsync(ctx->d_int, 0, 2 * sizeof(int), ctx->st));
   // the three step graphs, destroyed on every exit path
+  // each loop also as kGraphSteps steps in one graph (a graph launch is a
+  // full dependency; inside a graph the stages overlap)
   struct Execs {
-    cudaGraphExec_t g[3] = {nullptr, nullptr, nullptr};
+    cudaGraphExec_t g[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     ~Execs() {
       for (auto x : g)
         if (x) cudaGraphExecDestroy(x);
     }
   } ex;
   cudaGraphExec_t &gfwd = ex.g[0], &grec = ex.g[1], &gadj = ex.g[2];
+  cudaGraphExec_t &gfwd8 = ex.g[3], &grec8 = ex.g[4], &gadj8 = ex.g[5];
+  auto capture_steps = [&](cudaGraphExec_t* one, cudaGraphExec_t* many, const std::function<int()>& body) {
+    int rc = capture(ctx, one, body);
+    if (rc == MATTOHF_OK)
+      rc = capture(ctx, many, [&]() {
+        for (int k = 0; k < kGraphSteps; ++k) CKR(body());
+        return MATTOHF_OK;
+      });
+    return rc;
+  };
+  auto replay = [&](cudaGraphExec_t one, cudaGraphExec_t many, int n) -> int {
+    int j = 0;
+    for (; j + kGraphSteps <= n; j += kGraphSteps) CK(cudaGraphLaunch(many, ctx->st));
+    for (; j < n; ++j) CK(cudaGraphLaunch(one, ctx->st));
+    return MATTOHF_OK;
+  };
   // stage-store base step: the store slot of step it is (it - seg0)
   CK(cudaMemsetAsync(ctx->d_adj_int, 0, 4 * sizeof(int), ctx->st));
   // small problems run their forward steps through the fused stages
   if (use_small(ctx)) CKR(ensure_small_buffers(ctx));
   CK(cudaMemsetAsync(ctx->d_ticket, 0, sizeof(unsigned) * (1 + (size_t)NK * NB), ctx->st));
-  int rc = capture(ctx, &gfwd, [&]() {
+  int rc = capture_steps(&gfwd, &gfwd8, [&]() {
     if (store_all) return enq_recompute_step(ctx, fm, fave, fcur, dt);
     CK(launch_checkpoint(ctx->d_ckpt, ctx->d_u, ctx->d_int, C, elems, ctx->st));
     if (use_small(ctx)) return enq_small_step(ctx, fm, fave, fcur, dt);
@@ -1997,10 +2015,10 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
     return MATTOHF_OK;
   });
   if (rc == MATTOHF_OK && !store_all)
-    rc = capture(ctx, &grec, [&]() { return enq_recompute_step(ctx, fm, fave, fcur, dt); });
-  if (rc == MATTOHF_OK) rc = capture(ctx, &gadj, [&]() { return enq_adjoint_step(ctx, dt, elems); });
+    rc = capture_steps(&grec, &grec8, [&]() { return enq_recompute_step(ctx, fm, fave, fcur, dt); });
+  if (rc == MATTOHF_OK) rc = capture_steps(&gadj, &gadj8, [&]() { return enq_adjoint_step(ctx, dt, elems); });
   if (rc != MATTOHF_OK) return rc;
-  for (int it = 0; it < nt; ++it) CK(cudaGraphLaunch(gfwd, ctx->st));
+  CKR(replay(gfwd, gfwd8, nt));
   CK(cudaEventRecord(e1, ctx->st));
   // ---- objective at t = T and its gradient
   const double Afin = Ah[nt - 1];
@@ -2030,10 +2048,10 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
                          cudaMemcpyDeviceToDevice, ctx->st));
       CK(cudaMemcpyAsync(ctx->d_int, &s0, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
       CK(cudaMemcpyAsync(ctx->d_adj_int + 1, &s0, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
-      for (int j = 0; j < len; ++j) CK(cudaGraphLaunch(grec, ctx->st));
+      CKR(replay(grec, grec8, len));
     }
     CK(cudaMemcpyAsync(ctx->d_adj_int, hv, 2 * sizeof(int), cudaMemcpyHostToDevice, ctx->st));
-    for (int j = 0; j < len; ++j) CK(cudaGraphLaunch(gadj, ctx->st));
+    CKR(replay(gadj, gadj8, len));
     CK(cudaStreamSynchronize(ctx->st));  // host values above are stack-resident
   }
   CK(cudaEventRecord(e2, ctx->st));

@@ -41,6 +41,15 @@ constexpr int kAdjWarps = kAdjThreads / 32;
 
 __device__ __forceinline__ double2 times_i(double2 a) { return make_double2(-a.y, a.x); }
 
+// acc += i a b (4 FMA)
+__device__ __forceinline__ double2 cfma_i(double2 a, double2 b, double2 acc) {
+  acc.x = fma(-a.x, b.y, acc.x);
+  acc.x = fma(-a.y, b.x, acc.x);
+  acc.y = fma(a.x, b.x, acc.y);
+  acc.y = fma(-a.y, b.y, acc.y);
+  return acc;
+}
+
 template <int N>
 struct SmallAdjLayout {
   static constexpr int PW = Team<N>::PER_WARP;
@@ -182,7 +191,9 @@ __global__ void __launch_bounds__(kAdjThreads) k_small_adj(SmallAdjArgs a) {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
           const int q = TM::pos(tl, e);
-          x[e] = csub(cmulc(mA[q], vB[q]), cmulc(vA[q], mB[q]));
+          // mu_a conj(v_b) - v_a conj(mu_b): 4 + 4 FMA
+          const double2 t = cmulc(mA[q], vB[q]), va = vA[q], mb = mB[q];
+          x[e] = make_double2(fma(-va.y, mb.y, fma(-va.x, mb.x, t.x)), fma(va.x, mb.y, fma(-va.y, mb.x, t.y)));
         }
         fft_team<N, -1>(x, buf, tw_s, tl);
       }
@@ -199,11 +210,11 @@ __global__ void __launch_bounds__(kAdjThreads) k_small_adj(SmallAdjArgs a) {
             const int q = TM::pos(tl, e);
             const double sg = (q & 1) ? -1.0 : 1.0;
             const double2 pr = make_double2(fma(sg, cx, x[e].x), fma(sg, cy, x[e].y));
-            acc[e] = cadd(acc[e], times_i(cmul(pr, mB[q])));
+            acc[e] = cfma_i(pr, mB[q], acc[e]);
           }
         } else {
 #pragma unroll
-          for (int e = 0; e < E; ++e) acc[e] = cadd(acc[e], times_i(cmul(vB[TM::pos(tl, e)], x[e])));
+          for (int e = 0; e < E; ++e) acc[e] = cfma_i(vB[TM::pos(tl, e)], x[e], acc[e]);
         }
       }
     }
