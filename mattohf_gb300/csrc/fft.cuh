@@ -177,13 +177,15 @@ template <> struct FftPlan<128, 0> { static constexpr int NP = 3; static constex
 template <> struct FftPlan<256, 0> { static constexpr int NP = 3; static constexpr int R[8] = {8, 4, 8}; };
 template <> struct FftPlan<512, 0> { static constexpr int NP = 3; static constexpr int R[8] = {8, 8, 8}; };
 // L = 1: latency plans for kernels that run few transforms at a time (the
-// fused small-problem stages): radix-2 passes with two values per lane, so a
-// warp's dependent FP64 chain is about half that of the L = 0 plan for a few
-// percent more instructions in total.  Sizes without one use the L = 0 plan.
+// fused small-problem stages): 32-lane teams with two (N <= 64) or four
+// (N = 128) values per lane, so a warp's dependent FP64 chain is about half
+// that of the L = 0 plan for a few percent more instructions in total.  Sizes
+// without one use the L = 0 plan.
 template <int N> struct FftPlan<N, 1> : FftPlan<N, 0> {};
 template <> struct FftPlan<16, 1> { static constexpr int NP = 4; static constexpr int R[8] = {2, 2, 2, 2}; };
 template <> struct FftPlan<32, 1> { static constexpr int NP = 5; static constexpr int R[8] = {2, 2, 2, 2, 2}; };
 template <> struct FftPlan<64, 1> { static constexpr int NP = 6; static constexpr int R[8] = {2, 2, 2, 2, 2, 2}; };
+template <> struct FftPlan<128, 1> { static constexpr int NP = 4; static constexpr int R[8] = {4, 2, 4, 4}; };
 
 template <int N, int L>
 constexpr int fft_max_radix() {

@@ -40,8 +40,11 @@ namespace mattohf {
 
 constexpr int kSmallThreads = 256;
 constexpr int kSmallWarps = kSmallThreads / 32;
-// the latency FFT plans: few transforms run at a time, so a warp's chain counts
-constexpr int kSmallPlan = 1;
+// the latency FFT plans where few transforms run at a time and a warp's chain
+// counts (NG <= 64); at NG = 128 the stage is bound by each SM's FP64 rate and
+// the 16-lane plan balances better over the CTA's warps
+template <int N>
+constexpr int kSmallPlan = N <= 64 ? 1 : 0;
 
 __device__ __forceinline__ double small_warp_sum(double v) {
 #pragma unroll
@@ -51,7 +54,7 @@ __device__ __forceinline__ double small_warp_sum(double v) {
 
 template <int N>
 struct SmallLayout {
-  static constexpr int PW = Team<N, kSmallPlan>::PER_WARP;
+  static constexpr int PW = Team<N, kSmallPlan<N>>::PER_WARP;
   static constexpr int NTEAM = kSmallWarps * PW;
   // warps 0..5 apply exchange pairs; in the column's first CTA warp 6 does the
   // kinetic transform and warp 7 the density and Hartree potential
@@ -111,7 +114,7 @@ __device__ void small_finalize(const SmallStageArgs& a, const double* rho_s, con
 
 template <int N>
 __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a) {
-  using TM = Team<N, kSmallPlan>;
+  using TM = Team<N, kSmallPlan<N>>;
   constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
   constexpr int NTEAM = SmallLayout<N>::NTEAM;
   constexpr int PAIR_TEAMS = SmallLayout<N>::PAIR_TEAMS;
@@ -181,8 +184,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       double2 x[E];
 #pragma unroll
       for (int e = 0; e < E; ++e) x[e] = make_double2(rho_s[TM::pos(tl, e)], 0.0);
-      fft_team<N, -1, kSmallPlan>(x, buf, tw_s, tl);
-      fft_team_in<N, +1, kSmallPlan>(InScaled<N, kSmallPlan>{x, a.vCG, tl}, x, buf, tw_s, tl);
+      fft_team<N, -1, kSmallPlan<N>>(x, buf, tw_s, tl);
+      fft_team_in<N, +1, kSmallPlan<N>>(InScaled<N, kSmallPlan<N>>{x, a.vCG, tl}, x, buf, tw_s, tl);
       if (lane < T) {
 #pragma unroll
         for (int e = 0; e < E; ++e) vh_s[TM::pos(tl, e)] = x[e].x / (double)N;
@@ -196,7 +199,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       double2 x[E];
 #pragma unroll
       for (int e = 0; e < E; ++e) x[e] = wcol[TM::pos(tl, e)];
-      fft_team<N, -1, kSmallPlan>(x, buf, tw_s, tl);
+      fft_team<N, -1, kSmallPlan<N>>(x, buf, tw_s, tl);
       if (obs) {
         const int itn = *a.it;
         const double Ao = (itn >= 1 && a.Aobs) ? a.Aobs[itn - 1] : 0.0;
@@ -225,7 +228,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
           const double m = 0.5 * (G * G + 2.0 * G * kAx + kA2);
           x[e] = make_double2(m * x[e].x / (double)N, m * x[e].y / (double)N);
         }
-        fft_team<N, +1, kSmallPlan>(x, buf, tw_s, tl);
+        fft_team<N, +1, kSmallPlan<N>>(x, buf, tw_s, tl);
         if (lane < T) {
 #pragma unroll
           for (int e = 0; e < E; ++e) K_s[TM::pos(tl, e)] = x[e];
@@ -246,8 +249,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       const double2* ucol = a.u + ((size_t)kc * a.nb + bc) * N;
       const double* kern = a.kern + (size_t)(kr - kc + a.nk - 1) * N;
       double2 x[E];
-      fft_team_in<N, -1, kSmallPlan>(InConjProduct<N, kSmallPlan>{wcol, ucol, tl}, x, buf, tw_s, tl);
-      fft_team_in<N, +1, kSmallPlan>(InScaled<N, kSmallPlan>{x, kern, tl}, x, buf, tw_s, tl);
+      fft_team_in<N, -1, kSmallPlan<N>>(InConjProduct<N, kSmallPlan<N>>{wcol, ucol, tl}, x, buf, tw_s, tl);
+      fft_team_in<N, +1, kSmallPlan<N>>(InScaled<N, kSmallPlan<N>>{x, kern, tl}, x, buf, tw_s, tl);
       if (valid) {
 #pragma unroll
         for (int e = 0; e < E; ++e) acc[e] = cfma(x[e], ucol[TM::pos(tl, e)], acc[e]);

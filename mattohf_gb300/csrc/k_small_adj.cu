@@ -50,12 +50,15 @@ __device__ __forceinline__ double2 cfma_i(double2 a, double2 b, double2 acc) {
   return acc;
 }
 
+// 32-lane latency transforms: the (orbital, pass) work units are one warp's
+// team each, fine enough to balance over the CTA's warps
+constexpr int kAdjPlan = 1;
+
 template <int N>
 struct SmallAdjLayout {
-  static constexpr int PW = Team<N>::PER_WARP;
+  static constexpr int PW = Team<N, kAdjPlan>::PER_WARP;
   static constexpr int NTEAM = kAdjWarps * PW;
-  static constexpr int PAIR_TEAMS = 6 * PW;    // warps 0..5
-  static constexpr int PASS_TEAMS = 3 * PW;    // orbitals b per round
+  static constexpr int PASS_TEAMS = 3 * PW;    // orbitals b per round of warps 0..5 (host estimate)
   static constexpr int NSUB = (kAdjThreads / N) < 4 ? (kAdjThreads / N) : 4;
   // tw[N], bufs[NTEAM][N], F[N] (double2); vloc[N], psi[N], slices[2][NSUB][N] (double)
   static constexpr size_t bytes =
@@ -64,7 +67,7 @@ struct SmallAdjLayout {
 
 template <int N>
 __global__ void __launch_bounds__(kAdjThreads) k_small_adj(SmallAdjArgs a) {
-  using TM = Team<N>;
+  using TM = Team<N, kAdjPlan>;
   using L = SmallAdjLayout<N>;
   constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
   constexpr int NSUB = L::NSUB;
@@ -85,8 +88,15 @@ __global__ void __launch_bounds__(kAdjThreads) k_small_adj(SmallAdjArgs a) {
   const int chunk = blockIdx.x % a.P;
   const int ka = c / a.nb;
   const int M = ncols;
-  const int ppc = (M + a.P - 1) / a.P;     // orbitals b per CTA
-  const int b0 = chunk * ppc, b1 = min(M, b0 + ppc);
+  // orbitals b of this CTA, in groups of PW (a warp's teams).  The column's
+  // first CTA keeps warps 6 and 7 for the Hartree and kinetic work, so it takes
+  // half the share of the others.
+  const int G = (M + PW - 1) / PW;
+  const int wsum = 1 + 2 * (a.P - 1);
+  const int g0 = chunk == 0 ? 0 : (G * (2 * chunk - 1)) / wsum;
+  const int g1 = chunk + 1 == a.P ? G : (G * (2 * chunk + 1)) / wsum;
+  const int b0 = g0 * PW, b1 = min(M, g1 * PW);
+  const int workers = chunk == 0 ? kAdjWarps - 2 : kAdjWarps;
   double2* rv_g = a.part + (size_t)ncols * a.P * N + (size_t)c * N;         // (vloc, psi)
   double2* kin_g = a.part + (size_t)ncols * (a.P + 1) * N + (size_t)c * N;  // T_A mu_a
 
@@ -130,8 +140,8 @@ __global__ void __launch_bounds__(kAdjThreads) k_small_adj(SmallAdjArgs a) {
         x[e] = make_double2(a.occ * r, s);
         if (c == 0 && lane < T) a.gvion[q] += s;  // once per stage
       }
-      fft_team<N, -1>(x, buf, tw_s, tl);
-      fft_team_in<N, +1>(InScaled<N>{x, a.vCG, tl}, x, buf, tw_s, tl);
+      fft_team<N, -1, kAdjPlan>(x, buf, tw_s, tl);
+      fft_team_in<N, +1, kAdjPlan>(InScaled<N, kAdjPlan>{x, a.vCG, tl}, x, buf, tw_s, tl);
       if (lane < T) {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
@@ -149,8 +159,8 @@ __global__ void __launch_bounds__(kAdjThreads) k_small_adj(SmallAdjArgs a) {
         x[e] = mA[TM::pos(tl, e)];
         vf[e] = vA[TM::pos(tl, e)];
       }
-      fft_team<N, -1>(x, buf, tw_s, tl);
-      fft_team<N, -1>(vf, buf, tw_s, tl);
+      fft_team<N, -1, kAdjPlan>(x, buf, tw_s, tl);
+      fft_team<N, -1, kAdjPlan>(vf, buf, tw_s, tl);
       const double A = afield_value(a.af);
       const double kAx = a.kx[ka] + A, kA2 = kAx * kAx;
       double gp = 0.0;
@@ -162,22 +172,25 @@ __global__ void __launch_bounds__(kAdjThreads) k_small_adj(SmallAdjArgs a) {
         x[e] = make_double2(m * x[e].x / (double)N, m * x[e].y / (double)N);
       }
       gp = team_sum<T>(gp) / (double)N;
-      fft_team<N, +1>(x, buf, tw_s, tl);
+      fft_team<N, +1, kAdjPlan>(x, buf, tw_s, tl);
       if (lane < T) {
 #pragma unroll
         for (int e = 0; e < E; ++e) kin_g[TM::pos(tl, e)] = x[e];
       }
       if (lane == 0) a.gcol[c] = gp;
     }
-  } else {
-    // adjoint exchange of column a; the pass is uniform over a warp
-    const bool passB = (warp & 1) != 0;
-    const int wp = warp >> 1;
+  }
+  if (warp < workers) {
+    // adjoint exchange of column a: unit u = (group u/2 of PW orbitals b,
+    // pass u%2), dealt round-robin over the worker warps; the pass is uniform
+    // over a warp in each round
     double2 acc[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) acc[e] = make_double2(0.0, 0.0);
-    for (int base = b0 + wp * PW; base < b1; base += L::PASS_TEAMS) {
-      const int b = base + lane / T;
+    const int units = 2 * (g1 - g0);
+    for (int u = warp; u < units; u += workers) {
+      const bool passB = (u & 1) != 0;
+      const int b = b0 + (u >> 1) * PW + lane / T;
       const bool valid = b < b1;
       const int bb = valid ? b : b0;
       const int kb = bb / a.nb;
@@ -186,7 +199,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_small_adj(SmallAdjArgs a) {
       const double* kab = a.kern + (size_t)(ka - kb + a.nk - 1) * N;
       double2 x[E];
       if (!passB) {
-        fft_team_in<N, -1>(InConjProduct<N>{vA, vB, tl}, x, buf, tw_s, tl);
+        fft_team_in<N, -1, kAdjPlan>(InConjProduct<N, kAdjPlan>{vA, vB, tl}, x, buf, tw_s, tl);
       } else {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
@@ -195,12 +208,12 @@ __global__ void __launch_bounds__(kAdjThreads) k_small_adj(SmallAdjArgs a) {
           const double2 t = cmulc(mA[q], vB[q]), va = vA[q], mb = mB[q];
           x[e] = make_double2(fma(-va.y, mb.y, fma(-va.x, mb.x, t.x)), fma(va.x, mb.y, fma(-va.y, mb.x, t.y)));
         }
-        fft_team<N, -1>(x, buf, tw_s, tl);
+        fft_team<N, -1, kAdjPlan>(x, buf, tw_s, tl);
       }
       // Nyquist coefficient (pass A) in slot (p=0, r=R0/2) of the team's lane 0
       const double rnx = __shfl_sync(0xffffffffu, x[TM::R0 / 2].x, team_lane0);
       const double rny = __shfl_sync(0xffffffffu, x[TM::R0 / 2].y, team_lane0);
-      fft_team_in<N, +1>(InScaled<N>{x, kab, tl}, x, buf, tw_s, tl);
+      fft_team_in<N, +1, kAdjPlan>(InScaled<N, kAdjPlan>{x, kab, tl}, x, buf, tw_s, tl);
       if (valid) {
         if (!passB) {
           const double dk = __ldg(a.kern + (size_t)(kb - ka + a.nk - 1) * N + N / 2) - __ldg(kab + N / 2);
@@ -226,9 +239,10 @@ __global__ void __launch_bounds__(kAdjThreads) k_small_adj(SmallAdjArgs a) {
   // this CTA's partial (pair teams in order) -> part[c][chunk]; the first CTA
   // also publishes (vloc, psi)
   double2* mine = a.part + ((size_t)c * a.P + chunk) * N;
+  const int pair_teams = workers * PW;
   for (int i = tid; i < N; i += kAdjThreads) {
     double2 f = bufs[i];
-    for (int t2 = 1; t2 < L::PAIR_TEAMS; ++t2) f = cadd(f, bufs[(size_t)t2 * N + i]);
+    for (int t2 = 1; t2 < pair_teams; ++t2) f = cadd(f, bufs[(size_t)t2 * N + i]);
     mine[i] = f;
     if (chunk == 0) rv_g[i] = make_double2(vl_s[i], ps_s[i]);
   }
