@@ -213,7 +213,7 @@ def test_observables(name):
         assert abs(ob["Nele"] - 2.0 * S.NBocc) <= 1e-12
 
 
-@pytest.mark.parametrize("name", ["ng32_nk4", "ng64_nk8", "ng16_nk3_unocc"])
+@pytest.mark.parametrize("name", ["ng32_nk4", "ng64_nk8", "ng16_nk3_unocc", "ng128_nk4_nb3", "ng256_nk2"])
 @pytest.mark.parametrize("small", [0, 1])
 def test_rk4_run(name, small):
     """The RT loop vs the oracle, through the tiled path (small=0) and the fused
@@ -223,7 +223,9 @@ def test_rk4_run(name, small):
     cfg, ctx, S = setup(name)
     if small and cfg.NG > 256:
         pytest.skip("fused stages need NG <= 256")
-    cfg = dataclasses.replace(cfg, dt=0.004, NT=5, field_option="LP", omegac=1.55, Tpulse=0.1, E0=20.0)
+    # RK4 is stable for |E_max| dt < 2.8 with E_max ~ (pi NG / a)^2 / 2: scale dt with the grid
+    dt = 0.004 * min(1.0, (64.0 / cfg.NG) ** 2)
+    cfg = dataclasses.replace(cfg, dt=dt, NT=5, field_option="LP", omegac=1.55, Tpulse=0.1, E0=20.0)
     u0 = O.gram_schmidt(S, O.init_wf(S))
     _, A, Aave, _ = define_afield(cfg)
     ctx.set_orbitals(u0)
@@ -279,13 +281,14 @@ def test_taylor_propagators(variant):
 
 @pytest.mark.parametrize("small", [0, 1])
 def test_graph_equals_eager(small):
-    """The graph-replayed RT loop is bitwise identical to eager launches."""
+    """The graph-replayed RT loop (two eight-step graphs, then three one-step
+    graphs) is bitwise identical to eager launches."""
     from oracle import mattohf_oracle as O
     from mattohf_gb300 import _capi
     cfg, ctx, S = setup("ng64_nk8")
     ctx.set_option(_capi.OPT_SMALL_STAGES, small)
     u0 = O.gram_schmidt(S, O.init_wf(S))
-    A = np.linspace(0.0, 0.05, 4)
+    A = np.linspace(0.0, 0.05, 19)
     Aave = np.concatenate([[A[0] / 2], 0.5 * (A[1:] + A[:-1])])
     ctx.set_orbitals(u0)
     r1 = ctx.rk4_run(A, Aave, 0.005)
