@@ -2,7 +2,7 @@
 
 Tolerances (all complex128 / FP64):
   * tables, single operator applications: max|gpu-ref| <= 1e-12 * max|ref|
-  * RK4 series over a few steps: relative 1e-10 (the benchmark spec's bound)
+  * RK4 series over a few steps: relative 1e-10 (the parity bound for the RT series)
   * ground state: gauge-invariant quantities only (energies, Ritz values)
 """
 from __future__ import annotations
@@ -154,7 +154,7 @@ def test_hpsi_self_double_float(name):
 
 @pytest.mark.parametrize("name", ["ng32_nk4", "ng64_nk8"])
 def test_rk4_run_double_float(name):
-    """RK4 series with double-float exchange transforms vs the oracle (spec 1e-10)."""
+    """RK4 series with double-float exchange transforms vs the oracle (1e-10)."""
     from oracle import mattohf_oracle as O
     from mattohf_gb300 import _capi, define_afield
     cfg, ctx, S = setup(name)
