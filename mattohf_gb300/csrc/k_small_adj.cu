@@ -14,14 +14,18 @@
 //     vH[rho] + i vH[sigma]), giving vloc = vH[rho] + vion and psi = vH[sigma];
 //     warp 7 forms the kinetic term T_A mu_a and the field-gradient partial
 //     sum_G (G+k+A) Im(conj(FFT mu_a) FFT v_a) / N;
-//   * warps 0..5 apply the adjoint exchange of column a against the CTA's
-//     chunk of orbitals b, one b per team per round, in ordered form:
-//       pass A (warps 0, 2, 4): out_a += i (phi_ab + (-1)^m dk_ab R_ab) mu_b,
+//   * the CTA's worker warps (all eight, or warps 0..5 in the column's first
+//     CTA, which therefore takes half the others' share of orbitals) apply
+//     the adjoint exchange of column a against the CTA's orbitals b in
+//     ordered form.  A work unit is (a warp's group of orbitals b, pass);
+//     units are dealt round-robin over the worker warps:
+//       pass A: out_a += i (phi_ab + (-1)^m dk_ab R_ab) mu_b,
 //         phi_ab = Phi_ab[v_a conj(v_b)], R_ab its Nyquist coefficient,
 //         dk_ab = kern_ba[N/2] - kern_ab[N/2];
-//       pass B (warps 1, 3, 5): out_a += i v_b Phi_ab[mu_a conj(v_b) - v_a conj(mu_b)];
+//       pass B: out_a += i v_b Phi_ab[mu_a conj(v_b) - v_a conj(mu_b)];
 //     these are the row-a terms of the symmetric adjoint exchange (k_fock_adj)
-//     with the column terms written as the rows of the reversed pairs;
+//     with the column terms written as the rows of the reversed pairs.  The
+//     transforms use the 32-lane latency plans, so a unit is one team;
 //   * the column's last CTA (per-column ticket) adds the P partials in chunk
 //     order and does the stage bookkeeping element by element:
 //       lu = i (T_A + vloc) mu + Fa + 2 occ psi v,  lam_u += lu,
