@@ -12,29 +12,62 @@ namespace mattohf {
 
 constexpr int kGsThreads = 256;
 
-// Fixed-order CTA sum of a complex value (kGsThreads threads).
-__device__ double2 block_sum2(double2 v, double2* red) {
+// Fixed-order CTA sum of a complex value (kGsThreads threads), times `scale`.
+// Two barriers: every thread stores its partial, warp 0 adds the eight warp
+// partials of its lane (a fixed pairwise tree) and then its 32 lanes (a
+// shuffle tree), and lane 0 publishes the scaled result.  On this part one
+// FP64 warp instruction occupies a sub-partition's FP64 pipe for many cycles,
+// so the tree runs in one warp and only once, not redundantly in every
+// thread.  `red` and `res` are safe to reuse on the next call without a
+// third barrier: warp 0 reads `red` before the second barrier, and every
+// thread reads `res` before it reaches the next call's first barrier.
+__device__ double2 block_sum2(double2 v, double scale, double2* red, double2* res) {
+  static_assert(kGsThreads == 256, "eight warp partials per lane");
   red[threadIdx.x] = v;
   __syncthreads();
-  for (int o = kGsThreads / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) {
-      red[threadIdx.x].x += red[threadIdx.x + o].x;
-      red[threadIdx.x].y += red[threadIdx.x + o].y;
+  if (threadIdx.x < 32) {
+    const int l = threadIdx.x;
+    double2 p[8];
+#pragma unroll
+    for (int w = 0; w < 8; ++w) p[w] = red[w * 32 + l];
+#pragma unroll
+    for (int h = 4; h > 0; h >>= 1)
+#pragma unroll
+      for (int w = 0; w < h; ++w) {
+        p[w].x += p[w + h].x;
+        p[w].y += p[w + h].y;
+      }
+    double sx = p[0].x, sy = p[0].y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sx += __shfl_xor_sync(0xffffffffu, sx, o);
+      sy += __shfl_xor_sync(0xffffffffu, sy, o);
     }
-    __syncthreads();
+    if (l == 0) *res = make_double2(sx * scale, sy * scale);
   }
-  const double2 r = red[0];
   __syncthreads();
-  return r;
+  return *res;
 }
 
 // Modified Gram-Schmidt of nb columns per k, `passes` projection sweeps per
 // column.  One pass with weight vcell/NG is the reference's Gram_Schmidt; two
-// passes give the orthonormal basis of the Krylov block.
+// passes give the orthonormal basis of the Krylov block.  Thread t owns the
+// grid points t, t + kGsThreads, ... of every column, so between reductions
+// no thread reads what another wrote and only the reductions synchronise.
+// STAGE: the k-point's nb columns are held in shared memory for the sweep
+// (loaded and stored by their owners), so each projection waits on
+// shared-memory rather than L2 latency.
+template <bool STAGE>
 __global__ void __launch_bounds__(kGsThreads) k_mgs(double2* u, int kstride, int nb, int NG,
                                                     double weight, int passes, int* flag) {
+  extern __shared__ double2 cols[];  // STAGE: nb * NG
   __shared__ double2 red[kGsThreads];
-  double2* base = u + (size_t)blockIdx.x * kstride;
+  __shared__ double2 res;
+  double2* gbase = u + (size_t)blockIdx.x * kstride;
+  double2* base = STAGE ? cols : gbase;
+  if (STAGE)
+    for (int ib = 0; ib < nb; ++ib)
+      for (int i = threadIdx.x; i < NG; i += kGsThreads) cols[(size_t)ib * NG + i] = gbase[(size_t)ib * NG + i];
   for (int ib = 0; ib < nb; ++ib) {
     double2* ub = base + (size_t)ib * NG;
     for (int pass = 0; pass < passes; ++pass) {
@@ -46,9 +79,7 @@ __global__ void __launch_bounds__(kGsThreads) k_mgs(double2* u, int kstride, int
           s.x += a.x * b.x + a.y * b.y;   // conj(a)*b
           s.y += a.x * b.y - a.y * b.x;
         }
-        double2 zov = block_sum2(s, red);
-        zov.x = zov.x * weight;
-        zov.y = zov.y * weight;
+        const double2 zov = block_sum2(s, weight, red, &res);
         for (int i = threadIdx.x; i < NG; i += kGsThreads) {
           const double2 a = ut[i];
           double2 b = ub[i];
@@ -56,7 +87,6 @@ __global__ void __launch_bounds__(kGsThreads) k_mgs(double2* u, int kstride, int
           b.y -= a.x * zov.y + a.y * zov.x;
           ub[i] = b;
         }
-        __syncthreads();
       }
     }
     double2 s = make_double2(0.0, 0.0);
@@ -64,7 +94,7 @@ __global__ void __launch_bounds__(kGsThreads) k_mgs(double2* u, int kstride, int
       const double2 b = ub[i];
       s.x += b.x * b.x + b.y * b.y;
     }
-    const double nrm = block_sum2(s, red).x * weight;
+    const double nrm = block_sum2(s, weight, red, &res).x;
     if (!(nrm > 0.0) || !isfinite(nrm)) {
       if (threadIdx.x == 0 && flag) *flag = 1;
       continue;
@@ -76,8 +106,27 @@ __global__ void __launch_bounds__(kGsThreads) k_mgs(double2* u, int kstride, int
       b.y = b.y / sq;
       ub[i] = b;
     }
-    __syncthreads();
   }
+  if (STAGE)
+    for (int ib = 0; ib < nb; ++ib)
+      for (int i = threadIdx.x; i < NG; i += kGsThreads) gbase[(size_t)ib * NG + i] = cols[(size_t)ib * NG + i];
+}
+
+// k_mgs with the columns staged in shared memory when they fit
+constexpr size_t kMgsStageMax = 160 * 1024;
+static cudaError_t launch_mgs(double2* u, int kstride, int nb, int NG, double weight, int passes, int nk,
+                              int* flag, cudaStream_t s) {
+  const size_t bytes = sizeof(double2) * (size_t)nb * NG;
+  if (bytes <= kMgsStageMax) {
+    if (bytes > 48 * 1024) {
+      const cudaError_t e = cudaFuncSetAttribute(k_mgs<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      if (e != cudaSuccess) return e;
+    }
+    k_mgs<true><<<nk, kGsThreads, bytes, s>>>(u, kstride, nb, NG, weight, passes, flag);
+  } else {
+    k_mgs<false><<<nk, kGsThreads, 0, s>>>(u, kstride, nb, NG, weight, passes, flag);
+  }
+  return cudaGetLastError();
 }
 
 // M[k][i][j] = sum_x conj(x_i) y_j * weight ; one warp per (k, i, j).
@@ -111,14 +160,16 @@ __global__ void k_project(const double2* __restrict__ x, const double2* __restri
 // when the off-diagonal Frobenius norm is below 1e-15 of the full norm, or
 // after 60 sweeps (flag set).  Eigenvalues ascending; vectors in columns of V.
 constexpr int kJacMax = 64;
-__global__ void __launch_bounds__(128) k_jacobi(const double2* __restrict__ Min, int m,
+constexpr int kJacThreads = 128;
+__global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restrict__ Min, int m,
                                                double* __restrict__ evals,
                                                double2* __restrict__ evecs, int* flag) {
   extern __shared__ double2 jsm[];
   const int mp = m + (m & 1);  // even size; a padded index has no coupling
   double2* A = jsm;            // mp*mp, A[i*mp+j]
   double2* V = jsm + mp * mp;  // mp*mp
-  __shared__ double red[128];
+  __shared__ double2 red[kJacThreads];
+  __shared__ double2 norms;
   __shared__ int order[kJacMax + 1];
   __shared__ int pp[kJacMax / 2 + 1], qq[kJacMax / 2 + 1];
   __shared__ double rc[kJacMax / 2 + 1], rs[kJacMax / 2 + 1], rpr[kJacMax / 2 + 1], rpi[kJacMax / 2 + 1];
@@ -140,23 +191,30 @@ __global__ void __launch_bounds__(128) k_jacobi(const double2* __restrict__ Min,
   const int np = mp / 2;
   bool converged = false;
   for (int sweep = 0; sweep < 60 && !converged; ++sweep) {
+    // off-diagonal and total squared norms in one fixed-order reduction
+    // (four warp partials per lane, then the lanes of warp 0)
     double off = 0.0, tot = 0.0;
-    for (int idx = tid; idx < mp * mp; idx += blockDim.x) {
+    for (int idx = tid; idx < mp * mp; idx += kJacThreads) {
       const double2 v = A[idx];
       const double a2 = v.x * v.x + v.y * v.y;
       tot += a2;
       if (idx / mp != idx % mp) off += a2;
     }
-    red[tid] = off;
+    red[tid] = make_double2(off, tot);
     __syncthreads();
-    for (int o = 64; o > 0; o >>= 1) { if (tid < o) red[tid] += red[tid + o]; __syncthreads(); }
-    off = red[0];
+    if (tid < 32) {
+      const double2 r0 = red[tid], r1 = red[32 + tid], r2 = red[64 + tid], r3 = red[96 + tid];
+      double so = (r0.x + r1.x) + (r2.x + r3.x), st = (r0.y + r1.y) + (r2.y + r3.y);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        so += __shfl_xor_sync(0xffffffffu, so, o);
+        st += __shfl_xor_sync(0xffffffffu, st, o);
+      }
+      if (tid == 0) norms = make_double2(so, st);
+    }
     __syncthreads();
-    red[tid] = tot;
-    __syncthreads();
-    for (int o = 64; o > 0; o >>= 1) { if (tid < o) red[tid] += red[tid + o]; __syncthreads(); }
-    tot = red[0];
-    __syncthreads();
+    off = norms.x;
+    tot = norms.y;
     if (off <= 1e-30 * tot || off == 0.0) { converged = true; break; }
     for (int round = 0; round < mp - 1; ++round) {
       // circle-method pairing: player mp-1 is fixed
@@ -168,23 +226,29 @@ __global__ void __launch_bounds__(128) k_jacobi(const double2* __restrict__ Min,
         pp[tid] = p;
         qq[tid] = q;
         const double2 apq = A[p * mp + q];
-        const double mag = sqrt(apq.x * apq.x + apq.y * apq.y);
-        if (mag <= 1e-300) {
+        if (fabs(apq.x) + fabs(apq.y) <= 1e-150) {
           rc[tid] = 1.0; rs[tid] = 0.0; rpr[tid] = 1.0; rpi[tid] = 0.0;
         } else {
-          // zero A[p][q] with J = [[c, s e^{i phi}], [-s e^{-i phi}, c]], apq = mag e^{i phi}
-          const double tau = (A[q * mp + q].x - A[p * mp + p].x) / (2.0 * mag);
-          const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-          const double c = 1.0 / sqrt(1.0 + t * t);
-          rc[tid] = c;
-          rs[tid] = t * c;
-          rpr[tid] = apq.x / mag;
-          rpi[tid] = apq.y / mag;
+          // zero A[p][q] with J = [[c, s e^{i phi}], [-s e^{-i phi}, c]], apq = mag e^{i phi}.
+          // With tau = (A_qq - A_pp) / (2 mag), the angle obeys tan(2 theta) = 1 / |tau|
+          // (the smaller of the two solutions), so w = 1/sqrt(1 + tau^2) = sin(2 theta),
+          // |tau| w = cos(2 theta), c^2 = (1 + cos(2 theta)) / 2 and s = sin(2 theta) / (2c).
+          // Three reciprocal square roots and no division keep the serial chain of
+          // this single-warp step short; c^2 + s^2 = 1 to rounding.
+          const double rmag = rsqrt(apq.x * apq.x + apq.y * apq.y);  // 1 / mag
+          const double tau = (A[q * mp + q].x - A[p * mp + p].x) * (0.5 * rmag);
+          const double w = rsqrt(fma(tau, tau, 1.0));
+          const double c2 = fma(0.5 * fabs(tau), w, 0.5);
+          const double rcp_c = rsqrt(c2);
+          rc[tid] = c2 * rcp_c;
+          rs[tid] = (tau >= 0.0 ? 0.5 : -0.5) * w * rcp_c;
+          rpr[tid] = apq.x * rmag;
+          rpi[tid] = apq.y * rmag;
         }
       }
       __syncthreads();
       // columns p, q of A and V
-      for (int w = tid; w < np * mp; w += blockDim.x) {
+      for (int w = tid; w < np * mp; w += kJacThreads) {
         const int pr = w / mp, r = w % mp;
         const int p = pp[pr], q = qq[pr];
         const double c = rc[pr], s = rs[pr], ph_r = rpr[pr], ph_i = rpi[pr];
@@ -200,24 +264,23 @@ __global__ void __launch_bounds__(128) k_jacobi(const double2* __restrict__ Min,
                                      c * vq.y + s * (ph_r * vp.y + ph_i * vp.x));
       }
       __syncthreads();
-      // rows p, q (conjugate transpose)
-      for (int w = tid; w < np * mp; w += blockDim.x) {
+      // rows p, q (conjugate transpose); the rotated pair's coupling is set to
+      // exactly zero and its diagonal to exactly real here
+      for (int w = tid; w < np * mp; w += kJacThreads) {
         const int pr = w / mp, r = w % mp;
         const int p = pp[pr], q = qq[pr];
         const double c = rc[pr], s = rs[pr], ph_r = rpr[pr], ph_i = rpi[pr];
         const double2 xp = A[p * mp + r], xq = A[q * mp + r];
-        A[p * mp + r] = make_double2(c * xp.x - s * (ph_r * xq.x - ph_i * xq.y),
-                                     c * xp.y - s * (ph_r * xq.y + ph_i * xq.x));
-        A[q * mp + r] = make_double2(c * xq.x + s * (ph_r * xp.x + ph_i * xp.y),
-                                     c * xq.y + s * (ph_r * xp.y - ph_i * xp.x));
-      }
-      __syncthreads();
-      if (tid < np && rs[tid] != 0.0) {
-        const int p = pp[tid], q = qq[tid];
-        A[p * mp + q] = make_double2(0.0, 0.0);
-        A[q * mp + p] = make_double2(0.0, 0.0);
-        A[p * mp + p].y = 0.0;
-        A[q * mp + q].y = 0.0;
+        double2 np_ = make_double2(c * xp.x - s * (ph_r * xq.x - ph_i * xq.y),
+                                   c * xp.y - s * (ph_r * xq.y + ph_i * xq.x));
+        double2 nq_ = make_double2(c * xq.x + s * (ph_r * xp.x + ph_i * xp.y),
+                                   c * xq.y + s * (ph_r * xp.y - ph_i * xp.x));
+        if (s != 0.0) {
+          if (r == q) { np_ = make_double2(0.0, 0.0); nq_.y = 0.0; }       // A[p][q], A[q][q]
+          else if (r == p) { np_.y = 0.0; nq_ = make_double2(0.0, 0.0); }  // A[p][p], A[q][p]
+        }
+        A[p * mp + r] = np_;
+        A[q * mp + r] = nq_;
       }
       __syncthreads();
     }
@@ -290,14 +353,12 @@ __global__ void k_eps(const double2* __restrict__ u, const double2* __restrict__
 }
 
 cudaError_t launch_gram_schmidt(int NG, const GsArgs& a, int nk, cudaStream_t s) {
-  k_mgs<<<nk, kGsThreads, 0, s>>>(a.u, a.kstride, a.nb, NG, a.weight, 1, a.flag);
-  return cudaGetLastError();
+  return launch_mgs(a.u, a.kstride, a.nb, NG, a.weight, 1, nk, a.flag, s);
 }
 
 cudaError_t launch_block_orth(int NG, double2* x, int kstride, int m, double weight, int nk,
                               int* flag, cudaStream_t s) {
-  k_mgs<<<nk, kGsThreads, 0, s>>>(x, kstride, m, NG, weight, 2, flag);
-  return cudaGetLastError();
+  return launch_mgs(x, kstride, m, NG, weight, 2, nk, flag, s);
 }
 
 cudaError_t launch_project(int NG, const double2* x, const double2* y, int kstride, int m,
@@ -318,7 +379,7 @@ cudaError_t launch_jacobi(const double2* M, int m, double* evals, double2* evecs
     cudaError_t e = cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  k_jacobi<<<nk, 128, smem, s>>>(M, m, evals, evecs, flag);
+  k_jacobi<<<nk, kJacThreads, smem, s>>>(M, m, evals, evecs, flag);
   return cudaGetLastError();
 }
 

@@ -50,6 +50,7 @@ CONFIGS = {
     "ng64_nk5_nb4": make_cfg(NG=64, NK=5, NB=4, NBocc=3, acell=7.0),
     # any functional but 'HF' drops the exchange term (src/Functions.f90:85-87, 204-207, 276-278)
     "ng64_nk4_no_exchange": make_cfg(NG=64, NK=4, NB=3, NBocc=2, functional="PZ"),
+    "ng64_nk4_nb1": make_cfg(NG=64, NK=4, NB=1, NBocc=1),
 }
 
 _cache = {}
@@ -324,12 +325,18 @@ def test_nonfinite_detected(small):
     assert "step" in str(ei.value)
 
 
-@pytest.mark.parametrize("name", ["ng32_nk4", "ng16_nk3_unocc"])
-def test_gs_gauge_invariants(name):
+@pytest.mark.parametrize("name,ncg", [("ng32_nk4", 4), ("ng16_nk3_unocc", 2), ("ng16_nk3_unocc", 3),
+                                      ("ng64_nk4_nb1", 5)])  # Krylov dimension 8, 6, 9 and 5
+def test_gs_gauge_invariants(name, ncg):
+    """SCF iterations against the oracle.  A Krylov block amplifies rounding in
+    the h-applies: at NG=128, NB=3, NCG=3 a relative 1e-13 perturbation of h
+    alone moves the oracle's Je by 2.5e-10 and its Ritz values by 3.5e-9, so
+    the cases here are ones whose blocks are well conditioned (the same
+    perturbation moves Je by < 1e-13), odd Krylov dimensions included."""
     from oracle import mattohf_oracle as O
     cfg, ctx, S = setup(name)
     u0 = O.gram_schmidt(S, O.init_wf(S))
-    nscf, ncg = 4, 2 if S.NB == 3 else 4
+    nscf = 4
     S.cfg = dataclasses.replace(S.cfg, NCG=ncg)
     ref = O.gs_calculation(S, u0, nscf=nscf)
     ctx.set_orbitals(u0)
@@ -339,6 +346,25 @@ def test_gs_gauge_invariants(name):
     assert np.max(np.abs(got["Je"] - ref.Je)) <= 1e-9
     # density is gauge invariant
     assert rel(ctx.ubk_dns(ctx.get_orbitals()), O.ubk_dns(S, ref.ubk)) <= 1e-8
+
+
+@pytest.mark.parametrize("ng,nb", [(64, 5), (512, 24)])
+def test_gram_schmidt_staged_and_global(ng, nb):
+    """Gram-Schmidt with the k-point's columns held in shared memory (NB*NG*16 B
+    up to 160 KB) and in global memory (above it), against the oracle."""
+    from mattohf_gb300 import Context
+    from oracle import mattohf_oracle as O
+    cfg = make_cfg(NG=ng, NK=2, NB=nb, NBocc=1)
+    S = O.make_system(to_oracle_config(cfg))
+    u = O.init_wf(S)
+    rng = np.random.default_rng(11)
+    u = u + 0.3 * (rng.standard_normal(u.shape) + 1j * rng.standard_normal(u.shape)) * np.max(np.abs(u))
+    ref = O.gram_schmidt(S, u)
+    with Context(cfg) as ctx:
+        ctx.set_orbitals(u)
+        ctx.Gram_Schmidt()
+        got = ctx.get_orbitals()
+    assert rel(got, ref) <= 1e-11
 
 
 @pytest.mark.parametrize("case", ["hf_ng32_nk4", "hf_ng16_nk3_unocc"])
