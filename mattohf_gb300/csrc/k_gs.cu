@@ -172,7 +172,8 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
   __shared__ double2 norms;
   __shared__ int order[kJacMax + 1];
   __shared__ int pp[kJacMax / 2 + 1], qq[kJacMax / 2 + 1];
-  __shared__ double rc[kJacMax / 2 + 1], rs[kJacMax / 2 + 1], rpr[kJacMax / 2 + 1], rpi[kJacMax / 2 + 1];
+  // per pair: c, s and s e^{i phi} (the products are formed once, not per element)
+  __shared__ double rc[kJacMax / 2 + 1], rs[kJacMax / 2 + 1], rsr[kJacMax / 2 + 1], rsi[kJacMax / 2 + 1];
   const int k = blockIdx.x;
   const double2* Mk = Min + (size_t)k * m * m;
   const int tid = threadIdx.x;
@@ -227,7 +228,7 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
         qq[tid] = q;
         const double2 apq = A[p * mp + q];
         if (fabs(apq.x) + fabs(apq.y) <= 1e-150) {
-          rc[tid] = 1.0; rs[tid] = 0.0; rpr[tid] = 1.0; rpi[tid] = 0.0;
+          rc[tid] = 1.0; rs[tid] = 0.0; rsr[tid] = 0.0; rsi[tid] = 0.0;
         } else {
           // zero A[p][q] with J = [[c, s e^{i phi}], [-s e^{-i phi}, c]], apq = mag e^{i phi}.
           // With tau = (A_qq - A_pp) / (2 mag), the angle obeys tan(2 theta) = 1 / |tau|
@@ -240,10 +241,11 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
           const double w = rsqrt(fma(tau, tau, 1.0));
           const double c2 = fma(0.5 * fabs(tau), w, 0.5);
           const double rcp_c = rsqrt(c2);
+          const double sn = (tau >= 0.0 ? 0.5 : -0.5) * w * rcp_c;
           rc[tid] = c2 * rcp_c;
-          rs[tid] = (tau >= 0.0 ? 0.5 : -0.5) * w * rcp_c;
-          rpr[tid] = apq.x * rmag;
-          rpi[tid] = apq.y * rmag;
+          rs[tid] = sn;
+          rsr[tid] = sn * (apq.x * rmag);
+          rsi[tid] = sn * (apq.y * rmag);
         }
       }
       __syncthreads();
@@ -251,17 +253,13 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
       for (int w = tid; w < np * mp; w += kJacThreads) {
         const int pr = w / mp, r = w % mp;
         const int p = pp[pr], q = qq[pr];
-        const double c = rc[pr], s = rs[pr], ph_r = rpr[pr], ph_i = rpi[pr];
+        const double c = rc[pr], sr = rsr[pr], si = rsi[pr];  // (sr, si) = s e^{i phi}
         const double2 xp = A[r * mp + p], xq = A[r * mp + q];
-        A[r * mp + p] = make_double2(c * xp.x - s * (ph_r * xq.x + ph_i * xq.y),
-                                     c * xp.y - s * (ph_r * xq.y - ph_i * xq.x));
-        A[r * mp + q] = make_double2(c * xq.x + s * (ph_r * xp.x - ph_i * xp.y),
-                                     c * xq.y + s * (ph_r * xp.y + ph_i * xp.x));
+        A[r * mp + p] = make_double2(c * xp.x - (sr * xq.x + si * xq.y), c * xp.y - (sr * xq.y - si * xq.x));
+        A[r * mp + q] = make_double2(c * xq.x + (sr * xp.x - si * xp.y), c * xq.y + (sr * xp.y + si * xp.x));
         const double2 vp = V[r * mp + p], vq = V[r * mp + q];
-        V[r * mp + p] = make_double2(c * vp.x - s * (ph_r * vq.x + ph_i * vq.y),
-                                     c * vp.y - s * (ph_r * vq.y - ph_i * vq.x));
-        V[r * mp + q] = make_double2(c * vq.x + s * (ph_r * vp.x - ph_i * vp.y),
-                                     c * vq.y + s * (ph_r * vp.y + ph_i * vp.x));
+        V[r * mp + p] = make_double2(c * vp.x - (sr * vq.x + si * vq.y), c * vp.y - (sr * vq.y - si * vq.x));
+        V[r * mp + q] = make_double2(c * vq.x + (sr * vp.x - si * vp.y), c * vq.y + (sr * vp.y + si * vp.x));
       }
       __syncthreads();
       // rows p, q (conjugate transpose); the rotated pair's coupling is set to
@@ -269,13 +267,11 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
       for (int w = tid; w < np * mp; w += kJacThreads) {
         const int pr = w / mp, r = w % mp;
         const int p = pp[pr], q = qq[pr];
-        const double c = rc[pr], s = rs[pr], ph_r = rpr[pr], ph_i = rpi[pr];
+        const double c = rc[pr], sr = rsr[pr], si = rsi[pr];
         const double2 xp = A[p * mp + r], xq = A[q * mp + r];
-        double2 np_ = make_double2(c * xp.x - s * (ph_r * xq.x - ph_i * xq.y),
-                                   c * xp.y - s * (ph_r * xq.y + ph_i * xq.x));
-        double2 nq_ = make_double2(c * xq.x + s * (ph_r * xp.x + ph_i * xp.y),
-                                   c * xq.y + s * (ph_r * xp.y - ph_i * xp.x));
-        if (s != 0.0) {
+        double2 np_ = make_double2(c * xp.x - (sr * xq.x - si * xq.y), c * xp.y - (sr * xq.y + si * xq.x));
+        double2 nq_ = make_double2(c * xq.x + (sr * xp.x + si * xp.y), c * xq.y + (sr * xp.y - si * xp.x));
+        if (rs[pr] != 0.0) {
           if (r == q) { np_ = make_double2(0.0, 0.0); nq_.y = 0.0; }       // A[p][q], A[q][q]
           else if (r == p) { np_.y = 0.0; nq_ = make_double2(0.0, 0.0); }  // A[p][p], A[q][p]
         }
