@@ -214,7 +214,8 @@ def test_observables(name):
         assert abs(ob["Nele"] - 2.0 * S.NBocc) <= 1e-12
 
 
-@pytest.mark.parametrize("name", ["ng32_nk4", "ng64_nk8", "ng16_nk3_unocc", "ng128_nk4_nb3", "ng256_nk2"])
+@pytest.mark.parametrize("name", ["ng32_nk4", "ng64_nk8", "ng16_nk3_unocc", "ng128_nk4_nb3", "ng256_nk2",
+                                  "ng512_nk2", "ng64_nk4_nb1", "ng64_nk5_nb4"])
 @pytest.mark.parametrize("small", [0, 1])
 def test_rk4_run(name, small):
     """The RT loop vs the oracle, through the tiled path (small=0) and the fused
