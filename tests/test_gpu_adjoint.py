@@ -14,20 +14,28 @@ def _cfg(**kw):
     return RunConfig(**base)
 
 
+SHAPES = {
+    "ng32_nk4_nb2": {},
+    "ng16_nk3_nb3": dict(NG=16, NK=3, NB=3, NBocc=3),
+    "ng128_nk2_nb1": dict(NG=128, NK=2, NB=1, NBocc=1, acell=10.0),
+}
+
+
+@pytest.mark.parametrize("shape", list(SHAPES))
 @pytest.mark.parametrize("objective", ["energy", "current"])
 @pytest.mark.parametrize("ckpt", [0, 2])
 @pytest.mark.parametrize("small", [0, 1])
-def test_adjoint_matches_oracle(built_lib, objective, ckpt, small):
+def test_adjoint_matches_oracle(built_lib, shape, objective, ckpt, small):
     """Both the separate-launch path and the fused forward/reverse stages."""
     from mattohf_gb300 import Context, _capi
     from oracle import mattohf_oracle as O
     from conftest import to_oracle_config
-    cfg = _cfg()
+    cfg = _cfg(**SHAPES[shape])
     S = O.make_system(to_oracle_config(cfg))
     u0 = O.gram_schmidt(S, O.init_wf(S))
     rng = np.random.default_rng(4)
     A = 0.05 * rng.standard_normal(5)
-    dt = 0.004
+    dt = 0.004 * min(1.0, (64.0 / cfg.NG) ** 2)
     Lr, gr, gvr = O.rt_adjoint(S, u0, A, dt, objective)
     with Context(cfg) as ctx:
         ctx.set_option(_capi.OPT_SMALL_STAGES, small)
@@ -36,6 +44,18 @@ def test_adjoint_matches_oracle(built_lib, objective, ckpt, small):
     assert abs(L - Lr) <= 1e-10 * max(1.0, abs(Lr))
     assert np.max(np.abs(g - gr)) <= 1e-9 * np.max(np.abs(gr))
     assert np.max(np.abs(gv - gvr)) <= 1e-9 * np.max(np.abs(gvr))
+
+
+def test_adjoint_rejects_unoccupied_bands(built_lib):
+    """The adjoint is defined for all bands occupied; NB > NBocc is an argument error."""
+    from mattohf_gb300 import Context, MattohfError, _capi
+    cfg = _cfg(NG=16, NK=3, NB=3, NBocc=1)
+    with Context(cfg) as ctx:
+        ctx.Init_wf()
+        ctx.Gram_Schmidt()
+        with pytest.raises(MattohfError) as ei:
+            ctx.adjoint(np.zeros(4), 0.004, "energy")
+    assert ei.value.status == _capi.ERR_ARG
 
 
 def test_adjoint_finite_differences_gpu(built_lib):
