@@ -74,17 +74,18 @@ __global__ void __launch_bounds__(kGsThreads) k_mgs(double2* u, int kstride, int
       for (int ibt = 0; ibt < ib; ++ibt) {
         const double2* ut = base + (size_t)ibt * NG;
         double2 s = make_double2(0.0, 0.0);
+        // FMA chains: 2 FP64 instructions per real component (dot and update)
         for (int i = threadIdx.x; i < NG; i += kGsThreads) {
           const double2 a = ut[i], b = ub[i];
-          s.x += a.x * b.x + a.y * b.y;   // conj(a)*b
-          s.y += a.x * b.y - a.y * b.x;
+          s.x = fma(a.y, b.y, fma(a.x, b.x, s.x));   // conj(a)*b
+          s.y = fma(-a.y, b.x, fma(a.x, b.y, s.y));
         }
         const double2 zov = block_sum2(s, weight, red, &res);
         for (int i = threadIdx.x; i < NG; i += kGsThreads) {
           const double2 a = ut[i];
           double2 b = ub[i];
-          b.x -= a.x * zov.x - a.y * zov.y;
-          b.y -= a.x * zov.y + a.y * zov.x;
+          b.x = fma(a.y, zov.y, fma(-a.x, zov.x, b.x));   // b - a*zov
+          b.y = fma(-a.y, zov.x, fma(-a.x, zov.y, b.y));
           ub[i] = b;
         }
       }
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(kGsThreads) k_mgs(double2* u, int kstride, int
     double2 s = make_double2(0.0, 0.0);
     for (int i = threadIdx.x; i < NG; i += kGsThreads) {
       const double2 b = ub[i];
-      s.x += b.x * b.x + b.y * b.y;
+      s.x = fma(b.y, b.y, fma(b.x, b.x, s.x));
     }
     const double nrm = block_sum2(s, weight, red, &res).x;
     if (!(nrm > 0.0) || !isfinite(nrm)) {
