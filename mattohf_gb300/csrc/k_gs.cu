@@ -173,7 +173,8 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
   __shared__ double2 norms;
   __shared__ int order[kJacMax + 1];
   __shared__ int pp[kJacMax / 2 + 1], qq[kJacMax / 2 + 1];
-  // per pair: c, s and s e^{i phi} (the products are formed once, not per element)
+  // per pair: c, s / mag (only its being nonzero is used) and s e^{i phi}, the
+  // products formed once rather than per element
   __shared__ double rc[kJacMax / 2 + 1], rs[kJacMax / 2 + 1], rsr[kJacMax / 2 + 1], rsi[kJacMax / 2 + 1];
   const int k = blockIdx.x;
   const double2* Mk = Min + (size_t)k * m * m;
@@ -232,21 +233,21 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
           rc[tid] = 1.0; rs[tid] = 0.0; rsr[tid] = 0.0; rsi[tid] = 0.0;
         } else {
           // zero A[p][q] with J = [[c, s e^{i phi}], [-s e^{-i phi}, c]], apq = mag e^{i phi}.
-          // With tau = (A_qq - A_pp) / (2 mag), the angle obeys tan(2 theta) = 1 / |tau|
-          // (the smaller of the two solutions), so w = 1/sqrt(1 + tau^2) = sin(2 theta),
-          // |tau| w = cos(2 theta), c^2 = (1 + cos(2 theta)) / 2 and s = sin(2 theta) / (2c).
-          // Three reciprocal square roots and no division keep the serial chain of
+          // With d = A_qq - A_pp the angle obeys tan(2 theta) = 2 mag / |d| (the smaller
+          // solution), so with r = 1/sqrt(4 mag^2 + d^2): sin(2 theta) = 2 mag r,
+          // cos(2 theta) = |d| r, c^2 = (1 + cos(2 theta)) / 2 and
+          // s e^{i phi} = sign(d) sin(2 theta) / (2c) * apq / mag = sign(d) (r / c) apq.
+          // Two reciprocal square roots and no division keep the serial chain of
           // this single-warp step short; c^2 + s^2 = 1 to rounding.
-          const double rmag = rsqrt(apq.x * apq.x + apq.y * apq.y);  // 1 / mag
-          const double tau = (A[q * mp + q].x - A[p * mp + p].x) * (0.5 * rmag);
-          const double w = rsqrt(fma(tau, tau, 1.0));
-          const double c2 = fma(0.5 * fabs(tau), w, 0.5);
+          const double d = A[q * mp + q].x - A[p * mp + p].x;
+          const double r = rsqrt(fma(d, d, 4.0 * (apq.x * apq.x + apq.y * apq.y)));
+          const double c2 = fma(0.5 * fabs(d), r, 0.5);
           const double rcp_c = rsqrt(c2);
-          const double sn = (tau >= 0.0 ? 0.5 : -0.5) * w * rcp_c;
+          const double k = (d >= 0.0 ? r : -r) * rcp_c;  // s / mag with its sign
           rc[tid] = c2 * rcp_c;
-          rs[tid] = sn;
-          rsr[tid] = sn * (apq.x * rmag);
-          rsi[tid] = sn * (apq.y * rmag);
+          rs[tid] = k;  // nonzero exactly when the rotation is applied
+          rsr[tid] = k * apq.x;
+          rsi[tid] = k * apq.y;
         }
       }
       __syncthreads();
