@@ -167,8 +167,12 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
                                                double2* __restrict__ evecs, int* flag) {
   extern __shared__ double2 jsm[];
   const int mp = m + (m & 1);  // even size; a padded index has no coupling
-  double2* A = jsm;            // mp*mp, A[i*mp+j]
-  double2* V = jsm + mp * mp;  // mp*mp
+  // Row stride mp + 1: the column pass reads A[r][p] and V[r][p] for 16
+  // consecutive r per half-warp, which a stride of mp (a multiple of 256 B
+  // when mp is a multiple of 16) would put in one shared-memory bank group.
+  const int ld = mp + 1;
+  double2* A = jsm;            // mp rows of ld, A[i*ld+j]
+  double2* V = jsm + mp * ld;  // the same
   __shared__ double2 red[kJacThreads];
   __shared__ double2 norms;
   __shared__ int order[kJacMax + 1];
@@ -187,8 +191,8 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
       else if (i < j) { v = Mk[j * m + i]; v.y = -v.y; }
       else v = make_double2(Mk[i * m + i].x, 0.0);
     }
-    A[idx] = v;
-    V[idx] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    A[i * ld + j] = v;
+    V[i * ld + j] = make_double2(i == j ? 1.0 : 0.0, 0.0);
   }
   __syncthreads();
   const int np = mp / 2;
@@ -198,7 +202,7 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
     // (four warp partials per lane, then the lanes of warp 0)
     double off = 0.0, tot = 0.0;
     for (int idx = tid; idx < mp * mp; idx += kJacThreads) {
-      const double2 v = A[idx];
+      const double2 v = A[(idx / mp) * ld + idx % mp];
       const double a2 = v.x * v.x + v.y * v.y;
       tot += a2;
       if (idx / mp != idx % mp) off += a2;
@@ -228,7 +232,7 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
         if (p > q) { const int t = p; p = q; q = t; }
         pp[tid] = p;
         qq[tid] = q;
-        const double2 apq = A[p * mp + q];
+        const double2 apq = A[p * ld + q];
         if (fabs(apq.x) + fabs(apq.y) <= 1e-150) {
           rc[tid] = 1.0; rs[tid] = 0.0; rsr[tid] = 0.0; rsi[tid] = 0.0;
         } else {
@@ -239,7 +243,7 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
           // s e^{i phi} = sign(d) sin(2 theta) / (2c) * apq / mag = sign(d) (r / c) apq.
           // Two reciprocal square roots and no division keep the serial chain of
           // this single-warp step short; c^2 + s^2 = 1 to rounding.
-          const double d = A[q * mp + q].x - A[p * mp + p].x;
+          const double d = A[q * ld + q].x - A[p * ld + p].x;
           const double r = rsqrt(fma(d, d, 4.0 * (apq.x * apq.x + apq.y * apq.y)));
           const double c2 = fma(0.5 * fabs(d), r, 0.5);
           const double rcp_c = rsqrt(c2);
@@ -256,12 +260,12 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
         const int pr = w / mp, r = w % mp;
         const int p = pp[pr], q = qq[pr];
         const double c = rc[pr], sr = rsr[pr], si = rsi[pr];  // (sr, si) = s e^{i phi}
-        const double2 xp = A[r * mp + p], xq = A[r * mp + q];
-        A[r * mp + p] = make_double2(c * xp.x - (sr * xq.x + si * xq.y), c * xp.y - (sr * xq.y - si * xq.x));
-        A[r * mp + q] = make_double2(c * xq.x + (sr * xp.x - si * xp.y), c * xq.y + (sr * xp.y + si * xp.x));
-        const double2 vp = V[r * mp + p], vq = V[r * mp + q];
-        V[r * mp + p] = make_double2(c * vp.x - (sr * vq.x + si * vq.y), c * vp.y - (sr * vq.y - si * vq.x));
-        V[r * mp + q] = make_double2(c * vq.x + (sr * vp.x - si * vp.y), c * vq.y + (sr * vp.y + si * vp.x));
+        const double2 xp = A[r * ld + p], xq = A[r * ld + q];
+        A[r * ld + p] = make_double2(c * xp.x - (sr * xq.x + si * xq.y), c * xp.y - (sr * xq.y - si * xq.x));
+        A[r * ld + q] = make_double2(c * xq.x + (sr * xp.x - si * xp.y), c * xq.y + (sr * xp.y + si * xp.x));
+        const double2 vp = V[r * ld + p], vq = V[r * ld + q];
+        V[r * ld + p] = make_double2(c * vp.x - (sr * vq.x + si * vq.y), c * vp.y - (sr * vq.y - si * vq.x));
+        V[r * ld + q] = make_double2(c * vq.x + (sr * vp.x - si * vp.y), c * vq.y + (sr * vp.y + si * vp.x));
       }
       __syncthreads();
       // rows p, q (conjugate transpose); the rotated pair's coupling is set to
@@ -270,15 +274,15 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
         const int pr = w / mp, r = w % mp;
         const int p = pp[pr], q = qq[pr];
         const double c = rc[pr], sr = rsr[pr], si = rsi[pr];
-        const double2 xp = A[p * mp + r], xq = A[q * mp + r];
+        const double2 xp = A[p * ld + r], xq = A[q * ld + r];
         double2 np_ = make_double2(c * xp.x - (sr * xq.x - si * xq.y), c * xp.y - (sr * xq.y + si * xq.x));
         double2 nq_ = make_double2(c * xq.x + (sr * xp.x + si * xp.y), c * xq.y + (sr * xp.y - si * xp.x));
         if (rs[pr] != 0.0) {
           if (r == q) { np_ = make_double2(0.0, 0.0); nq_.y = 0.0; }       // A[p][q], A[q][q]
           else if (r == p) { np_.y = 0.0; nq_ = make_double2(0.0, 0.0); }  // A[p][p], A[q][p]
         }
-        A[p * mp + r] = np_;
-        A[q * mp + r] = nq_;
+        A[p * ld + r] = np_;
+        A[q * ld + r] = nq_;
       }
       __syncthreads();
     }
@@ -289,17 +293,17 @@ __global__ void __launch_bounds__(kJacThreads) k_jacobi(const double2* __restric
     for (int i = 0; i < m; ++i) order[i] = i;
     for (int i = 1; i < m; ++i) {
       const int oi = order[i];
-      const double v = A[oi * mp + oi].x;
+      const double v = A[oi * ld + oi].x;
       int j = i - 1;
-      while (j >= 0 && A[order[j] * mp + order[j]].x > v) { order[j + 1] = order[j]; --j; }
+      while (j >= 0 && A[order[j] * ld + order[j]].x > v) { order[j + 1] = order[j]; --j; }
       order[j + 1] = oi;
     }
   }
   __syncthreads();
-  for (int i = tid; i < m; i += blockDim.x) evals[(size_t)k * m + i] = A[order[i] * mp + order[i]].x;
+  for (int i = tid; i < m; i += blockDim.x) evals[(size_t)k * m + i] = A[order[i] * ld + order[i]].x;
   for (int idx = tid; idx < m * m; idx += blockDim.x) {
     const int r = idx / m, cidx = idx % m;
-    evecs[(size_t)k * m * m + idx] = V[r * mp + order[cidx]];  // [row][col]
+    evecs[(size_t)k * m * m + idx] = V[r * ld + order[cidx]];  // [row][col]
   }
 }
 
@@ -372,7 +376,7 @@ cudaError_t launch_jacobi(const double2* M, int m, double* evals, double2* evecs
                           int* flag, cudaStream_t s) {
   if (m > kJacMax) return cudaErrorInvalidValue;
   const int mp = m + (m & 1);
-  const size_t smem = sizeof(double2) * 2 * (size_t)mp * mp;
+  const size_t smem = sizeof(double2) * 2 * (size_t)mp * (mp + 1);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
