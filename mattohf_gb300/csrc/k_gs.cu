@@ -130,26 +130,34 @@ static cudaError_t launch_mgs(double2* u, int kstride, int nb, int NG, double we
   return cudaGetLastError();
 }
 
-// M[k][i][j] = sum_x conj(x_i) y_j * weight ; one warp per (k, i, j).
+// M[k][i][j] = sum_x conj(x_i) y_j * weight for i >= j, one warp per (k, i, j):
+// the eigensolver reads only the strictly lower triangle and the real part of
+// the diagonal (the reference's whw/ubhub assembly), so the upper triangle is
+// neither computed nor written.
 __global__ void k_project(const double2* __restrict__ x, const double2* __restrict__ y, int kstride,
                           int m, int NG, double weight, double2* __restrict__ M, int total) {
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (wid >= total) return;
-  const int k = wid / (m * m), ij = wid % (m * m), i = ij / m, j = ij % m;
+  const int ntri = m * (m + 1) / 2;
+  const int k = wid / ntri, t = wid % ntri;
+  int i = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);  // row of lower-triangle entry t
+  while (i * (i + 1) / 2 > t) --i;
+  while ((i + 1) * (i + 2) / 2 <= t) ++i;
+  const int j = t - i * (i + 1) / 2;
   const double2* xi = x + (size_t)k * kstride + (size_t)i * NG;
   const double2* yj = y + (size_t)k * kstride + (size_t)j * NG;
   double sr = 0.0, si = 0.0;
   for (int g = lane; g < NG; g += 32) {
     const double2 a = xi[g], b = yj[g];
-    sr += a.x * b.x + a.y * b.y;
-    si += a.x * b.y - a.y * b.x;
+    sr = fma(a.y, b.y, fma(a.x, b.x, sr));
+    si = fma(-a.y, b.x, fma(a.x, b.y, si));
   }
   for (int o = 16; o > 0; o >>= 1) {
     sr += __shfl_xor_sync(0xffffffffu, sr, o);
     si += __shfl_xor_sync(0xffffffffu, si, o);
   }
-  if (lane == 0) M[wid] = make_double2(sr * weight, si * weight);
+  if (lane == 0) M[((size_t)k * m + i) * m + j] = make_double2(sr * weight, si * weight);
 }
 
 // Parallel (round-robin ordered) Jacobi for a complex Hermitian m x m matrix,
@@ -365,7 +373,7 @@ cudaError_t launch_block_orth(int NG, double2* x, int kstride, int m, double wei
 
 cudaError_t launch_project(int NG, const double2* x, const double2* y, int kstride, int m,
                            double weight, double2* M, int nk, cudaStream_t s) {
-  const int total = nk * m * m;
+  const int total = nk * (m * (m + 1) / 2);
   const int warps_per_block = 8;
   k_project<<<(total + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0, s>>>(
       x, y, kstride, m, NG, weight, M, total);
