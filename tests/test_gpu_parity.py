@@ -349,6 +349,26 @@ def test_gs_gauge_invariants(name, ncg):
     assert rel(ctx.ubk_dns(ctx.get_orbitals()), O.ubk_dns(S, ref.ubk)) <= 1e-8
 
 
+def test_gs_wide_krylov_block():
+    """Krylov dimension 48 (NB=24, NCG=2): the eigensolver's and the staged
+    Gram-Schmidt's shared memory exceed 48 KB.  A relative 1e-13 perturbation
+    of h moves the oracle's Ritz values by 8e-11 here, well inside the bounds."""
+    from mattohf_gb300 import Context
+    from oracle import mattohf_oracle as O
+    cfg = make_cfg(NG=128, NK=1, NB=24, NBocc=24)
+    S = O.make_system(to_oracle_config(cfg))
+    nscf, ncg = 3, 2
+    S.cfg = dataclasses.replace(S.cfg, NCG=ncg)
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    ref = O.gs_calculation(S, u0, nscf=nscf)
+    with Context(cfg) as ctx:
+        ctx.set_orbitals(u0)
+        got = ctx.GS_calculation(nscf, ncg)
+    assert np.max(np.abs(got["Etot"] - ref.Etot)) <= 1e-9 * np.max(np.abs(ref.Etot))
+    assert np.max(np.abs(got["epsbk"] - ref.epsbk)) <= 1e-8 * np.max(np.abs(ref.epsbk))
+    assert np.max(np.abs(got["Je"] - ref.Je)) <= 1e-9
+
+
 @pytest.mark.parametrize("ng,nb", [(64, 5), (512, 24)])
 def test_gram_schmidt_staged_and_global(ng, nb):
     """Gram-Schmidt with the k-point's columns held in shared memory (NB*NG*16 B
