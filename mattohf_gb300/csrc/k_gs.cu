@@ -49,20 +49,29 @@ __device__ double2 block_sum2(double2 v, double scale, double2* red, double2* re
   return *res;
 }
 
-// Modified Gram-Schmidt of nb columns per k, `passes` projection sweeps per
-// column.  One pass with weight vcell/NG is the reference's Gram_Schmidt; two
-// passes give the orthonormal basis of the Krylov block.  Thread t owns the
-// grid points t, t + kGsThreads, ... of every column, so between reductions
-// no thread reads what another wrote and only the reductions synchronise.
-// STAGE: the k-point's nb columns are held in shared memory for the sweep
-// (loaded and stored by their owners), so each projection waits on
-// shared-memory rather than L2 latency.
+// Gram-Schmidt of nb columns per k with weight `weight`.
+//   passes == 1: modified Gram-Schmidt, the reference's Gram_Schmidt.
+//   passes == 2: the orthonormal basis of the Krylov block, by classical
+//     Gram-Schmidt applied twice ("twice is enough": Giraud, Langou and
+//     Rozloznik, 2005).  Each pass projects a column on all earlier columns at
+//     once; the dot products are summed eight at a time, one per warp, so the
+//     reductions use every sub-partition instead of serialising in one warp.
+// Thread t owns the grid points t, t + kGsThreads, ... of every column, so
+// between reductions no thread reads what another wrote and only the
+// reductions synchronise.  STAGE: the k-point's nb columns are held in shared
+// memory for the sweep (loaded and stored by their owners), so each projection
+// waits on shared-memory rather than L2 latency.
+constexpr int kCgsChunk = kGsThreads / 32;  // dot products reduced per round
+constexpr int kCgsMaxCols = 64;
 template <bool STAGE>
 __global__ void __launch_bounds__(kGsThreads) k_mgs(double2* u, int kstride, int nb, int NG,
                                                     double weight, int passes, int* flag) {
   extern __shared__ double2 cols[];  // STAGE: nb * NG
   __shared__ double2 red[kGsThreads];
   __shared__ double2 res;
+  __shared__ double2 part[kCgsChunk][kGsThreads];  // passes == 2: per-thread partial dots
+  __shared__ double2 zc[kCgsMaxCols];              // passes == 2: projections of the pass
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double2* gbase = u + (size_t)blockIdx.x * kstride;
   double2* base = STAGE ? cols : gbase;
   if (STAGE)
@@ -70,7 +79,60 @@ __global__ void __launch_bounds__(kGsThreads) k_mgs(double2* u, int kstride, int
       for (int i = threadIdx.x; i < NG; i += kGsThreads) cols[(size_t)ib * NG + i] = gbase[(size_t)ib * NG + i];
   for (int ib = 0; ib < nb; ++ib) {
     double2* ub = base + (size_t)ib * NG;
-    for (int pass = 0; pass < passes; ++pass) {
+    for (int pass = 0; passes == 2 && pass < 2 && ib > 0; ++pass) {
+      // zc[t] = weight * <u_t|u_ib> for all t < ib, from the column as it
+      // stands at the start of the pass, kCgsChunk at a time
+      for (int t0 = 0; t0 < ib; t0 += kCgsChunk) {
+        const int nt = min(kCgsChunk, ib - t0);
+        double2 acc[kCgsChunk];
+#pragma unroll
+        for (int c = 0; c < kCgsChunk; ++c) acc[c] = make_double2(0.0, 0.0);
+        for (int i = threadIdx.x; i < NG; i += kGsThreads) {
+          const double2 b = ub[i];
+#pragma unroll
+          for (int c = 0; c < kCgsChunk; ++c)
+            if (c < nt) {
+              const double2 a = base[(size_t)(t0 + c) * NG + i];
+              acc[c].x = fma(a.y, b.y, fma(a.x, b.x, acc[c].x));   // conj(a)*b
+              acc[c].y = fma(-a.y, b.x, fma(a.x, b.y, acc[c].y));
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kCgsChunk; ++c) part[c][threadIdx.x] = acc[c];
+        __syncthreads();
+        if (warp < nt) {  // warp c sums dot product t0 + c in a fixed order
+          double2 p[kGsThreads / 32];
+#pragma unroll
+          for (int w = 0; w < kGsThreads / 32; ++w) p[w] = part[warp][w * 32 + lane];
+#pragma unroll
+          for (int h = kGsThreads / 64; h > 0; h >>= 1)
+#pragma unroll
+            for (int w = 0; w < h; ++w) {
+              p[w].x += p[w + h].x;
+              p[w].y += p[w + h].y;
+            }
+          double sx = p[0].x, sy = p[0].y;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            sx += __shfl_xor_sync(0xffffffffu, sx, o);
+            sy += __shfl_xor_sync(0xffffffffu, sy, o);
+          }
+          if (lane == 0) zc[t0 + warp] = make_double2(sx * weight, sy * weight);
+        }
+        __syncthreads();
+      }
+      // u_ib -= sum_t zc[t] u_t, t ascending
+      for (int i = threadIdx.x; i < NG; i += kGsThreads) {
+        double2 b = ub[i];
+        for (int t = 0; t < ib; ++t) {
+          const double2 a = base[(size_t)t * NG + i], z = zc[t];
+          b.x = fma(a.y, z.y, fma(-a.x, z.x, b.x));
+          b.y = fma(-a.y, z.x, fma(-a.x, z.y, b.y));
+        }
+        ub[i] = b;
+      }
+    }
+    for (int pass = 0; passes == 1 && pass < 1; ++pass) {
       for (int ibt = 0; ibt < ib; ++ibt) {
         const double2* ut = base + (size_t)ibt * NG;
         double2 s = make_double2(0.0, 0.0);
@@ -117,12 +179,13 @@ __global__ void __launch_bounds__(kGsThreads) k_mgs(double2* u, int kstride, int
 constexpr size_t kMgsStageMax = 160 * 1024;
 static cudaError_t launch_mgs(double2* u, int kstride, int nb, int NG, double weight, int passes, int nk,
                               int* flag, cudaStream_t s) {
+  if ((passes != 1 && passes != 2) || (passes == 2 && nb > kCgsMaxCols)) return cudaErrorInvalidValue;
   const size_t bytes = sizeof(double2) * (size_t)nb * NG;
   if (bytes <= kMgsStageMax) {
-    if (bytes > 48 * 1024) {
-      const cudaError_t e = cudaFuncSetAttribute(k_mgs<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-      if (e != cudaSuccess) return e;
-    }
+    // the static buffers take about 37 KB, so even small stagings pass the
+    // 48 KB default: always raise the dynamic limit to what this launch needs
+    const cudaError_t e = cudaFuncSetAttribute(k_mgs<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
     k_mgs<true><<<nk, kGsThreads, bytes, s>>>(u, kstride, nb, NG, weight, passes, flag);
   } else {
     k_mgs<false><<<nk, kGsThreads, 0, s>>>(u, kstride, nb, NG, weight, passes, flag);
