@@ -210,6 +210,17 @@ int mattohf_fourier(int device, int nt, const double* time, const double* J, dou
  * Requires NB == NBocc.  Leaves the orbitals at u_nt. */
 int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double dt, const double* A, int ckpt_every,
                     double* L, double* dLdA, double* dLdvion);
+/* Gradient with respect to the ion-potential parameters, by the chain rule
+ * from a gradient on the grid (dLdvion[NG], e.g. from mattohf_adjoint) through
+ * Prep_periodic_ion_potential (src/Prep_periodic_ion_potential.f90:10-20):
+ * vion(x) = vraw(x) - max vraw, vraw(x) = -sum_ion sum_{icell=-4NK..4NK}
+ * Zeff/sqrt((x - a Rion - a icell)^2 + alpha^2).  Outputs dLdZeff[nspecies],
+ * dLdalpha[nspecies] (per species) and dLdRion[nion] (reduced positions).  The
+ * max shift is differentiated at the first grid point attaining the maximum
+ * (exact wherever the maximum is unique; one of the one-sided gradients at a
+ * tie).  No reference counterpart (the reference has no gradients). */
+int mattohf_ion_param_grad(mattohf_ctx* ctx, const double* dLdvion, double* dLdZeff, double* dLdalpha,
+                           double* dLdRion);
 /* Device times of the last mattohf_adjoint: the forward pass alone and the whole gradient. */
 int mattohf_adjoint_timing(mattohf_ctx* ctx, double* forward_ms, double* total_ms);
 
@@ -228,6 +239,16 @@ mattohf_ctx* mattohf_batch_run(mattohf_batch* b, int run);
 int mattohf_batch_rk4_run(mattohf_batch* b, int nt, const double* dt, const double* A,
                           const double* Aave, double* Etot, double* Je, double* Nele);
 int mattohf_batch_last_run_ms(mattohf_batch* b, double* ms);
+/* Adjoint gradients of every member (mattohf_adjoint per run, no reference
+ * counterpart): A [nruns][nt], dt [nruns]; L [nruns], dLdA [nruns][nt],
+ * dLdvion [nruns][NG] (outputs may be NULL).  Members run one at a time, each
+ * with all free device memory for its checkpoint segments (fitted to it when
+ * ckpt_every <= 0) and released before the next member; a member's results are
+ * those of mattohf_adjoint on it alone.  mattohf_batch_last_run_ms then gives
+ * the summed device time; mattohf_adjoint_timing on a member its own.  Each
+ * member is left at its final state. */
+int mattohf_batch_adjoint(mattohf_batch* b, int objective, int nt, const double* dt, const double* A,
+                          int ckpt_every, double* L, double* dLdA, double* dLdvion);
 /* Batch options: MATTOHF_OPT_FOCK_DF64, and MATTOHF_OPT_SYM_TILE (the exchange
  * tile of every run's tile pairs; 0 = a CTA's teams, the default). */
 int mattohf_batch_set_option(mattohf_batch* b, int option, long long value);
@@ -255,8 +276,11 @@ int mattohf_diag_dmma_peak(int device, double* tflops);
  *   stream  cudaStream_t to enqueue on (NULL = default stream); asynchronous.
  * Scratch comes from one 16 MiB device array inside the library that every GPU
  * loading the library holds until exit.  The first call on a device looks up
- * that array's device address (cudaGetSymbolAddress) with the device current,
- * so make it before any stream capture.  All calls share the array: calls that
+ * that array's device address (cudaGetSymbolAddress) and the device's
+ * multiprocessor count with the device current, so make it before any stream
+ * capture.  The cached address belongs to the CUDA runtime's primary context:
+ * after cudaDeviceReset, or with another driver context current, do not call
+ * this again in the same process.  All calls share the array: calls that
  * overlap on the GPU race and must be serialised by the caller.  Returns
  * MATTOHF_ERR_TOO_LARGE when the twiddles, the table and one NK*nbw*NG
  * complex128 set of partial sums do not fit in 16 MiB. */

@@ -45,7 +45,7 @@ EXPORTS = [
     "mattohf_batch_create", "mattohf_batch_destroy", "mattohf_batch_last_error", "mattohf_batch_run",
     "mattohf_batch_rk4_run", "mattohf_batch_last_run_ms", "mattohf_adjoint", "mattohf_adjoint_timing",
     "mattohf_fourier", "mattohf_vck", "mattohf_te_step", "mattohf_batch_set_option", "mattohf_autotune",
-    "mattohf_batch_autotune",
+    "mattohf_batch_autotune", "mattohf_ion_param_grad", "mattohf_batch_adjoint",
 ]
 
 
@@ -116,6 +116,8 @@ def load(path: str = LIB_PATH):
         "mattohf_batch_set_option": ([P, I, C.c_longlong], I),
         "mattohf_adjoint": ([P, I, I, C.c_double, D, I, D, D, D], I),
         "mattohf_adjoint_timing": ([P, D, D], I),
+        "mattohf_ion_param_grad": ([P, D, D, D, D], I),
+        "mattohf_batch_adjoint": ([P, I, I, D, D, I, D, D, D], I),
         "mattohf_vck": ([P, D, I, D], I),
         "mattohf_te_step": ([P, I, C.c_double, C.c_double], I),
         "mattohf_fourier": ([I, I, D, D, C.c_double, D, D, D, I, C.c_double, C.c_double, D], I),

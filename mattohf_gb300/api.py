@@ -250,6 +250,18 @@ class Context:
                                              C.byref(L), _dp(g), _dp(gv)))
         return L.value, g, gv
 
+    def ion_param_grad(self, dLdvion) -> Dict[str, np.ndarray]:
+        """Chain rule from dL/dvion on the grid to the ion-potential parameters
+        (src/Prep_periodic_ion_potential.f90:10-20): dL/dZeff and dL/dalpha per
+        species, dL/dRion per ion (reduced position)."""
+        g = np.ascontiguousarray(dLdvion, dtype=np.float64)
+        if g.shape != (self.NG,):
+            raise ValueError(f"expected shape ({self.NG},), got {g.shape}")
+        ns, ni = len(self.cfg.Zeff), len(self.cfg.Rion)
+        dZ, da, dR = np.empty(ns), np.empty(ns), np.empty(ni)
+        self._check(self.lib.mattohf_ion_param_grad(self.h, _dp(g), _dp(dZ), _dp(da), _dp(dR)))
+        return {"Zeff": dZ, "alpha": da, "Rion": dR}
+
     def adjoint_timing(self):
         f, t = C.c_double(), C.c_double()
         self._check(self.lib.mattohf_adjoint_timing(self.h, C.byref(f), C.byref(t)))
@@ -349,6 +361,19 @@ class Batch:
         ms = C.c_double()
         self._check(self.lib.mattohf_batch_last_run_ms(self.h, C.byref(ms)))
         return ms.value
+
+    def adjoint(self, A, dt, objective: str = "energy", ckpt_every: int = 0):
+        """Every member's (L, dL/dA[n], dL/dvion[x]) from its current orbitals
+        (mattohf_batch_adjoint).  A: (nruns, nt); dt: scalar or (nruns,).
+        Returns L (nruns,), dLdA (nruns, nt), dLdvion (nruns, NG)."""
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        R, nt = A.shape
+        dts = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, dtype=np.float64), (R,)))
+        obj = {"energy": 0, "current": 1}[objective]
+        L, g, gv = np.empty(R), np.empty((R, nt)), np.empty((R, self.cfgs[0].NG))
+        self._check(self.lib.mattohf_batch_adjoint(self.h, obj, nt, _dp(dts), _dp(A), int(ckpt_every), _dp(L),
+                                                    _dp(g), _dp(gv)))
+        return L, g, gv
 
     def set_option(self, opt: int, value: int):
         self._check(self.lib.mattohf_batch_set_option(self.h, opt, int(value)))

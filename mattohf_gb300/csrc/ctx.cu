@@ -195,13 +195,13 @@ int ensure_stage(mattohf_ctx* ctx, size_t elems) {
   return MATTOHF_OK;
 }
 
-// Pair chunking of the Fock kernel: enough items to fill 152 SMs several
-// times over, each chunk a whole number of team rounds.
+// Pair chunking of the Fock kernel: enough items to fill the device's SMs
+// eight times over, each chunk a whole number of team rounds.
 void fock_split(const mattohf_ctx* c, int ncols, int* nchunks, int* chunk) {
   const int npairs = c->NK * c->NBocc;
   int nch = c->opt_chunks;
   if (nch <= 0) {
-    const int target = 152 * 8;
+    const int target = std::max(1, c->nsm) * 8;
     nch = (target + ncols - 1) / ncols;
   }
   nch = std::max(1, std::min(nch, npairs));
@@ -312,7 +312,7 @@ int timed_end(mattohf_ctx* ctx) {
 constexpr int kGraphSteps = 8;
 
 int sym_tile(const mattohf_ctx* ctx) {
-  return ctx->opt_tile > 0 ? ctx->opt_tile : choose_sym_tile(ctx->NG, ctx->NK * ctx->NBocc);
+  return ctx->opt_tile > 0 ? ctx->opt_tile : choose_sym_tile(ctx->NG, ctx->NK * ctx->NBocc, ctx->nsm);
 }
 
 // Every buffer the RK4 step's exchange applies need, allocated up front so a
@@ -761,6 +761,64 @@ void compute_vion(mattohf_ctx* c) {
   for (double& v : c->vion) v = v - top;
 }
 
+// Chain rule from dL/dvion(x) to the parameters of the ion potential
+// (src/Prep_periodic_ion_potential.f90:10-20):
+//   vraw(x) = -sum_ii sum_icell Z_s / sqrt(d^2 + alpha_s^2),  d = x - a R_ii - a icell,
+//   vion(x) = vraw(x) - max_x' vraw(x'),
+// so dL/dp = sum_x g(x) dvraw(x)/dp - (sum_x g(x)) dvraw(x*)/dp, x* the grid
+// point of the maximum.  The shift is differentiable wherever the maximum is
+// attained at one grid point; at a tie the first such point in grid order is
+// taken (one of the one-sided gradients).  Per ion and cell image, with
+// r = (d^2 + alpha^2)^(-1/2):
+//   dvraw/dZ_s = -r,  dvraw/dalpha_s = Z alpha r^3,  dvraw/dR_ii = -a Z d r^3.
+void ion_param_grad(const mattohf_ctx* c, const double* g, double* dZ, double* dal, double* dR) {
+  const int NG = c->NG;
+  const double ax = c->acell;
+  std::vector<double> vraw(NG, 0.0);
+  for (size_t ii = 0; ii < c->Rion.size(); ++ii) {
+    const int sp = c->Kion[ii] - 1;
+    const double Za = c->Zeff[sp], al = c->alpha[sp];
+    for (int icell = -4 * c->NK; icell <= 4 * c->NK; ++icell)
+      for (int x = 0; x < NG; ++x) {
+        const double dist = std::fabs(c->rx[x] - ax * c->Rion[ii] - ax * (double)icell);
+        vraw[x] = vraw[x] - Za / std::sqrt(dist * dist + al * al);
+      }
+  }
+  int xs = 0;
+  for (int x = 1; x < NG; ++x)
+    if (vraw[x] > vraw[xs]) xs = x;
+  double gsum = 0.0;
+  for (int x = 0; x < NG; ++x) gsum += g[x];
+  const size_t ns = c->Zeff.size(), ni = c->Rion.size();
+  std::fill(dZ, dZ + ns, 0.0);
+  std::fill(dal, dal + ns, 0.0);
+  std::fill(dR, dR + ni, 0.0);
+  for (size_t ii = 0; ii < ni; ++ii) {
+    const int sp = c->Kion[ii] - 1;
+    const double Za = c->Zeff[sp], al = c->alpha[sp];
+    double sZ = 0.0, sa = 0.0, sR = 0.0;
+    for (int icell = -4 * c->NK; icell <= 4 * c->NK; ++icell)
+      for (int x = 0; x < NG; ++x) {
+        const double w = x == xs ? g[x] - gsum : g[x];
+        const double d = c->rx[x] - ax * c->Rion[ii] - ax * (double)icell;
+        const double r = 1.0 / std::sqrt(d * d + al * al), r3 = r * r * r;
+        sZ += w * -r;
+        sa += w * Za * al * r3;
+        sR += w * -ax * Za * d * r3;
+      }
+    dZ[sp] += sZ;
+    dal[sp] += sa;
+    dR[ii] += sR;
+  }
+}
+
+// The adjoint's segment storage (checkpoints and stage inputs), the only
+// buffers of the adjoint that scale with the window.
+void release_adjoint_storage(mattohf_ctx* ctx) {
+  dalloc(ctx, &ctx->d_ckpt, 0);
+  dalloc(ctx, &ctx->d_store, 0);
+}
+
 int ensure_series(mattohf_ctx* ctx, int nt) {
   if (nt <= ctx->series_cap) return MATTOHF_OK;
   destroy_graph(ctx);  // graph holds the old pointers
@@ -1018,6 +1076,14 @@ int mattohf_set_vion(mattohf_ctx* ctx, const double* vion) {
   ctx->vion.assign(vion, vion + ctx->NG);
   CK(cudaMemcpyAsync(ctx->d_vion, ctx->vion.data(), sizeof(double) * ctx->NG, cudaMemcpyHostToDevice, ctx->st));
   return sync_and_flag(ctx);
+}
+
+int mattohf_ion_param_grad(mattohf_ctx* ctx, const double* dLdvion, double* dLdZeff, double* dLdalpha,
+                           double* dLdRion) {
+  CKR(check_ctx(ctx));
+  if (!dLdvion || !dLdZeff || !dLdalpha || !dLdRion) return fail(ctx, MATTOHF_ERR_ARG, "null argument");
+  ion_param_grad(ctx, dLdvion, dLdZeff, dLdalpha, dLdRion);
+  return MATTOHF_OK;
 }
 
 int mattohf_set_orbitals(mattohf_ctx* ctx, const double* ubk) {
@@ -1909,20 +1975,28 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   if (ctx->NB != ctx->NBocc) return fail(ctx, MATTOHF_ERR_ARG, "the adjoint needs all bands occupied (NB == NBocc)");
   const int NG = ctx->NG, NB = ctx->NB, NK = ctx->NK;
   const size_t elems = orb_elems(ctx, NB);
-  // Checkpoint interval C.  C >= nt: the forward pass itself stores every
-  // stage input and the backward pass needs no recomputation.  Automatic
-  // (ckpt_every <= 0): that whenever it fits in three quarters of the free
-  // device memory, else sqrt(nt) (checkpoints plus one segment of stage inputs).
+  // Segments of at most C steps, aligned to the END of the window: the last
+  // segment is [nt - C, nt) and the first one takes the remainder.  The
+  // forward pass keeps a checkpoint at the start of every segment but the
+  // last, and stores the stage inputs of the last segment itself, so the
+  // backward pass recomputes only the nt - C steps before it (none when
+  // C >= nt).  Automatic (ckpt_every <= 0): the largest C whose stage inputs
+  // (4 per step), checkpoints and work buffers fit in three quarters of the
+  // free device memory.
+  release_adjoint_storage(ctx);   // a previous call's segments do not count against this one
   size_t freeb = 0, totalb = 0;
   CK(cudaMemGetInfo(&freeb, &totalb));
   int C = ckpt_every;
   if (C <= 0) {
-    const size_t all = sizeof(double2) * elems * (4 * (size_t)nt + 12);
-    C = all <= freeb / 4 * 3 ? nt : std::max(1, (int)std::lround(std::sqrt((double)nt)));
+    const long long slots = (long long)(freeb / 4 * 3 / (sizeof(double2) * elems));   // stage-input sized
+    long long c = std::min<long long>(nt, (slots - 12) / 4);
+    while (c > 1 && 4 * c + (nt + c - 1) / c + 12 > slots) --c;
+    C = (int)std::max<long long>(1, c);
   }
   C = std::min(C, nt);
-  const bool store_all = C == nt;
-  const int nseg = (nt + C - 1) / C;
+  const int phase = (C - nt % C) % C;        // segment starts: 0 and t with (t + phase) % C == 0
+  const int nseg = (nt + phase) / C;
+  const int s_last = nt - C;                 // start of the last segment (0 when C == nt)
   const size_t need = sizeof(double2) * elems * ((size_t)nseg + 4 * (size_t)C + 10);
   if (need > freeb) return fail(ctx, MATTOHF_ERR_ALLOC, "checkpoint storage exceeds free device memory; lower ckpt_every");
   CKR(ensure_series(ctx, nt));
@@ -2006,19 +2080,26 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   // small problems run their forward steps through the fused stages
   if (use_small(ctx)) CKR(ensure_small_buffers(ctx));
   CK(cudaMemsetAsync(ctx->d_ticket, 0, sizeof(unsigned) * (1 + (size_t)NK * NB), ctx->st));
-  int rc = capture_steps(&gfwd, &gfwd8, [&]() {
-    if (store_all) return enq_recompute_step(ctx, fm, fave, fcur, dt);
-    CK(launch_checkpoint(ctx->d_ckpt, ctx->d_u, ctx->d_int, C, elems, ctx->st));
-    if (use_small(ctx)) return enq_small_step(ctx, fm, fave, fcur, dt);
-    CKR(enq_rk4(ctx, fm, fave, fcur, dt, nullptr));
-    CK(launch_counter_add(ctx->d_int, 1, ctx->st));
-    return MATTOHF_OK;
-  });
-  if (rc == MATTOHF_OK && !store_all)
+  // gfwd: a step that keeps the segment checkpoint; grec: a step that stores
+  // its stage inputs (the last segment in the forward pass, and every
+  // recomputed segment)
+  int rc = MATTOHF_OK;
+  if (nseg > 1)
+    rc = capture_steps(&gfwd, &gfwd8, [&]() {
+      CK(launch_checkpoint(ctx->d_ckpt, ctx->d_u, ctx->d_int, C, phase, elems, ctx->st));
+      if (use_small(ctx)) return enq_small_step(ctx, fm, fave, fcur, dt);
+      CKR(enq_rk4(ctx, fm, fave, fcur, dt, nullptr));
+      CK(launch_counter_add(ctx->d_int, 1, ctx->st));
+      return MATTOHF_OK;
+    });
+  if (rc == MATTOHF_OK)
     rc = capture_steps(&grec, &grec8, [&]() { return enq_recompute_step(ctx, fm, fave, fcur, dt); });
   if (rc == MATTOHF_OK) rc = capture_steps(&gadj, &gadj8, [&]() { return enq_adjoint_step(ctx, dt, elems); });
   if (rc != MATTOHF_OK) return rc;
-  CKR(replay(gfwd, gfwd8, nt));
+  if (nseg > 1) CKR(replay(gfwd, gfwd8, s_last));
+  // the last segment's stage inputs go to store slots it - s_last
+  CK(cudaMemcpyAsync(ctx->d_adj_int + 1, &s_last, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+  CKR(replay(grec, grec8, nt - s_last));
   CK(cudaEventRecord(e1, ctx->st));
   // ---- objective at t = T and its gradient
   const double Afin = Ah[nt - 1];
@@ -2029,9 +2110,12 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   CK(cudaMemcpyAsync(ctx->d_uN, ctx->d_u, sizeof(double2) * elems, cudaMemcpyDeviceToDevice, ctx->st));
   Block ub = blk(ctx->d_u, NB, NG, NB);
   if (objective == 0) {
-    // dE = <2 occ dvcell h[u] u, du>
+    // dE = <2 occ dvcell h[u] u + (exchange Nyquist term), du>
     CKR(enq_hpsi(ctx, ub, ub, blko(ctx->d_lam, NB, NG, NB), aval(Afin), CM_H));
     CK(launch_scale2(ctx->d_lam, 2.0 * ctx->occ * ctx->dvcell, elems, ctx->st));
+    if (ctx->hf)
+      CK(launch_energy_grad_nyquist(ctx->d_u, ctx->d_lam, ctx->d_kern, NG, NK, NB, ctx->occ * ctx->dvcell,
+                                    ctx->st));
   } else {
     // dJ = <-2 occ (dvcell/vcell) P_A u, du>
     CK(launch_velocity(NG, ctx->d_u, ctx->d_lam, ctx->tw, ctx->d_Gx, ctx->d_kx, NB, Afin,
@@ -2041,9 +2125,9 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   CK(cudaMemsetAsync(ctx->d_gstage, 0, sizeof(double) * 4 * nt, ctx->st));
   // ---- backward over segments: recompute stage inputs, then reverse them
   for (int seg = nseg - 1; seg >= 0; --seg) {
-    const int s0 = seg * C, len = std::min(C, nt - s0);
+    const int s0 = std::max(0, seg * C - phase), len = std::min(nt, (seg + 1) * C - phase) - s0;
     const int hv[2] = {s0 + len - 1, s0};
-    if (!store_all) {
+    if (seg < nseg - 1) {
       CK(cudaMemcpyAsync(ctx->d_u, ctx->d_ckpt + (size_t)seg * elems, sizeof(double2) * elems,
                          cudaMemcpyDeviceToDevice, ctx->st));
       CK(cudaMemcpyAsync(ctx->d_int, &s0, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
@@ -2626,6 +2710,30 @@ int mattohf_batch_autotune(mattohf_batch* b, int steps, int* tile, double* us) {
 int mattohf_batch_last_run_ms(mattohf_batch* b, double* ms) {
   if (!b || !ms) return MATTOHF_ERR_ARG;
   *ms = b->last_ms;
+  return MATTOHF_OK;
+}
+
+// The adjoint of every member, one member at a time.  A member of the largest
+// shapes (NG = 512, NK = 128, Nocc = 8: half a million exchange pairs per
+// apply) fills the FP64 pipe by itself, so members side by side would gain no
+// throughput and would split the device memory that the checkpoint segments
+// use; in turn, each member gets all of it (its segment is fitted to the free
+// memory when ckpt_every <= 0) and releases it before the next one starts.
+int mattohf_batch_adjoint(mattohf_batch* b, int objective, int nt, const double* dt, const double* A,
+                          int ckpt_every, double* L, double* dLdA, double* dLdvion) {
+  if (!b) return MATTOHF_ERR_ARG;
+  if (nt < 1 || !dt || !A) return bfail(b, MATTOHF_ERR_ARG, "bad batch adjoint arguments");
+  double ms = 0.0;
+  for (int r = 0; r < b->R; ++r) {
+    mattohf_ctx* c = b->runs[r];
+    const int rc = mattohf_adjoint(c, objective, nt, dt[r], A + (size_t)r * nt, ckpt_every,
+                                   L ? L + r : nullptr, dLdA ? dLdA + (size_t)r * nt : nullptr,
+                                   dLdvion ? dLdvion + (size_t)r * b->NG : nullptr);
+    release_adjoint_storage(c);
+    if (rc != MATTOHF_OK) return bfail(b, rc, "run " + std::to_string(r) + ": " + c->err);
+    ms += c->last_adj_ms;
+  }
+  b->last_ms = ms;
   return MATTOHF_OK;
 }
 

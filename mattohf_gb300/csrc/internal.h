@@ -286,7 +286,7 @@ cudaError_t launch_density(int NG, const DensArgs& a, cudaStream_t s);
 cudaError_t launch_fock(int NG, const FockArgs& a, int ncols, cudaStream_t s);
 cudaError_t launch_fock_sym(int NG, const FockSymArgs& a, cudaStream_t s);
 int fock_sym_teams(int NG);  // teams of a full symmetric-exchange CTA (largest tile size)
-int choose_sym_tile(int NG, int M);  // tile size for a single run of M occupied orbitals
+int choose_sym_tile(int NG, int M, int nsm);  // tile size for a single run of M occupied orbitals on nsm SMs
 cudaError_t sym_launch_params(int NG, int S, int* threads, size_t* smem);
 cudaError_t configure_kernels();
 struct ExArgs {
@@ -358,12 +358,16 @@ cudaError_t launch_adj_init(const double2* lam, double2* lam_u, double2* const* 
                             cudaStream_t s);
 cudaError_t launch_stage_copy(double2* dst, const double2* src, double2* store, const int* n, const int* seg0,
                               int slot, size_t elems, int to_store, cudaStream_t s);
-cudaError_t launch_checkpoint(double2* ckpt, const double2* u, const int* it, int every, size_t elems,
+cudaError_t launch_checkpoint(double2* ckpt, const double2* u, const int* it, int every, int phase, size_t elems,
                               cudaStream_t s);
 cudaError_t launch_counter_add(int* p, int d, cudaStream_t s);
 cudaError_t launch_velocity(int NG, const double2* u, double2* out, const double2* tw, const double* Gx,
                             const double* kx, int nb, double A, double scale, int ncols, cudaStream_t s);
 cudaError_t launch_scale2(double2* x, double sc, size_t n, cudaStream_t s);
+// g += the Nyquist term of the exchange-energy gradient (all nk*nb columns of u
+// occupied); sc = occ * dvcell
+cudaError_t launch_energy_grad_nyquist(const double2* u, double2* g, const double* kern, int NG, int nk, int nb,
+                                       double sc, cudaStream_t s);
 
 cudaError_t launch_te_update(double2* w, const double2* h0, const double2* h1, double c, double iorder,
                              double2* acc, size_t n, cudaStream_t s);

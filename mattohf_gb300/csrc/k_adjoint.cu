@@ -8,8 +8,13 @@
 //   J^T mu = i h[v](a) mu                                  kinetic, local, exchange at fixed v
 //          + 2 occ vH[sigma] v,  sigma = sum Im(conj(mu) v)  Hartree response
 //          + i sum_j conj(phi_ji) mu_j                      exchange: dependence through the source orbital
-//          + i sum_j v_j Phi_ij[mu_i conj(v_j) - v_i conj(mu_j)]   (the i VF mu term folded in)
+//          + i sum_j v_j (Phi_ij[mu_i conj(v_j)] - Phi~_ji[v_i conj(mu_j)])   (the i VF mu term folded in)
 // with phi_ij = Phi_ij[v_i conj(v_j)] the pair potentials of the forward step.
+// Phi~_ji, the transpose of dv_j -> Phi_ij[v_i conj(dv_j)], has the multiplier
+// kern_ji(-G): that is kern_ij(G) (v is even) except at the self-aliased
+// Nyquist index N/2, where it stays kern_ji.  So
+//   Phi~_ji[f] = Phi_ij[f] + dk_ij Nyq(f) (-1)^m,  dk_ij = kern_ji[N/2] - kern_ij[N/2],
+// Nyq(f) = sum_m (-1)^m f(m) the Nyquist coefficient of the forward transform.
 // k_fock_adj evaluates the two exchange sums over unordered occupied pairs
 // with two transform pairs per pair (pair densities v_i conj(v_j) and
 // mu_i conj(v_j) - v_i conj(mu_j)), using the same conjugate-plus-Nyquist
@@ -71,8 +76,8 @@ __global__ void __launch_bounds__(kThreads) k_fock_adj(AdjFockArgs a) {
     double2 x[E];
     // ---- pass A: phi_ab = Phi_ab[v_a conj(v_b)]
     fft_team_in<N, -1>(InConjProduct<N>{vA, vB, tl}, x, buf, tw_s, tl);
-    double rnx = __shfl_sync(0xffffffffu, x[TM::R0 / 2].x, team_lane0);
-    double rny = __shfl_sync(0xffffffffu, x[TM::R0 / 2].y, team_lane0);
+    const double rnx = __shfl_sync(0xffffffffu, x[TM::R0 / 2].x, team_lane0);
+    const double rny = __shfl_sync(0xffffffffu, x[TM::R0 / 2].y, team_lane0);
     fft_team_in<N, +1>(InScaled<N>{x, kab, tl}, x, buf, tw_s, tl);
     if (valid) {
       if (self) {
@@ -94,31 +99,36 @@ __global__ void __launch_bounds__(kThreads) k_fock_adj(AdjFockArgs a) {
         }
       }
     }
-    // ---- pass B: phi'_ab = Phi_ab[mu_a conj(v_b) - v_a conj(mu_b)]
+    // ---- pass B: phi'_ab = Phi_ab[mu_a conj(v_b) - v_a conj(mu_b)], and
+    //      n2 = Nyq(v_a conj(mu_b)) for the transposed operator's Nyquist term
+    double n2x = 0.0, n2y = 0.0;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       const int q = TM::pos(tl, e);
-      x[e] = csub(cmulc(mA[q], vB[q]), cmulc(vA[q], mB[q]));
+      const double sg = (q & 1) ? -1.0 : 1.0;
+      const double2 t2 = cmulc(vA[q], mB[q]);
+      x[e] = csub(cmulc(mA[q], vB[q]), t2);
+      n2x = fma(sg, t2.x, n2x);
+      n2y = fma(sg, t2.y, n2y);
     }
+    n2x = team_sum<T>(n2x);
+    n2y = team_sum<T>(n2y);
     fft_team<N, -1>(x, buf, tw_s, tl);
-    rnx = __shfl_sync(0xffffffffu, x[TM::R0 / 2].x, team_lane0);
-    rny = __shfl_sync(0xffffffffu, x[TM::R0 / 2].y, team_lane0);
     fft_team_in<N, +1>(InScaled<N>{x, kab, tl}, x, buf, tw_s, tl);
     if (valid) {
-      // out_a += i v_b phi'_ab
+      // y = Phi_ab[mu_a conj(v_b)] - Phi~_ba[v_a conj(mu_b)] = phi'_ab - dk n2 (-1)^m;
+      // out_a += i v_b y.  The pair's reversed term is its mirror image:
+      // Phi_ba[mu_b conj(v_a)] - Phi~_ab[v_b conj(mu_a)] = -conj(y), so
+      // out_b += i v_a (-conj(y)).  (dk = 0 on the diagonal.)
+      const double cx = dk * n2x, cy = dk * n2y;
+      double2* col = cacc + lb * N;
 #pragma unroll
-      for (int e = 0; e < E; ++e) racc[e] = cadd(racc[e], mul_i(cmul(vB[TM::pos(tl, e)], x[e])));
-      if (!self) {
-        // phi'_ba = -conj(phi'_ab) - c' (-1)^m,  c' = dk conj(R');  out_b += i v_a phi'_ba
-        const double cx = dk * rnx, cy = -dk * rny;
-        double2* col = cacc + lb * N;
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-          const int q = TM::pos(tl, e);
-          const double sg = (q & 1) ? -1.0 : 1.0;
-          const double2 pba = make_double2(-fma(sg, cx, x[e].x), fma(-sg, cy, x[e].y));
-          col[q] = cadd(col[q], mul_i(cmul(vA[q], pba)));
-        }
+      for (int e = 0; e < E; ++e) {
+        const int q = TM::pos(tl, e);
+        const double sg = (q & 1) ? -1.0 : 1.0;
+        const double2 y = make_double2(fma(-sg, cx, x[e].x), fma(-sg, cy, x[e].y));
+        racc[e] = cadd(racc[e], mul_i(cmul(vB[q], y)));
+        if (!self) col[q] = cadd(col[q], mul_i(cmul(vA[q], make_double2(-y.x, y.y))));
       }
     }
     __syncthreads();
@@ -251,11 +261,13 @@ __global__ void k_stage_copy(double2* dst, const double2* src, double2* store, c
 }
 
 // checkpoint u every `every` steps: ckpt[it / every] = u when it % every == 0
-__global__ void k_checkpoint(double2* ckpt, const double2* u, const int* it, int every, size_t elems) {
+// Checkpoint j holds the state at the start of segment j; segments start at
+// step 0 and at every t with (t + phase) % every == 0.
+__global__ void k_checkpoint(double2* ckpt, const double2* u, const int* it, int every, int phase, size_t elems) {
   const int t = *it;
-  if (t % every != 0) return;
+  if (t != 0 && (t + phase) % every != 0) return;
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < elems) ckpt[(size_t)(t / every) * elems + i] = u[i];
+  if (i < elems) ckpt[(size_t)((t + phase) / every) * elems + i] = u[i];
 }
 
 __global__ void k_counter_add(int* p, int d) {
@@ -381,9 +393,9 @@ cudaError_t launch_stage_copy(double2* dst, const double2* src, double2* store, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_checkpoint(double2* ckpt, const double2* u, const int* it, int every, size_t elems,
+cudaError_t launch_checkpoint(double2* ckpt, const double2* u, const int* it, int every, int phase, size_t elems,
                               cudaStream_t s) {
-  k_checkpoint<<<(unsigned)((elems + 255) / 256), 256, 0, s>>>(ckpt, u, it, every, elems);
+  k_checkpoint<<<(unsigned)((elems + 255) / 256), 256, 0, s>>>(ckpt, u, it, every, phase, elems);
   return cudaGetLastError();
 }
 
@@ -409,6 +421,75 @@ cudaError_t launch_velocity(int NG, const double2* u, double2* out, const double
 
 cudaError_t launch_scale2(double2* x, double sc, size_t n, cudaStream_t s) {
   k_scale2<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, sc, n);
+  return cudaGetLastError();
+}
+
+// Nyquist term of the exchange-energy gradient.  Ex = 1/2 occ dvcell
+// sum_ij <p_ij, Phi_ij p_ij>, p_ij = u_i conj(u_j) (src/Functions.f90:165-183).
+// Varying the conj(u_j) factor brings in conj(Phi_ij[p_ij]), which equals
+// Phi_ji[p_ji] except at the self-aliased Nyquist index; so the gradient is
+// 2 occ dvcell h[u] u plus, for column i,
+//   g_i += sc sum_j (kern_ji - kern_ij)[N/2] Nyq(p_ij) (-1)^m u_j,
+// Nyq(p) = sum_m (-1)^m p(m), sc = occ dvcell.  One CTA per column i; the
+// orbitals j are visited in order, each dot product reduced in a fixed order.
+constexpr int kNyqThreads = 256;
+__global__ void __launch_bounds__(kNyqThreads) k_energy_grad_nyquist(const double2* __restrict__ u, double2* g,
+                                                                      const double* __restrict__ kern, int N,
+                                                                      int nk, int nb, double sc) {
+  __shared__ double2 red[kNyqThreads / 32];
+  const int i = blockIdx.x, ki = i / nb;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const double2* ui = u + (size_t)i * N;
+  const int M = nk * nb;
+  constexpr int kMaxPer = 512 / kNyqThreads;    // N <= 512
+  double2 acc[kMaxPer];
+#pragma unroll
+  for (int r = 0; r < kMaxPer; ++r) acc[r] = make_double2(0.0, 0.0);
+  for (int j = 0; j < M; ++j) {
+    const int kj = j / nb;
+    if (kj == ki) continue;   // the two multipliers coincide
+    const double d = kern[(size_t)(kj - ki + nk - 1) * N + N / 2] - kern[(size_t)(ki - kj + nk - 1) * N + N / 2];
+    const double2* uj = u + (size_t)j * N;
+    double px = 0.0, py = 0.0;
+    for (int m = tid; m < N; m += kNyqThreads) {
+      const double sg = (m & 1) ? -1.0 : 1.0;
+      const double2 t = cmulc(ui[m], uj[m]);
+      px = fma(sg, t.x, px);
+      py = fma(sg, t.y, py);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      px += __shfl_xor_sync(0xffffffffu, px, o);
+      py += __shfl_xor_sync(0xffffffffu, py, o);
+    }
+    if (lane == 0) red[warp] = make_double2(px, py);
+    __syncthreads();
+    double2 c = red[0];
+    for (int w = 1; w < kNyqThreads / 32; ++w) c = cadd(c, red[w]);
+    __syncthreads();
+    const double2 f = make_double2(sc * d * c.x, sc * d * c.y);
+#pragma unroll
+    for (int r = 0; r < kMaxPer; ++r) {
+      const int m = tid + r * kNyqThreads;
+      if (m < N) {
+        const double sg = (m & 1) ? -1.0 : 1.0;
+        const double2 t = cmul(f, uj[m]);
+        acc[r] = make_double2(fma(sg, t.x, acc[r].x), fma(sg, t.y, acc[r].y));
+      }
+    }
+  }
+  double2* gi = g + (size_t)i * N;
+#pragma unroll
+  for (int r = 0; r < kMaxPer; ++r) {
+    const int m = tid + r * kNyqThreads;
+    if (m < N) gi[m] = cadd(gi[m], acc[r]);
+  }
+}
+
+cudaError_t launch_energy_grad_nyquist(const double2* u, double2* g, const double* kern, int NG, int nk, int nb,
+                                       double sc, cudaStream_t s) {
+  if (NG > 512) return cudaErrorInvalidValue;
+  k_energy_grad_nyquist<<<nk * nb, kNyqThreads, 0, s>>>(u, g, kern, NG, nk, nb, sc);
   return cudaGetLastError();
 }
 

@@ -720,13 +720,15 @@ cudaError_t launch_fock_sym(int NG, const FockSymArgs& a, cudaStream_t s) {
 }
 
 // Largest tile size (a power of two up to the teams of a full CTA) that still
-// yields enough tile pairs to occupy every SM several times; small systems
-// fall back to small tiles so their few pairs spread over many SMs.
-int choose_sym_tile(int NG, int M) {
+// yields enough tile pairs to occupy every one of the device's nsm SMs four
+// times; small systems fall back to small tiles so their few pairs spread over
+// many SMs.
+int choose_sym_tile(int NG, int M, int nsm) {
   int S = fock_sym_teams(NG);
+  const int want = 4 * (nsm > 0 ? nsm : 1);
   while (S > 1) {
     const int T = (M + S - 1) / S;
-    if (T * (T + 1) / 2 >= 4 * 152) break;
+    if (T * (T + 1) / 2 >= want) break;
     S >>= 1;
   }
   return S;

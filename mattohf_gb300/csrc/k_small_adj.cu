@@ -22,7 +22,10 @@
 //       pass A: out_a += i (phi_ab + (-1)^m dk_ab R_ab) mu_b,
 //         phi_ab = Phi_ab[v_a conj(v_b)], R_ab its Nyquist coefficient,
 //         dk_ab = kern_ba[N/2] - kern_ab[N/2];
-//       pass B: out_a += i v_b Phi_ab[mu_a conj(v_b) - v_a conj(mu_b)];
+//       pass B: out_a += i v_b (Phi_ab[mu_a conj(v_b) - v_a conj(mu_b)]
+//                              - dk_ab Nyq(v_a conj(mu_b)) (-1)^m),
+//         the second part being the Nyquist term of the transposed pair
+//         operator (see k_adjoint.cu), Nyq(f) = sum_m (-1)^m f(m);
 //     these are the row-a terms of the symmetric adjoint exchange (k_fock_adj)
 //     with the column terms written as the rows of the reversed pairs.  The
 //     transforms use the 32-lane latency plans, so a unit is one team;
@@ -202,16 +205,22 @@ __global__ void __launch_bounds__(kAdjThreads) k_small_adj(SmallAdjArgs a) {
       const double2* mB = a.mu + (size_t)bb * N;
       const double* kab = a.kern + (size_t)(ka - kb + a.nk - 1) * N;
       double2 x[E];
+      double n2x = 0.0, n2y = 0.0;   // pass B: Nyq(v_a conj(mu_b))
       if (!passB) {
         fft_team_in<N, -1, kAdjPlan>(InConjProduct<N, kAdjPlan>{vA, vB, tl}, x, buf, tw_s, tl);
       } else {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
           const int q = TM::pos(tl, e);
-          // mu_a conj(v_b) - v_a conj(mu_b): 4 + 4 FMA
-          const double2 t = cmulc(mA[q], vB[q]), va = vA[q], mb = mB[q];
-          x[e] = make_double2(fma(-va.y, mb.y, fma(-va.x, mb.x, t.x)), fma(va.x, mb.y, fma(-va.y, mb.x, t.y)));
+          const double sg = (q & 1) ? -1.0 : 1.0;
+          // mu_a conj(v_b) - v_a conj(mu_b)
+          const double2 t = cmulc(mA[q], vB[q]), t2 = cmulc(vA[q], mB[q]);
+          x[e] = csub(t, t2);
+          n2x = fma(sg, t2.x, n2x);
+          n2y = fma(sg, t2.y, n2y);
         }
+        n2x = team_sum<T>(n2x);
+        n2y = team_sum<T>(n2y);
         fft_team<N, -1, kAdjPlan>(x, buf, tw_s, tl);
       }
       // Nyquist coefficient (pass A) in slot (p=0, r=R0/2) of the team's lane 0
@@ -230,8 +239,15 @@ __global__ void __launch_bounds__(kAdjThreads) k_small_adj(SmallAdjArgs a) {
             acc[e] = cfma_i(pr, mB[q], acc[e]);
           }
         } else {
+          const double dk = __ldg(a.kern + (size_t)(kb - ka + a.nk - 1) * N + N / 2) - __ldg(kab + N / 2);
+          const double cx = dk * n2x, cy = dk * n2y;
 #pragma unroll
-          for (int e = 0; e < E; ++e) acc[e] = cfma_i(vB[TM::pos(tl, e)], x[e], acc[e]);
+          for (int e = 0; e < E; ++e) {
+            const int q = TM::pos(tl, e);
+            const double sg = (q & 1) ? -1.0 : 1.0;
+            const double2 y = make_double2(fma(-sg, cx, x[e].x), fma(-sg, cy, x[e].y));
+            acc[e] = cfma_i(vB[q], y, acc[e]);
+          }
         }
       }
     }

@@ -30,9 +30,15 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Host-side address of g_noalloc_scratch per device (the host symbol itself
-// is only a stand-in, not a device address).
+// Per device, resolved once with that device current: the device address of
+// g_noalloc_scratch (the host symbol itself is only a stand-in, not a device
+// address) and the device's multiprocessor count (the pair-chunking target).
+// The cache belongs to the CUDA runtime's primary context of each device: a
+// caller that resets a device (cudaDeviceReset) or makes another driver
+// context current invalidates it and must not call this entry point again in
+// that process.
 void* g_scratch_addr[kMaxDevices] = {nullptr};
+int g_scratch_nsm[kMaxDevices] = {0};
 std::mutex g_scratch_mu;
 
 __global__ void k_noalloc_prep(double2* tw, int NG, const double* vcq, double* kern, int total,
@@ -58,20 +64,24 @@ __global__ void k_noalloc_sum(const double2* __restrict__ part, int nchunks, int
   out[i] = f;
 }
 
-// Device address of the scratch array on the current device; resolved once
-// per device with that device current.
-int scratch_address(void** out) {
+// Device address of the scratch array and the multiprocessor count of the
+// current device; set up once per device with that device current.
+int scratch_setup(void** out, int* nsm) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return MATTOHF_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return MATTOHF_ERR_ARG;
   std::lock_guard<std::mutex> lk(g_scratch_mu);
   if (!g_scratch_addr[dev]) {
     void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr) return MATTOHF_ERR_CUDA;
+    int n = 0;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return MATTOHF_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
+      return MATTOHF_ERR_CUDA;
+    g_scratch_nsm[dev] = n;
     g_scratch_addr[dev] = p;
   }
   *out = g_scratch_addr[dev];
+  *nsm = g_scratch_nsm[dev];
   return MATTOHF_OK;
 }
 
@@ -90,9 +100,13 @@ extern "C" int mattohf_fock_noalloc(int NG, int NK, int NB, int NBocc, int nbw, 
   const size_t kern_bytes = align256(sizeof(double) * (size_t)(2 * NK - 1) * NG);
   const size_t col_bytes = sizeof(double2) * ncols * NG;  // one chunk of partials
   if (tw_bytes + kern_bytes + col_bytes > kNoAllocScratchBytes) return MATTOHF_ERR_TOO_LARGE;
+  void* base = nullptr;
+  int nsm = 0;
+  const int rc = scratch_setup(&base, &nsm);
+  if (rc != MATTOHF_OK) return rc;
   // same pair chunking as the context path, capped by the scratch budget
   const int npairs = NK * NBocc;
-  int nch = (152 * 8 + (int)ncols - 1) / (int)ncols;
+  int nch = (nsm * 8 + (int)ncols - 1) / (int)ncols;
   const int fit = (int)((kNoAllocScratchBytes - tw_bytes - kern_bytes) / col_bytes);
   nch = nch < fit ? nch : fit;
   nch = nch < npairs ? nch : npairs;
@@ -100,9 +114,6 @@ extern "C" int mattohf_fock_noalloc(int NG, int NK, int NB, int NBocc, int nbw, 
   const int chunk = (npairs + nch - 1) / nch;
   nch = (npairs + chunk - 1) / chunk;
 
-  void* base = nullptr;
-  const int rc = scratch_address(&base);
-  if (rc != MATTOHF_OK) return rc;
   unsigned char* b = static_cast<unsigned char*>(base);
   double2* tw = reinterpret_cast<double2*>(b);
   double* kern = reinterpret_cast<double*>(b + tw_bytes);

@@ -352,6 +352,36 @@ def ion_potential(cfg: Config, rx: np.ndarray) -> np.ndarray:
     return vion - vion.max()
 
 
+def ion_param_grad(cfg: Config, rx: np.ndarray, g: np.ndarray):
+    """dL/d(Zeff, alpha per species; Rion per ion) from dL/dvion = g on the grid,
+    by the chain rule through :func:`ion_potential`.  The max shift
+     contributes -(sum g) dvraw(x*)/dp at the grid point x* of the
+    maximum (the first one at a tie).  Extension: the reference has no
+    gradients."""
+    ax, NK = cfg.acell, cfg.NK
+    vraw = np.zeros_like(rx)
+    for ii in range(cfg.nion):
+        sp = cfg.Kion[ii] - 1
+        for icell in range(-4 * NK, 4 * NK + 1):
+            dist = np.abs(rx - ax * cfg.Rion[ii] - ax * icell)
+            vraw = vraw - float(cfg.Zeff[sp]) / np.sqrt(dist * dist + float(cfg.alpha[sp]) ** 2)
+    w = np.asarray(g, dtype=np.float64).copy()
+    w[int(np.argmax(vraw))] -= np.sum(g)
+    dZ = np.zeros(len(cfg.Zeff))
+    da = np.zeros(len(cfg.alpha))
+    dR = np.zeros(cfg.nion)
+    for ii in range(cfg.nion):
+        sp = cfg.Kion[ii] - 1
+        Za, al = float(cfg.Zeff[sp]), float(cfg.alpha[sp])
+        for icell in range(-4 * NK, 4 * NK + 1):
+            d = rx - ax * cfg.Rion[ii] - ax * icell
+            r = 1.0 / np.sqrt(d * d + al * al)
+            dZ[sp] += np.sum(w * -r)
+            da[sp] += np.sum(w * Za * al * r ** 3)
+            dR[ii] += np.sum(w * -ax * Za * d * r ** 3)
+    return dZ, da, dR
+
+
 # ---------------------------------------------------------------------------
 # Initial guess and orthonormalisation (src/mATTOHF.f90:134-196)
 # ---------------------------------------------------------------------------
@@ -688,8 +718,27 @@ def _zheev(a):
     return w, v
 
 
-def ks_ubk2_svd(sysm: System, ubk: np.ndarray, A0: float = 0.0) -> np.ndarray:
-    """Block-Krylov Rayleigh-Ritz (``KS_ubk2_SVD``, GS:124-194)."""
+def cgs2_block(blk: np.ndarray, weight: float) -> np.ndarray:
+    """Orthonormal basis of the rows of ``blk`` (m, NG) by classical
+    Gram-Schmidt applied twice per column, in column order, with the inner
+    product weight * <a|b>.  Not the reference's method: it is the
+    orthonormalisation the GPU path uses in place of ZGESVD('O') (GS:161-166),
+    restated here so the two choices can be compared on the same inputs."""
+    q = blk.copy()
+    for j in range(q.shape[0]):
+        c = q[j]
+        for _ in range(2 if j > 0 else 0):
+            z = weight * (np.conj(q[:j]) @ c)
+            c = c - z @ q[:j]
+        q[j] = c / math.sqrt(weight * float(np.real(np.vdot(c, c))))
+    return q
+
+
+def ks_ubk2_svd(sysm: System, ubk: np.ndarray, A0: float = 0.0, ortho: str = "svd") -> np.ndarray:
+    """Block-Krylov Rayleigh-Ritz (``KS_ubk2_SVD``, GS:124-194).
+
+    ``ortho="svd"`` is the reference's ZGESVD('O') basis; ``ortho="cgs2"``
+    swaps in :func:`cgs2_block` (the GPU path's choice) for comparisons."""
     from scipy.linalg import lapack
     NK, NB, NG, NCG = sysm.NK, sysm.NB, sysm.NG, sysm.cfg.NCG
     m = NB * NCG
@@ -699,6 +748,9 @@ def ks_ubk2_svd(sysm: System, ubk: np.ndarray, A0: float = 0.0) -> np.ndarray:
         work[:, NB * iCG:NB * (iCG + 1)] = ubkwbk_hwbk(
             sysm, ubk, work[:, NB * (iCG - 1):NB * iCG], A0)
     for ik in range(NK):                                        # GS:161-166
+        if ortho == "cgs2":
+            work[ik] = cgs2_block(work[ik], sysm.dvcell)
+            continue
         a = np.asfortranarray(work[ik].T)                       # (NG, m)
         u_, s_, vt_, info = lapack.zgesvd(a, compute_uv=1, full_matrices=0)
         if info != 0:
@@ -747,8 +799,8 @@ class GSResult:
     Ecomps: np.ndarray
 
 
-def gs_calculation(sysm: System, ubk: np.ndarray, nscf: Optional[int] = None) -> GSResult:
-    """SCF loop (``GS_calculation``, GS:26-60)."""
+def gs_calculation(sysm: System, ubk: np.ndarray, nscf: Optional[int] = None, ortho: str = "svd") -> GSResult:
+    """SCF loop (``GS_calculation``, GS:26-60); ``ortho`` as in :func:`ks_ubk2_svd`."""
     nscf = sysm.cfg.Nscf if nscf is None else nscf
     u = ubk.copy()
     dnsmix = 0.5
@@ -760,7 +812,7 @@ def gs_calculation(sysm: System, ubk: np.ndarray, nscf: Optional[int] = None) ->
     eps = err = None
     for it in range(nscf):
         u = gram_schmidt(sysm, u)
-        u = ks_ubk2_svd(sysm, u, 0.0)
+        u = ks_ubk2_svd(sysm, u, 0.0, ortho)
         u = gram_schmidt(sysm, u)
         u = subspace_diag(sysm, u, 0.0)
         Et[it + 1] = ubk_Etot(sysm, u, 0.0)
@@ -826,6 +878,19 @@ def _pair_potential(S: System, ki: int, kj: int, rho: np.ndarray) -> np.ndarray:
     return fftb(-v * g / float(S.NG))
 
 
+def _pair_potential_reflected(S: System, ki: int, kj: int, rho: np.ndarray) -> np.ndarray:
+    """Phi~_ji[rho]: the pair convolution with multiplier m_ji(-G), where m_ji(G)
+    = -vCGkk(G, kj, ki)/(NG NK) is Phi_ji's.  Because v is even this equals
+    Phi_ij (multiplier m_ij(G)) at every G except the self-aliased Nyquist index
+    NG/2 (Gx = -NG/2 bx, src/Initialization.f90:97-102), where -G is G itself and
+    the multiplier stays m_ji.  It is the operator that the transpose of the
+    map dv_j -> Phi_ij[v_i conj(dv_j)] brings in."""
+    v = S.vCGkk[ki * S.NK + kj].copy()
+    v[S.NG // 2] = S.vCGkk[kj * S.NK + ki][S.NG // 2]
+    g = fftf(rho / float(S.NK))
+    return fftb(-v * g / float(S.NG))
+
+
 def velocity(S: System, u: np.ndarray, A: float) -> np.ndarray:
     """P_A u = IFFT((G+k+A) FFT(u)/NG) per column (the operator inside ubk_Je, F:306-310)."""
     GkA = S.Gx[None, :] + S.kx[:, None] + A            # (NK, NG)
@@ -845,7 +910,9 @@ def hf_vjp(S: System, v: np.ndarray, mu: np.ndarray, A: float) -> np.ndarray:
     if S.hf:
         # exchange operator's dependence on v:
         #   out_i += i sum_j conj(phi_ji) mu_j,  phi_ji = Phi_ji[v_j conj(v_i)]
-        #   out_i += -i sum_j v_j Phi_ij[v_i conj(mu_j)]
+        #   out_i += -i sum_j v_j Phi~_ji[v_i conj(mu_j)]   (the transpose of
+        #            dv_j -> Phi_ij[v_i conj(dv_j)]; Phi~_ji differs from Phi_ij
+        #            only at the Nyquist index)
         for ki in range(NK):
             for bi in range(NB):
                 acc = np.zeros(S.NG, dtype=np.complex128)
@@ -853,7 +920,8 @@ def hf_vjp(S: System, v: np.ndarray, mu: np.ndarray, A: float) -> np.ndarray:
                     for bj in range(NB):
                         phi_ji = _pair_potential(S, kj, ki, v[kj, bj] * np.conj(v[ki, bi]))
                         acc += 1j * np.conj(phi_ji) * mu[kj, bj]
-                        acc += -1j * v[kj, bj] * _pair_potential(S, ki, kj, v[ki, bi] * np.conj(mu[kj, bj]))
+                        acc += -1j * v[kj, bj] * _pair_potential_reflected(S, ki, kj,
+                                                                           v[ki, bi] * np.conj(mu[kj, bj]))
                 out[ki, bi] += acc
     return out
 
@@ -864,9 +932,26 @@ def _field_grad(S: System, lam_k: np.ndarray, v: np.ndarray, a: float) -> float:
 
 
 def objective_grad_u(S: System, u: np.ndarray, A: float, objective: str) -> np.ndarray:
-    """Gradient g of the objective w.r.t. u (dL = <g, du>_R)."""
+    """Gradient g of the objective w.r.t. u (dL = <g, du>_R).
+
+    Energy: 2 occ dvcell h[u] u, plus a Nyquist term of the exchange energy.
+    Ex = 1/2 occ dvcell sum_ij <p_ij, Phi_ij p_ij> with p_ij = u_i conj(u_j)
+    (F:165-183); varying the conj(u_j) factor brings in conj(Phi_ij[p_ij]),
+    which is Phi_ji[p_ji] except at the self-aliased Nyquist index, so
+      g_i += occ dvcell sum_j (m_ji - m_ij)(N/2) Nyq(p_ij) (-1)^x u_j,
+    with m_ij = -vCGkk(:, ki, kj)/(NG NK) and Nyq(p) = sum_x (-1)^x p(x)."""
     if objective == "energy":
-        return 2.0 * S.occbk[:, :, None] * S.dvcell * ubkwbk_hwbk(S, u, u, A)
+        g = 2.0 * S.occbk[:, :, None] * S.dvcell * ubkwbk_hwbk(S, u, u, A)
+        if S.hf:
+            NK, NG, NBo = S.NK, S.NG, S.NBocc
+            sg = (-1.0) ** np.arange(NG)
+            occ = 2.0 / float(NK)
+            m = -S.vCGkk[:, NG // 2].reshape(NK, NK) / float(NG * NK)   # m[ki, kj] at N/2
+            nyq = np.einsum("ibx,jcx,x->ibjc", u[:, :NBo], np.conj(u[:, :NBo]), sg)
+            d = (m.T - m)[:, None, :, None]                             # m_ji - m_ij
+            corr = np.einsum("ibjc,jcx->ibx", d * nyq, u[:, :NBo]) * sg
+            g[:, :NBo] += occ * S.dvcell * corr
+        return g
     if objective == "current":
         return -2.0 * S.occbk[:, :, None] * (S.dvcell / S.vcell) * velocity(S, u, A)
     raise ValueError(objective)

@@ -58,8 +58,39 @@ def test_adjoint_rejects_unoccupied_bands(built_lib):
     assert ei.value.status == _capi.ERR_ARG
 
 
-def test_adjoint_finite_differences_gpu(built_lib):
-    """Central differences (h = 1e-6) of the GPU objective on random samples agree to 1e-6."""
+def fd_check(obj, A, g, samples, h_small=1e-6, h_large=1e-4):
+    """Per-sample central differences of `obj` against the adjoint gradient g.
+
+    h_large = 1e-4: truncation (h^2) and round-off stay far below 1e-7 of each
+    sample, so that is the bound.  h_small = 1e-6: the quotient carries the
+    round-off of two full propagations (about 1e-15 absolute in L, so ~1e-9 in
+    the quotient), which exceeds 1e-6 of the smaller samples; its size is
+    estimated per sample from the spread between the quotients at h and
+    1.25 h (independent round-off, negligible truncation), and the bound is
+    1e-6 |fd| + 3 x that spread.  Returns the per-sample table."""
+    rows = []
+    for n in samples:
+        q = {}
+        for h in (h_large, h_small, 1.25 * h_small):
+            Ap, Am = A.copy(), A.copy()
+            Ap[n] += h
+            Am[n] -= h
+            q[h] = (obj(Ap) - obj(Am)) / (2 * h)
+        spread = abs(q[h_small] - q[1.25 * h_small])
+        rows.append((int(n), g[n], q[h_large], q[h_small], spread))
+    print("  n        g              fd(1e-4) rel     fd(1e-6) rel     round-off bound (rel)")
+    for n, gn, fl, fs, sp in rows:
+        print(f"  {n:5d}  {gn: .6e}  {abs(gn - fl) / abs(fl):.2e}         {abs(gn - fs) / abs(fs):.2e}"
+              f"         {3 * sp / abs(fs):.2e}")
+    for n, gn, fl, fs, sp in rows:
+        assert abs(gn - fl) <= 1e-7 * abs(fl) + 1e-14, (n, gn, fl)
+        assert abs(gn - fs) <= 1e-6 * abs(fs) + 3 * sp + 1e-14, (n, gn, fs, sp)
+    return rows
+
+
+@pytest.mark.parametrize("objective", ["energy", "current"])
+def test_adjoint_finite_differences_gpu(built_lib, objective):
+    """Central differences of the GPU objective on random samples, per sample."""
     from mattohf_gb300 import Context
     cfg = _cfg(NG=64, NK=4, NB=2, NBocc=2, acell=10.0)
     rng = np.random.default_rng(5)
@@ -70,19 +101,42 @@ def test_adjoint_finite_differences_gpu(built_lib):
         ctx.Init_wf()
         ctx.Gram_Schmidt()
         u0 = ctx.get_orbitals()
-        L, g, _ = ctx.adjoint(A, dt, "energy", ckpt_every=5)
+        L, g, _ = ctx.adjoint(A, dt, objective, ckpt_every=5)
 
         def obj(Ax):
             ctx.set_orbitals(u0)
-            return ctx.adjoint(Ax, dt, "energy", ckpt_every=nt)[0]
+            return ctx.adjoint(Ax, dt, objective, ckpt_every=nt)[0]
 
-        h = 1e-6
-        for n in rng.choice(nt, size=6, replace=False):
-            Ap, Am = A.copy(), A.copy()
-            Ap[n] += h
-            Am[n] -= h
-            fd = (obj(Ap) - obj(Am)) / (2 * h)
-            assert abs(g[n] - fd) <= 1e-6 * np.max(np.abs(g)) + 2e-10, (n, g[n], fd)
+        fd_check(obj, A, g, rng.choice(nt, size=6, replace=False))
+
+
+def test_adjoint_finite_differences_differentiation_shape(built_lib):
+    """The differentiation workload's shape (a = 10, one ion of charge 2 at a/2,
+    NG = 128, NK = 16, NB = NBocc = 2, dt = 2.5e-3, control = the A0 = 0.05,
+    w = 0.057, T = 100 pulse plus N(0, 1e-3) noise, seed 2), truncated to 400
+    steps: the absorbed-energy gradient against central differences on 12
+    random samples, per sample (fd_check)."""
+    from mattohf_gb300 import Context, RunConfig, aave_from_samples, define_afield
+    nt = 400
+    cfg = RunConfig.from_pulse(0.05, 0.057, 100.0, acell=10.0, NG=128, NK=16, NB=2, NBocc=2, Zeff=[2.0],
+                               alpha=[1.0], Rion=[0.5], Kion=[1], dt=2.5e-3, NT=nt)
+    rng = np.random.default_rng(2)
+    A = define_afield(cfg)[1] + 1e-3 * rng.standard_normal(nt)
+    with Context(cfg) as ctx:
+        ctx.Init_wf()
+        ctx.Gram_Schmidt()
+        ctx.GS_calculation(5, 4)
+        u0 = ctx.get_orbitals()
+        E0 = ctx.observables(0.0)["Etot"]
+        L, g, _ = ctx.adjoint(A, cfg.dt, "energy", ckpt_every=100)
+
+        def obj(Ax):          # the plain forward: Etot(u_nt, A[nt-1]) - Etot(u_0, 0)
+            ctx.set_orbitals(u0)
+            E, _, _ = ctx.rk4_run(Ax, aave_from_samples(Ax), cfg.dt)
+            return E[-1] - E0
+
+        assert abs(obj(A) - L) <= 1e-12 * max(1.0, abs(L))
+        fd_check(obj, A, g, rng.choice(nt, size=12, replace=False))
 
 
 @pytest.mark.parametrize("NG,NK,NB", [(16, 3, 2), (32, 5, 1), (64, 4, 2), (128, 8, 2), (256, 3, 3)])
@@ -116,3 +170,55 @@ def test_fused_reverse_stages_match_separate_launches(built_lib, NG, NK, NB, obj
         assert np.max(np.abs(v1 - v0)) <= 1e-11 * np.max(np.abs(v0))
     # the checkpoint modes of the fused path agree bitwise
     assert np.array_equal(out[1, 0][1], out[1, 3][1])
+
+
+def test_ion_parameter_gradients(built_lib):
+    """dL/d(Zeff, alpha) per species and dL/dRion per ion of the absorbed energy
+    (the adjoint's dL/dvion carried through the ion potential and its max
+    shift, src/Prep_periodic_ion_potential.f90:10-20) against the oracle's chain
+    rule on the same dL/dvion (1e-12), and against central differences of the
+    plain forward objective with the ion potential rebuilt for each perturbed
+    parameter (h = 1e-5; 1e-6 relative)."""
+    from mattohf_gb300 import Context, RunConfig, aave_from_samples
+    from oracle import mattohf_oracle as O
+    from conftest import to_oracle_config
+    import dataclasses
+    cfg = RunConfig(acell=10.0, NG=128, NK=8, NB=2, NBocc=2, Zeff=[1.5, 0.5], alpha=[1.0, 1.0],
+                    Rion=[0.25, 0.75], Kion=[1, 2])
+    nt, dt = 60, 2.5e-3
+    rng = np.random.default_rng(12)
+    A = 0.05 * np.sin(0.05 * np.arange(1, nt + 1)) + 1e-3 * rng.standard_normal(nt)
+    ocfg = to_oracle_config(cfg)
+    rx = np.arange(cfg.NG) / cfg.NG * cfg.acell
+    with Context(cfg) as ctx:
+        ctx.Init_wf()
+        ctx.Gram_Schmidt()
+        u0 = ctx.get_orbitals()
+        L, g, gv = ctx.adjoint(A, dt, "energy", ckpt_every=0)
+        grad = ctx.ion_param_grad(gv)
+        dZ, da, dR = O.ion_param_grad(ocfg, rx, gv)
+        for k, ref in (("Zeff", dZ), ("alpha", da), ("Rion", dR)):
+            assert np.max(np.abs(grad[k] - ref)) <= 1e-12 * np.max(np.abs(ref)), k
+        vion0 = ctx.vion
+
+        def obj(**kw):
+            ctx.vion = O.ion_potential(dataclasses.replace(ocfg, **kw), rx)
+            ctx.set_orbitals(u0)
+            E0 = ctx.observables(0.0)["Etot"]
+            E, _, _ = ctx.rk4_run(A, aave_from_samples(A), dt)
+            return E[-1] - E0
+
+        h = 1e-5
+        rows = []
+        for name in ("Zeff", "alpha", "Rion"):
+            for i in range(len(getattr(cfg, name))):
+                p, m = list(getattr(cfg, name)), list(getattr(cfg, name))
+                p[i] += h
+                m[i] -= h
+                fd = (obj(**{name: p}) - obj(**{name: m})) / (2 * h)
+                rows.append((name, i, grad[name][i], fd))
+        ctx.vion = vion0
+    for name, i, gn, fd in rows:
+        print(f"  dL/d{name}[{i}] = {gn: .10e}   central difference {fd: .10e}   rel {abs(gn - fd) / abs(fd):.1e}")
+    for name, i, gn, fd in rows:
+        assert abs(gn - fd) <= 1e-6 * abs(fd), (name, i, gn, fd)

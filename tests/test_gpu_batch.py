@@ -138,3 +138,31 @@ def test_batch_autotune_restores_state_and_keeps_results(built_lib):
             E, J, N = b.rk4_run(A, Aave, dts)
             assert np.max(np.abs(E - E0)) <= 1e-13 * np.max(np.abs(E0)), tile
             assert np.max(np.abs(J - J0)) <= 1e-13 * max(1.0, np.max(np.abs(J0))), tile
+
+
+@pytest.mark.parametrize("ckpt", [0, 3])
+def test_batch_adjoint_matches_single_runs(built_lib, ckpt):
+    """mattohf_batch_adjoint gives every member the gradients of mattohf_adjoint
+    run on that member alone (1e-11), for uneven members, both objectives'
+    energy form and an explicit and a fitted checkpoint interval."""
+    from mattohf_gb300 import Batch, RunConfig
+    cfgs = [RunConfig(acell=a, NG=64, NK=k, NB=b, NBocc=b, Zeff=[2.0], alpha=[1.0], Rion=[0.5], Kion=[1])
+            for a, k, b in [(10.0, 4, 2), (8.0, 6, 1), (12.0, 3, 3)]]
+    nt = 10
+    rng = np.random.default_rng(21)
+    A = 0.05 * np.sin(0.2 * np.arange(1, nt + 1))[None, :] + 1e-3 * rng.standard_normal((len(cfgs), nt))
+    dts = np.array([2e-3, 1.5e-3, 2.5e-3])
+    with Batch(cfgs) as b:
+        u0 = []
+        for r in range(len(cfgs)):
+            b[r].Init_wf()
+            b[r].Gram_Schmidt()
+            u0.append(b[r].get_orbitals())
+        L, g, gv = b.adjoint(A, dts, "energy", ckpt_every=ckpt)
+        for r in range(len(cfgs)):
+            b[r].set_orbitals(u0[r])
+            Lr, gr, gvr = b[r].adjoint(A[r], dts[r], "energy", ckpt_every=ckpt)
+            assert abs(L[r] - Lr) <= 1e-11 * max(1.0, abs(Lr))
+            assert np.max(np.abs(g[r] - gr)) <= 1e-11 * np.max(np.abs(gr))
+            assert np.max(np.abs(gv[r] - gvr)) <= 1e-11 * np.max(np.abs(gvr))
+        assert b.last_run_ms() > 0

@@ -326,14 +326,33 @@ def test_nonfinite_detected(small):
     assert "step" in str(ei.value)
 
 
+def gs_errors(got, ref, S, dns):
+    """Gauge-invariant deviations of a GPU ground state from the oracle's: Etot of
+    every iteration (relative per iteration), final Ritz values and
+    eigen-residuals (the reference's sum of abs, not abs^2, F:353; max-norm
+    relative), Je of every iteration (absolute) and the final density."""
+    from oracle import mattohf_oracle as O
+    return {"Etot": float(np.max(np.abs(got["Etot"] - ref.Etot) / np.abs(ref.Etot))),
+            "epsbk": rel(got["epsbk"], ref.epsbk),
+            "epserrorbk": rel(got["epserrorbk"], ref.epserrorbk),
+            "Je": float(np.max(np.abs(got["Je"] - ref.Je))),
+            "density": rel(dns, O.ubk_dns(S, ref.ubk))}
+
+
+def check_gs(label, errs, bound):
+    print(f"{label}: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+    for k, v in errs.items():
+        assert v <= bound[k], (label, k, v, bound[k])
+
+
 @pytest.mark.parametrize("name,ncg", [("ng32_nk4", 4), ("ng16_nk3_unocc", 2), ("ng16_nk3_unocc", 3),
                                       ("ng64_nk4_nb1", 5)])  # Krylov dimension 8, 6, 9 and 5
 def test_gs_gauge_invariants(name, ncg):
     """SCF iterations against the oracle.  A Krylov block amplifies rounding in
-    the h-applies: at NG=128, NB=3, NCG=3 a relative 1e-13 perturbation of h
-    alone moves the oracle's Je by 2.5e-10 and its Ritz values by 3.5e-9, so
-    the cases here are ones whose blocks are well conditioned (the same
-    perturbation moves Je by < 1e-13), odd Krylov dimensions included."""
+    the h-applies, so each case's bounds sit 100x above what a relative 1e-13
+    perturbation of every h-apply does to the oracle (measured on these cases:
+    Etot <= 2.3e-13, epsbk <= 1.1e-12, epserrorbk <= 1.4e-11, Je <= 1.8e-13,
+    density <= 2.1e-12).  Odd Krylov dimensions are included."""
     from oracle import mattohf_oracle as O
     cfg, ctx, S = setup(name)
     u0 = O.gram_schmidt(S, O.init_wf(S))
@@ -342,17 +361,17 @@ def test_gs_gauge_invariants(name, ncg):
     ref = O.gs_calculation(S, u0, nscf=nscf)
     ctx.set_orbitals(u0)
     got = ctx.GS_calculation(nscf, ncg)
-    assert np.max(np.abs(got["Etot"] - ref.Etot)) <= 1e-9 * np.max(np.abs(ref.Etot))
-    assert np.max(np.abs(got["epsbk"] - ref.epsbk)) <= 1e-8 * np.max(np.abs(ref.epsbk))
-    assert np.max(np.abs(got["Je"] - ref.Je)) <= 1e-9
-    # density is gauge invariant
-    assert rel(ctx.ubk_dns(ctx.get_orbitals()), O.ubk_dns(S, ref.ubk)) <= 1e-8
+    errs = gs_errors(got, ref, S, ctx.ubk_dns(ctx.get_orbitals()))
+    check_gs(f"GS {name} ncg={ncg}", errs,
+             {"Etot": 1e-11, "epsbk": 1e-10, "epserrorbk": 1e-9, "Je": 1e-11, "density": 1e-10})
 
 
 def test_gs_wide_krylov_block():
     """Krylov dimension 48 (NB=24, NCG=2): the eigensolver's and the staged
     Gram-Schmidt's shared memory exceed 48 KB.  A relative 1e-13 perturbation
-    of h moves the oracle's Ritz values by 8e-11 here, well inside the bounds."""
+    of every h-apply moves the oracle by Etot 4.5e-12, epsbk 7.7e-11,
+    epserrorbk 8.2e-9, Je 3.2e-11 and the density 1.4e-9; the bounds sit 10x
+    above (Etot and Je 100x)."""
     from mattohf_gb300 import Context
     from oracle import mattohf_oracle as O
     cfg = make_cfg(NG=128, NK=1, NB=24, NBocc=24)
@@ -364,9 +383,40 @@ def test_gs_wide_krylov_block():
     with Context(cfg) as ctx:
         ctx.set_orbitals(u0)
         got = ctx.GS_calculation(nscf, ncg)
-    assert np.max(np.abs(got["Etot"] - ref.Etot)) <= 1e-9 * np.max(np.abs(ref.Etot))
-    assert np.max(np.abs(got["epsbk"] - ref.epsbk)) <= 1e-8 * np.max(np.abs(ref.epsbk))
-    assert np.max(np.abs(got["Je"] - ref.Je)) <= 1e-9
+        errs = gs_errors(got, ref, S, ctx.ubk_dns(ctx.get_orbitals()))
+    check_gs("GS wide block", errs, {"Etot": 1e-9, "epsbk": 1e-9, "epserrorbk": 1e-7, "Je": 1e-9,
+                                     "density": 1e-8})
+
+
+def test_gs_krylov_block_in_global_memory():
+    """Krylov dimension 48 at NG=256 (NB=24, NCG=2): the block of a k-point is
+    48*256*16 B = 192 KB, above the 160 KB shared-memory staging limit, so the
+    Krylov Gram-Schmidt (classical, applied twice) runs on global memory.  A
+    relative 1e-13 perturbation of every h-apply moves the oracle by Etot
+    2.5e-10, epsbk 8.6e-10, epserrorbk 6.7e-8, Je 7.3e-11 and the density
+    5.0e-9; the bounds sit 10x above that, except for Je.  At one k-point
+    (kx = 0) with real Gaussian orbitals the current vanishes by symmetry but
+    for the unpaired Nyquist component G = -NG/2 bx (src/Initialization.f90:97-102),
+    so Je (about 2.5e-6 here) measures the orbitals' highest-frequency content,
+    where the Krylov block [u, hu] holds its largest and the GPU's transforms
+    and orthonormalisation round differently from the oracle's (measured
+    5.9e-9).  Its bound is 2e-8 absolute."""
+    from mattohf_gb300 import Context
+    from oracle import mattohf_oracle as O
+    cfg = make_cfg(NG=256, NK=1, NB=24, NBocc=24)
+    S = O.make_system(to_oracle_config(cfg), vCk=O.k_vCk_fast)
+    nscf, ncg = 3, 2
+    S.cfg = dataclasses.replace(S.cfg, NCG=ncg)
+    u0 = O.gram_schmidt(S, O.init_wf(S))
+    ref = O.gs_calculation(S, u0, nscf=nscf)
+    with Context(cfg) as ctx:
+        vCG, vCq = ctx.coulomb()
+        assert rel(vCG, S.vCG) <= TOL_OP and rel(vCq[0], S.vCGkk[0]) <= TOL_OP
+        ctx.set_orbitals(u0)
+        got = ctx.GS_calculation(nscf, ncg)
+        errs = gs_errors(got, ref, S, ctx.ubk_dns(ctx.get_orbitals()))
+    check_gs("GS block in global memory", errs, {"Etot": 3e-9, "epsbk": 1e-8, "epserrorbk": 1e-6, "Je": 2e-8,
+                                                  "density": 5e-8})
 
 
 @pytest.mark.parametrize("ng,nb", [(64, 5), (512, 24)])

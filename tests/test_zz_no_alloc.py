@@ -47,6 +47,41 @@ def test_fock_noalloc_matches_fock(built_lib):
             assert _rel(got, ref) <= TOL, (call, _rel(got, ref))
 
 
+def test_fock_noalloc_matches_oracle_ng512(built_lib):
+    """A second shape, NG=512, NK=4, NB=NBocc=4 with nbw=4, against the oracle's
+    ubkwbk_vFwbk (src/Functions.f90:237-261) with the context's Coulomb table;
+    two calls in a row."""
+    import torch
+    from mattohf_gb300 import Context, RunConfig, _capi
+    from conftest import to_oracle_config
+    from oracle import mattohf_oracle as O
+
+    cfg = RunConfig(acell=11.0, NG=512, NK=4, NB=4, NBocc=4, Zeff=[1.0], alpha=[1.0], Rion=[0.3], Kion=[1])
+    nbw = 4
+    with Context(cfg) as ctx:
+        vCG, vCq = ctx.coulomb()
+    S = O.make_system(to_oracle_config(cfg), vCk=lambda k, *a: np.zeros(np.shape(k)))
+    NK = cfg.NK
+    S.vCGkk = vCq[(np.arange(NK)[:, None] - np.arange(NK)[None, :] + NK - 1).reshape(-1)]
+    S.vCG = vCG
+    d_vcq = torch.from_numpy(np.ascontiguousarray(vCq)).cuda()
+    rng = np.random.default_rng(7)
+    for call in range(2):
+        u = O.gram_schmidt(S, rng.standard_normal((NK, cfg.NB, cfg.NG)) + 1j * rng.standard_normal((NK, cfg.NB, cfg.NG)))
+        w = u if call == 1 else rng.standard_normal((NK, nbw, cfg.NG)) + 1j * rng.standard_normal((NK, nbw, cfg.NG))
+        ref = O.ubkwbk_vFwbk(S, u, w)
+        d_u = torch.from_numpy(u.view(np.float64).copy()).cuda()
+        d_w = torch.from_numpy(np.ascontiguousarray(w).view(np.float64).copy()).cuda()
+        d_out = torch.full_like(d_w, float("nan"))
+        torch.cuda.synchronize()
+        st = built_lib.mattohf_fock_noalloc(cfg.NG, NK, cfg.NB, cfg.NBocc, nbw, d_vcq.data_ptr(), d_u.data_ptr(),
+                                            d_w.data_ptr(), d_out.data_ptr(), None)
+        assert st == _capi.OK, st
+        torch.cuda.synchronize()
+        got = d_out.cpu().numpy().view(np.complex128).reshape(ref.shape)
+        assert _rel(got, ref) <= TOL, (call, _rel(got, ref))
+
+
 def test_fock_noalloc_rejects_oversize(built_lib):
     """Sizes whose partial sums exceed the fixed scratch are refused before any launch."""
     from mattohf_gb300 import _capi
