@@ -623,45 +623,72 @@ def run_small(args):
     print(json.dumps(measure_small()), flush=True)
 
 
-def run_large(args):
-    """Largest configuration shape, one variant: a = 12, NG = 512, NK = 128,
-    NB = Nocc = 8, three ions (Z=1 at a/6, a/2, 5a/6), dt = 2.5e-4 (the
-    configured 0.01 is RK4-unstable here).  RK4 steps/s in FP64 and with the
-    double-float exchange, and the adjoint/forward ratio over a short window.
-    """
-    from mattohf_gb300 import Context, RunConfig, define_afield, aave_from_samples, _capi
+def measure_large(variants: int, K: int, W: int) -> dict:
+    """The largest configuration: a = 12, NG = 512, NK = 128, NB = Nocc = 8,
+    three ions (Z = 1 at a/6, a/2, 5a/6), `variants` pulse variants (A0 in
+    U[0.02, 0.2], w in U[0.04, 0.08], T = 200, seed 3), dt = 2.5e-4 (the
+    configured 0.01 is RK4-unstable here).  Every variant forward for a window
+    of K steps as one batch, then the adjoint of the absorbed energy for every
+    variant over the same window (mattohf_batch_adjoint: members in turn, each
+    with its checkpoint segment fitted to the free device memory, and once with
+    four segments and recomputation), and one variant alone with the
+    double-float exchange."""
     import dataclasses
-    K, W = args.steps, args.warmup
-    cfg = RunConfig.from_pulse(0.1, 0.06, 200.0, acell=12.0, NG=512, NK=128, NB=8, NBocc=8, Zeff=[1.0],
-                               alpha=[1.0], Rion=[1 / 6, 0.5, 5 / 6], Kion=[1, 1, 1], dt=2.5e-4, NT=W + K)
-    A = define_afield(cfg)[1]
-    Aave = aave_from_samples(A)
-    out = {"metric": "TDHF RK4 steps/s (largest shape, one variant)", "unit": "steps/s", "dtype": "f64",
-           "data": "synthetic", "steps": K, "warmup": W,
-           "config": {"workload": "a=12, NG=512, NK=128, Nocc=NB=8, 3 ions, dt=2.5e-4"}}
-    with Context(cfg) as ctx:
-        ctx.Init_wf()
-        ctx.Gram_Schmidt()
-        u0 = ctx.get_orbitals()
-        for mode, key in ((0, "value"), (1, "double_float_exchange")):
-            ctx.set_option(_capi.OPT_FOCK_DF64, mode)
-            ctx.set_orbitals(u0)
-            ctx.rk4_run(A[:W], Aave[:W], cfg.dt)
-            ctx.set_orbitals(u0)
-            ctx.rk4_run(A[W:], Aave[W:], cfg.dt)
-            out[key] = K / (ctx.last_run_timing()[0] * 1e-3)
-        ctx.set_option(_capi.OPT_FOCK_DF64, 0)
-        ctx.set_orbitals(u0)
-        ctx.rk4_run(A[:K], Aave[:K], cfg.dt)
-        t_fwd = ctx.last_run_timing()[0]
-        ctx.set_orbitals(u0)
-        ctx.adjoint(A[:K], cfg.dt, "energy", ckpt_every=max(1, K // 4))
-        out["adjoint_over_forward"] = ctx.adjoint_timing()[1] / t_fwd
-        # checkpoint interval fitted to device memory by the library
-        ctx.set_orbitals(u0)
-        ctx.adjoint(A[:K], cfg.dt, "energy", ckpt_every=0)
-        out["adjoint_over_forward_auto_checkpoint"] = ctx.adjoint_timing()[1] / t_fwd
-    print(json.dumps(out), flush=True)
+    from mattohf_gb300 import Batch, RunConfig, define_afield, _capi
+    rng = np.random.default_rng(3)
+    A0 = rng.uniform(0.02, 0.2, size=variants)
+    w = rng.uniform(0.04, 0.08, size=variants)
+    dt = 2.5e-4
+    cfgs = [RunConfig.from_pulse(float(A0[r]), float(w[r]), 200.0, acell=12.0, NG=512, NK=128, NB=8, NBocc=8,
+                                 Zeff=[1.0], alpha=[1.0], Rion=[1 / 6, 0.5, 5 / 6], Kion=[1, 1, 1], dt=dt,
+                                 NT=W + K) for r in range(variants)]
+    t0 = time.perf_counter()
+    b = Batch(cfgs)
+    setup_s = time.perf_counter() - t0
+    A = np.stack([define_afield(c)[1] for c in cfgs])
+    Aave = np.concatenate([0.5 * A[:, :1], 0.5 * (A[:, 1:] + A[:, :-1])], axis=1)
+    b[0].Init_wf()
+    b[0].Gram_Schmidt()
+    u0 = b[0].get_orbitals()
+    for r in range(1, variants):
+        b[r].set_orbitals(u0)
+    b.rk4_run(A[:, :W], Aave[:, :W], dt)                  # warm-up and graph capture
+    for r in range(variants):
+        b[r].set_orbitals(u0)
+    b.rk4_run(A[:, W:], Aave[:, W:], dt)
+    t_fwd = b.last_run_ms()
+    for r in range(variants):
+        b[r].set_orbitals(u0)
+    b.adjoint(A[:, W:], dt, "energy", ckpt_every=0)
+    t_adj = b.last_run_ms()
+    for r in range(variants):
+        b[r].set_orbitals(u0)
+    b.adjoint(A[:, W:], dt, "energy", ckpt_every=max(1, K // 4))
+    t_adj_ck = b.last_run_ms()
+    m = b[0]
+    m.set_option(_capi.OPT_FOCK_DF64, 1)
+    m.set_orbitals(u0)
+    m.rk4_run(A[0, :W], Aave[0, :W], dt)
+    m.set_orbitals(u0)
+    m.rk4_run(A[0, W:], Aave[0, W:], dt)
+    t_df = m.last_run_timing()[0]
+    m.set_option(_capi.OPT_FOCK_DF64, 0)
+    b.close()
+    return {"metric": "TDHF RK4 steps/s (largest shape, batched pulse variants)",
+            "value": variants * K / (t_fwd * 1e-3), "unit": "run-steps/s", "per_variant_steps_per_s":
+            K / (t_fwd * 1e-3 / variants), "dtype": "f64", "data": "synthetic", "steps": K, "warmup": W,
+            "variants": variants, "forward_ms": t_fwd,
+            "adjoint": {"value": t_adj / t_fwd, "unit": "batched adjoint / batched forward time", "adjoint_ms": t_adj,
+                        "checkpoint": "fitted to free memory (every stage input of the window stored)",
+                        "four_segments": {"value": t_adj_ck / t_fwd, "adjoint_ms": t_adj_ck,
+                                          "checkpoint": f"every {max(1, K // 4)} steps, recomputation"}},
+            "double_float_exchange_one_variant": K / (t_df * 1e-3),
+            "config": {"workload": f"a=12, NG=512, NK=128, Nocc=NB=8, 3 ions, {variants} pulse variants, "
+                                   f"dt={dt}, window of {K} steps", "setup_s": setup_s}}
+
+
+def run_large(args):
+    print(json.dumps(measure_large(args.variants, args.steps, args.warmup)), flush=True)
 
 
 def main():
@@ -674,6 +701,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="plain", choices=["plain", "ensemble", "adjoint", "large", "small"])
     ap.add_argument("--runs", type=int, default=256)
+    ap.add_argument("--variants", type=int, default=32, help="pulse variants of --workload large")
     ap.add_argument("--adj-steps", type=int, default=4000)
     ap.add_argument("--fd-samples", type=int, default=32)
     ap.add_argument("--ens-steps", type=int, default=10, help="timed ensemble steps in the default line")

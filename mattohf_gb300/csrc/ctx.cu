@@ -13,6 +13,9 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <mutex>
+#include <tuple>
+#include <map>
 #include <algorithm>
 #include <functional>
 
@@ -708,9 +711,26 @@ void destroy_graph(mattohf_ctx* c) {
   }
 }
 
+// Coulomb tables already built in this process, by (acell, NG, NK): runs that
+// share a cell (pulse variants, repeated contexts) reuse the k_vCk sums, which
+// at NG = 512, NK = 128 take 1.7e11 terms.  Values are the kernel's own output,
+// bit for bit.  At most kTableCacheMax entries (1 MiB each at that size).
+constexpr size_t kTableCacheMax = 64;
+std::mutex g_table_mu;
+std::map<std::tuple<uint64_t, int, int>, std::vector<double>> g_tables;
+
 int compute_tables(mattohf_ctx* ctx) {
   const int NG = ctx->NG, NK = ctx->NK;
   const int nd = 2 * NK - 1;
+  uint64_t abits = 0;
+  std::memcpy(&abits, &ctx->acell, sizeof abits);
+  const auto key = std::make_tuple(abits, NG, NK);
+  std::vector<double> cached;
+  {
+    std::lock_guard<std::mutex> lk(g_table_mu);
+    auto it = g_tables.find(key);
+    if (it != g_tables.end()) cached = it->second;
+  }
   std::vector<double> q((size_t)nd * NG + NG);
   for (int d = 0; d < nd; ++d) {
     const int diff = d - (NK - 1);              // kr - kc
@@ -722,11 +742,21 @@ int compute_tables(mattohf_ctx* ctx) {
   double* d_q = nullptr;
   double* d_all = nullptr;
   double* d_g = nullptr;
-  CKR(dalloc(ctx, &d_q, q.size()));
   CKR(dalloc(ctx, &d_all, q.size()));
-  CKR(dalloc(ctx, &d_g, (size_t)vck_points(ctx->acell, NG, NK)));
-  CK(cudaMemcpyAsync(d_q, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-  CK(launch_vck_table(NG, NK, ctx->acell, d_q, (int)q.size(), d_g, d_all, ctx->st));
+  if (cached.size() == q.size()) {
+    CK(cudaMemcpyAsync(d_all, cached.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+  } else {
+    CKR(dalloc(ctx, &d_q, q.size()));
+    CKR(dalloc(ctx, &d_g, (size_t)vck_points(ctx->acell, NG, NK)));
+    CK(cudaMemcpyAsync(d_q, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    CK(launch_vck_table(NG, NK, ctx->acell, d_q, (int)q.size(), d_g, d_all, ctx->st));
+    std::vector<double> h(q.size());
+    CK(cudaMemcpyAsync(h.data(), d_all, q.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    std::lock_guard<std::mutex> lk(g_table_mu);
+    if (g_tables.size() >= kTableCacheMax) g_tables.clear();
+    g_tables[key] = std::move(h);
+  }
   CKR(dalloc(ctx, &ctx->d_vcq, (size_t)nd * NG));
   CKR(dalloc(ctx, &ctx->d_vCG, NG));
   CKR(dalloc(ctx, &ctx->d_kern, (size_t)nd * NG));

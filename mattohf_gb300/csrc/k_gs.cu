@@ -63,14 +63,17 @@ __device__ double2 block_sum2(double2 v, double scale, double2* red, double2* re
 // waits on shared-memory rather than L2 latency.
 constexpr int kCgsChunk = kGsThreads / 32;  // dot products reduced per round
 constexpr int kCgsMaxCols = 64;
-template <bool STAGE>
+template <bool STAGE, int PASSES>
 __global__ void __launch_bounds__(kGsThreads) k_mgs(double2* u, int kstride, int nb, int NG,
-                                                    double weight, int passes, int* flag) {
+                                                    double weight, int* flag) {
+  constexpr int passes = PASSES;
+  // the classical pass's buffers exist only in its instantiation (32 KB)
+  constexpr int kPartRows = PASSES == 2 ? kCgsChunk : 1, kPartCols = PASSES == 2 ? kGsThreads : 1;
   extern __shared__ double2 cols[];  // STAGE: nb * NG
   __shared__ double2 red[kGsThreads];
   __shared__ double2 res;
-  __shared__ double2 part[kCgsChunk][kGsThreads];  // passes == 2: per-thread partial dots
-  __shared__ double2 zc[kCgsMaxCols];              // passes == 2: projections of the pass
+  __shared__ double2 part[kPartRows][kPartCols];               // passes == 2: per-thread partial dots
+  __shared__ double2 zc[PASSES == 2 ? kCgsMaxCols : 1];        // passes == 2: projections of the pass
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double2* gbase = u + (size_t)blockIdx.x * kstride;
   double2* base = STAGE ? cols : gbase;
@@ -181,16 +184,20 @@ static cudaError_t launch_mgs(double2* u, int kstride, int nb, int NG, double we
                               int* flag, cudaStream_t s) {
   if ((passes != 1 && passes != 2) || (passes == 2 && nb > kCgsMaxCols)) return cudaErrorInvalidValue;
   const size_t bytes = sizeof(double2) * (size_t)nb * NG;
-  if (bytes <= kMgsStageMax) {
-    // the static buffers take about 37 KB, so even small stagings pass the
-    // 48 KB default: always raise the dynamic limit to what this launch needs
-    const cudaError_t e = cudaFuncSetAttribute(k_mgs<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e != cudaSuccess) return e;
-    k_mgs<true><<<nk, kGsThreads, bytes, s>>>(u, kstride, nb, NG, weight, passes, flag);
-  } else {
-    k_mgs<false><<<nk, kGsThreads, 0, s>>>(u, kstride, nb, NG, weight, passes, flag);
-  }
-  return cudaGetLastError();
+  const bool stage = bytes <= kMgsStageMax;
+  // the static buffers take about 37 KB with two passes, so even small
+  // stagings can pass the 48 KB default: always raise the dynamic limit to
+  // what this launch needs
+  auto go = [&](auto kern) {
+    if (stage) {
+      const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+      if (e != cudaSuccess) return e;
+    }
+    kern<<<nk, kGsThreads, stage ? bytes : 0, s>>>(u, kstride, nb, NG, weight, flag);
+    return cudaGetLastError();
+  };
+  if (passes == 2) return stage ? go(k_mgs<true, 2>) : go(k_mgs<false, 2>);
+  return stage ? go(k_mgs<true, 1>) : go(k_mgs<false, 1>);
 }
 
 // M[k][i][j] = sum_x conj(x_i) y_j * weight for i >= j, one warp per (k, i, j):

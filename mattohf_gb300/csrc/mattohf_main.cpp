@@ -22,6 +22,7 @@
 #include <charconv>
 #include <chrono>
 #include <cmath>
+#include <limits>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -304,10 +305,51 @@ std::string repr(double x) {
 
 std::string rjust(const std::string& s, int w) { return std::string(std::max(0, w - (int)s.size()), ' ') + s; }
 
+// Fortran Fw.d: w asterisks when the value does not fit, Infinity for +-inf.
 std::string fixed(double x, int w, int d) {
-  char b[64];
-  std::snprintf(b, sizeof b, "%*.*f", w, d, x);
-  return b;
+  if (std::isinf(x)) return rjust(x > 0 ? "Infinity" : "-Infinity", w);
+  char b[400];
+  std::snprintf(b, sizeof b, "%.*f", d, x);
+  std::string s = b;
+  if ((int)s.size() > w && (s.rfind("0.", 0) == 0 || s.rfind("-0.", 0) == 0)) s.erase(s.find('0'), 1);
+  return (int)s.size() <= w ? rjust(s, w) : std::string(w, '*');
+}
+
+const double kHuge = std::numeric_limits<double>::max();  // Fortran huge(1.d0): minval of an empty section
+
+// '(i5,3e20.12,4x,1e20.12,4x,1000e20.12)' (src/GS_calculation.f90:102, 114): the
+// first group takes kx, the mean residual and epsbk(1); each 4x and the group
+// after it appear only while bands remain.
+std::string band_record(int ik, double kx, double errsum, const std::vector<double>& ek) {
+  std::vector<double> items{kx, errsum};
+  items.insert(items.end(), ek.begin(), ek.end());
+  char b[16];
+  std::snprintf(b, sizeof b, "%5d", ik);
+  std::string s = b + row(std::vector<double>(items.begin(), items.begin() + std::min<size_t>(3, items.size())));
+  if (items.size() > 3) s += "    " + row({items[3]});
+  if (items.size() > 4) s += "    " + row(std::vector<double>(items.begin() + 4, items.end()));
+  return s;
+}
+
+// The last two GSinfo columns (src/GS_calculation.f90:51-52).  With every band
+// occupied, minval over the empty conduction section is huge(1.d0), and the
+// second column reads epsbk(NB+1,ik), i.e. epsbk(1,ik+1) in column-major
+// storage; the k-point ik = NK, whose read lies past the array, is left out.
+std::vector<double> gap_columns(const std::vector<double>& eps, int NK, int NB, int NBocc) {
+  double vmax = -kHuge, cmin = kHuge, opt = kHuge;
+  for (int ik = 0; ik < NK; ++ik)
+    for (int ib = 0; ib < NB; ++ib) {
+      const double x = eps[(size_t)ik * NB + ib];
+      if (ib < NBocc) vmax = std::max(vmax, x);
+      else cmin = std::min(cmin, x);
+    }
+  if (NBocc < NB) {
+    for (int ik = 0; ik < NK; ++ik)
+      opt = std::min(opt, eps[(size_t)ik * NB + NBocc] - eps[(size_t)ik * NB + NBocc - 1]);
+    return {cmin - vmax, opt};
+  }
+  for (int ik = 0; ik + 1 < NK; ++ik) opt = std::min(opt, eps[(size_t)(ik + 1) * NB] - eps[(size_t)ik * NB + NB - 1]);
+  return {kHuge - vmax, opt};
 }
 
 // ---------------------------------------------------------------------------
@@ -424,9 +466,10 @@ int run(const Config& c, const std::string& dir) {
   const auto t_gs0 = std::chrono::steady_clock::now();
   std::vector<double> dprev = density_of_state(h, c);
   double Et_prev = e0.Etot;
+  // the format literal continues on the next source line with its leading blanks (GS:23-24)
   std::vector<std::string> lines{
       "#iter, Etotscf(iter), Etoscf(iter)-Etotscf(iter-1), ,sum(abs(dnsscf(:,iter+1)-dnsscf(:,iter)))/dble(NG) "
-      "sum(epserrorbk)/dble(NB*NK),maxval(epserrorbk),Fundamental gap, Optical Gap"};
+      "         sum(epserrorbk)/dble(NB*NK),maxval(epserrorbk),Fundamental gap, Optical Gap"};
   std::vector<double> eps((size_t)NK * NB), err((size_t)NK * NB);
   bool have_eps = false;
   for (int it = 1; it <= c.Nscf; ++it) {
@@ -448,19 +491,7 @@ int run(const Config& c, const std::string& dir) {
       emax = std::max(emax, x);
     }
     std::vector<double> vals{Et, Et - Et_prev, dd, esum / (NB * NK), emax};
-    if (NB > NBocc) {
-      double cmin = INFINITY, vmax = -INFINITY, opt = INFINITY;
-      for (int ik = 0; ik < NK; ++ik) {
-        for (int ib = 0; ib < NB; ++ib) {
-          const double x = eps[(size_t)ik * NB + ib];
-          if (ib >= NBocc) cmin = std::min(cmin, x);
-          else vmax = std::max(vmax, x);
-        }
-        opt = std::min(opt, eps[(size_t)ik * NB + NBocc] - eps[(size_t)ik * NB + NBocc - 1]);
-      }
-      vals.push_back(cmin - vmax);
-      vals.push_back(opt);
-    }
+    for (double g : gap_columns(eps, NK, NB, NBocc)) vals.push_back(g);
     char ib[16];
     std::snprintf(ib, sizeof ib, "%5d", it);
     lines.push_back(std::string("  ") + ib + row(vals));
@@ -473,11 +504,27 @@ int run(const Config& c, const std::string& dir) {
   const char* labs[4] = {"Ekin ", "Eion ", "EH   ", "Exc  "};
   for (int i = 0; i < 4; ++i) lines.push_back(std::string("#") + labs[i] + " at SCF:" + fixed(ec.Ecomps[i], 12, 8));
   if (have_eps) {
+    // GS:75-90; the conduction-bottom line prints maxval of the conduction
+    // bands, as the reference does
     const double mn = *std::min_element(eps.begin(), eps.end()), mx = *std::max_element(eps.begin(), eps.end());
-    lines.push_back("#Min. value of the spectra: minval(epsbk)    =" + fixed(mn, 12, 8) + " =" +
-                    fixed(mn * kHartree, 12, 8) + " [eV]");
-    lines.push_back("#Max. value of the spectra: maxval(epsbk)    =" + fixed(mx, 12, 8) + " =" +
-                    fixed(mx * kHartree, 12, 8) + " [eV]");
+    double vtop = -kHuge, cmax = -kHuge;
+    for (int ik = 0; ik < NK; ++ik)
+      for (int ib = 0; ib < NB; ++ib) {
+        const double x = eps[(size_t)ik * NB + ib];
+        if (ib < NBocc) vtop = std::max(vtop, x);
+        else cmax = std::max(cmax, x);
+      }
+    const std::vector<double> gp = gap_columns(eps, NK, NB, NBocc);
+    const std::pair<const char*, double> rows[] = {
+        {"#Min. value of the spectra: minval(epsbk)    =", mn},
+        {"#Max. value of the spectra: maxval(epsbk)    =", mx},
+        {"#Valence top: maxval(epsbk(:NBocc,:))        =", vtop},
+        {"#Conduction bottom: minval(epsbk(NBocc+1:,:))=", cmax},
+        {"#Fundamental gap: ", gp[0]},
+        {"#Min. gap among same k-point: ", gp[1]}};
+    for (const auto& r : rows)
+      lines.push_back(std::string(r.first) + fixed(r.second, 12, 8) + " =" + fixed(r.second * kHartree, 12, 8) +
+                      " [eV]");
   }
   {
     std::ofstream f = open_out(dir, sysn + "_GSinfo.out");
@@ -513,11 +560,9 @@ int run(const Config& c, const std::string& dir) {
       double es = 0.0;
       for (int ib = 0; ib < NB; ++ib) es += err[(size_t)ik * NB + ib];
       std::vector<double> ek(eps.begin() + (size_t)ik * NB, eps.begin() + (size_t)(ik + 1) * NB);
-      char kb[16];
-      std::snprintf(kb, sizeof kb, "%5d", ik + 1);
-      const std::string body = row({kx[ik], es / NB}) + "    " + row({0.0}) + "    " + row(ek);
-      fd << "# " << kb << body << "\n";
-      fb << kb << body << "\n";
+      const std::string rec = band_record(ik + 1, kx[ik], es / NB, ek);
+      fd << "# " << rec << "\n";
+      fb << rec << "\n";
     }
     for (int i = 0; i < n; ++i) fd << row({e[i], dos[i] / norm, docc[i] / norm}, 20, 12, 3) << "\n";
   }

@@ -61,6 +61,48 @@ def _row(values, w=20, d=12, e=2) -> str:
     return "".join(fortran_e(v, w, d, e) for v in values)
 
 
+def fortran_f(x: float, w: int = 12, d: int = 8) -> str:
+    """Fortran Fw.d: asterisks when the value does not fit, Infinity for +-inf."""
+    x = float(x)
+    if math.isinf(x):
+        s = "Infinity" if x > 0 else "-Infinity"
+        return s.rjust(w)
+    s = f"{x:.{d}f}"
+    if len(s) > w and s.startswith(("0.", "-0.")):
+        s = s.replace("0.", ".", 1)
+    return s.rjust(w) if len(s) <= w else "*" * w
+
+
+HUGE = float(np.finfo(np.float64).max)   # Fortran huge(1.d0): minval of an empty section
+GSINFO_HEADER = ("#iter, Etotscf(iter), Etoscf(iter)-Etotscf(iter-1), ,sum(abs(dnsscf(:,iter+1)-dnsscf(:,iter)))"
+                 "/dble(NG)          sum(epserrorbk)/dble(NB*NK),maxval(epserrorbk),Fundamental gap, Optical Gap")
+
+
+def band_record(ik: int, kx: float, errsum: float, eps_k) -> str:
+    """'(i5,3e20.12,4x,1e20.12,4x,1000e20.12)' (src/GS_calculation.f90:102, 114): the
+    first group takes kx, the mean residual and epsbk(1); each 4x and the
+    group after it appear only while bands remain."""
+    items = [kx, errsum] + [float(v) for v in eps_k]
+    s = f"{ik:5d}" + _row(items[:3])
+    if len(items) > 3:
+        s += "    " + _row(items[3:4])
+    if len(items) > 4:
+        s += "    " + _row(items[4:])
+    return s
+
+
+def gap_columns(eps: np.ndarray, NBocc: int):
+    """The last two GSinfo columns (src/GS_calculation.f90:51-52).  With every band
+    occupied, minval over the empty conduction section is huge(1.d0), and the
+    second column reads epsbk(NB+1,ik), i.e. epsbk(1,ik+1) in column-major
+    storage; the k-point ik = NK, whose read lies past the array, is left out."""
+    NK, NB = eps.shape
+    vmax = eps[:, :NBocc].max()
+    if NBocc < NB:
+        return [eps[:, NBocc:].min() - vmax, float(np.min(eps[:, NBocc] - eps[:, NBocc - 1]))]
+    return [HUGE - vmax, HUGE if NK == 1 else float(np.min(eps[1:, 0] - eps[:-1, NB - 1]))]
+
+
 def read_name(stream) -> str:
     line = stream.readline()
     s = line.strip()
@@ -142,8 +184,7 @@ def run(cfg: RunConfig, out_dir: str = ".", rt_chunk: int = 1000, log=print) -> 
     t_gs = time.perf_counter()
     dprev = ctx.ubk_dns(ctx.get_orbitals())
     Et_prev = e0["Etot"]
-    lines: List[str] = ["#iter, Etotscf(iter), Etoscf(iter)-Etotscf(iter-1), ,sum(abs(dnsscf(:,iter+1)-dnsscf(:,iter)))/dble(NG) "
-                        "sum(epserrorbk)/dble(NB*NK),maxval(epserrorbk),Fundamental gap, Optical Gap"]
+    lines: List[str] = [GSINFO_HEADER]
     eps = err = None
     for it in range(1, cfg.Nscf + 1):
         r = ctx.GS_calculation(1, cfg.NCG)
@@ -152,18 +193,25 @@ def run(cfg: RunConfig, out_dir: str = ".", rt_chunk: int = 1000, log=print) -> 
         dnew = 0.5 * ctx.ubk_dns(ctx.get_orbitals()) + 0.5 * dprev
         dd = np.sum(np.abs(dnew - dprev)) / NG
         dprev = dnew
-        gaps = []
-        if NB > NBocc:
-            gaps = [eps[:, NBocc:].min() - eps[:, :NBocc].max(), np.min(eps[:, NBocc] - eps[:, NBocc - 1])]
-        lines.append("  " + f"{it:5d}" + _row([Et, Et - Et_prev, dd, err.sum() / (NB * NK), err.max()] + gaps))
+        lines.append("  " + f"{it:5d}" + _row([Et, Et - Et_prev, dd, err.sum() / (NB * NK), err.max()] +
+                                              gap_columns(eps, NBocc)))
         log(f"iter, Etotscf(iter), JeGS ={it:4d}{Et:14.8f}{Et - Et_prev:12.4E}  {r['Je'][0]:12.4E}")
         Et_prev = Et
     ec = ctx.observables(0.0)
     for lab, key in (("Ekin ", "Ekin"), ("Eion ", "Eion"), ("EH   ", "EH"), ("Exc  ", "Exc")):
-        lines.append(f"#{lab} at SCF:{ec[key]:12.8f}")
+        lines.append(f"#{lab} at SCF:" + fortran_f(ec[key]))
     if eps is not None:
-        lines.append(f"#Min. value of the spectra: minval(epsbk)    ={eps.min():12.8f} ={eps.min() * HARTREE:12.8f} [eV]")
-        lines.append(f"#Max. value of the spectra: maxval(epsbk)    ={eps.max():12.8f} ={eps.max() * HARTREE:12.8f} [eV]")
+        # src/GS_calculation.f90:75-90; the conduction-bottom line prints maxval
+        # of the conduction bands, as the reference does
+        fund, opt = gap_columns(eps, NBocc)
+        for lab, v in (("#Min. value of the spectra: minval(epsbk)    =", eps.min()),
+                       ("#Max. value of the spectra: maxval(epsbk)    =", eps.max()),
+                       ("#Valence top: maxval(epsbk(:NBocc,:))        =", eps[:, :NBocc].max()),
+                       ("#Conduction bottom: minval(epsbk(NBocc+1:,:))=",
+                        eps[:, NBocc:].max() if NBocc < NB else -HUGE),
+                       ("#Fundamental gap: ", fund),
+                       ("#Min. gap among same k-point: ", opt)):
+            lines.append(lab + fortran_f(v) + " =" + fortran_f(v * HARTREE) + " [eV]")
     with open(p(f"{sysn}_GSinfo.out"), "w") as fh:
         fh.write("\n".join(lines) + "\n")
     if eps is not None:
@@ -171,15 +219,13 @@ def run(cfg: RunConfig, out_dir: str = ".", rt_chunk: int = 1000, log=print) -> 
         with open(p(f"{sysn}_DoS.out"), "w") as fh:
             fh.write(" # ik,kx(ik),  sum(epserrorbk(:,ik))/dble(NB),  epsbk(:,ik)\n")
             for ik in range(NK):
-                fh.write(f"# {ik + 1:5d}" + _row([g["kx"][ik], err[ik].sum() / NB]) + "    " +
-                         _row([0.0]) + "    " + _row(eps[ik]) + "\n")
+                fh.write("# " + band_record(ik + 1, g["kx"][ik], err[ik].sum() / NB, eps[ik]) + "\n")
             for i in range(e.size):
                 fh.write(_row([e[i], dos[i], docc[i]], e=3) + "\n")
         with open(p(f"{sysn}_band.out"), "w") as fh:
             fh.write(" # ik,kx(ik),  sum(epserrorbk(:,ik))/dble(NB),  epsbk(:,ik)\n")
             for ik in range(NK):
-                fh.write(f"{ik + 1:5d}" + _row([g["kx"][ik], err[ik].sum() / NB]) + "    " + _row([0.0]) +
-                         "    " + _row(eps[ik]) + "\n")
+                fh.write(band_record(ik + 1, g["kx"][ik], err[ik].sum() / NB, eps[ik]) + "\n")
     t_gs = time.perf_counter() - t_gs
     # ---- real time (RT:2-69)
     t_rt = time.perf_counter()

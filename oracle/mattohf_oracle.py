@@ -797,6 +797,8 @@ class GSResult:
     epserrorbk: np.ndarray    # final (NK, NB)
     dnsdiff: np.ndarray       # sum|dnsscf(iter+1)-dnsscf(iter)|/NG per iteration
     Ecomps: np.ndarray
+    eps_hist: Optional[list] = None     # epsbk of every iteration (the GSinfo columns)
+    err_hist: Optional[list] = None     # epserrorbk of every iteration
 
 
 def gs_calculation(sysm: System, ubk: np.ndarray, nscf: Optional[int] = None, ortho: str = "svd") -> GSResult:
@@ -810,6 +812,7 @@ def gs_calculation(sysm: System, ubk: np.ndarray, nscf: Optional[int] = None, or
     Je = np.empty(nscf)
     dd = np.empty(nscf)
     eps = err = None
+    eh, rh = [], []
     for it in range(nscf):
         u = gram_schmidt(sysm, u)
         u = ks_ubk2_svd(sysm, u, 0.0, ortho)
@@ -819,10 +822,12 @@ def gs_calculation(sysm: System, ubk: np.ndarray, nscf: Optional[int] = None, or
         Je[it] = ubk_Je(sysm, u, 0.0)
         eps = ubk_epsbk(sysm, u)
         err = ubk_epserrorbk(sysm, u)
+        eh.append(eps)
+        rh.append(err)
         dnew = dnsmix * ubk_dns(sysm, u) + (1.0 - dnsmix) * dprev   # GS:44 (never fed back)
         dd[it] = np.sum(np.abs(dnew - dprev)) / float(sysm.NG)
         dprev = dnew
-    return GSResult(u, Et, Je, eps, err, dd, ubk_Ecomps(sysm, u, 0.0))
+    return GSResult(u, Et, Je, eps, err, dd, ubk_Ecomps(sysm, u, 0.0), eh, rh)
 
 
 # ---------------------------------------------------------------------------

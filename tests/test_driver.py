@@ -207,3 +207,74 @@ def test_cpp_driver_matches_python_driver(tmp_path, built_lib, field):
         # same kernels in the same order; host-side sums (SCF density change,
         # DoS broadening) may round differently from numpy's pairwise sums
         assert np.allclose(a, b, rtol=1e-11, atol=1e-300), f
+
+
+# ---------------------------------------------------------------------------
+# Drivers against the oracle's restatement of the program (oracle/mattohf_program.py)
+# ---------------------------------------------------------------------------
+_NUM = r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[eE][-+]?\d+|[-+]\d{3})?"
+
+
+def _parse(tok: str) -> float:
+    import re
+    m = re.fullmatch(r"([-+]?(?:\d+\.\d*|\.\d+|\d+))([-+]\d{3})", tok)   # Ew.d with a 3-digit exponent
+    return float(m.group(1) + "e" + m.group(2)) if m else float(tok)
+
+
+def _compare_with_oracle(got_path, ref_path, fixed_width: bool, rtol=1e-8):
+    """Same records: for fixed-width (E/F/I edit descriptor) files the text with
+    every number masked must be identical (headers, asterisks, Infinity, field
+    layout); every number must agree to rtol, with an absolute floor of 1e-11
+    of the file's largest finite magnitude."""
+    import re
+    got = open(got_path).read().splitlines()
+    ref = open(ref_path).read().splitlines()
+    assert len(got) == len(ref), (got_path, len(got), len(ref))
+    gnums, rnums = [], []
+    for a, b in zip(got, ref):
+        if fixed_width:
+            assert re.sub(_NUM, "#", a) == re.sub(_NUM, "#", b), (got_path, a, b)
+        else:
+            assert len(re.findall(_NUM, a)) == len(re.findall(_NUM, b)), (got_path, a, b)
+        gnums += [_parse(t) for t in re.findall(_NUM, a)]
+        rnums += [_parse(t) for t in re.findall(_NUM, b)]
+    g, r = np.array(gnums), np.array(rnums)
+    finite = np.abs(r[np.abs(r) < 1e300])
+    floor = 1e-11 * (finite.max() if finite.size else 1.0)
+    bad = np.abs(g - r) > rtol * np.abs(r) + floor
+    assert not bad.any(), (got_path, g[bad][:5], r[bad][:5])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("field,nb", [("LP", 2), ("LR", 2), ("LP", 3)])
+def test_drivers_match_oracle_program(tmp_path, built_lib, field, nb):
+    """Every reference output file of the C++ drop-in driver and of the Python
+    driver against the file the oracle's restatement of the program writes
+    from its own results and the reference's edit descriptors
+    (src/GS_calculation.f90:21-118, 239-265; src/RT_calculation.f90:21-65,
+    246-351; src/Prep_periodic_ion_potential.f90:23-27;
+    src/Initialization.f90:148-155).  With nb = 2 every band is occupied (the
+    gap columns of GSinfo take their empty-section values), with nb = 3 one
+    band is empty."""
+    from mattohf_gb300 import read_input
+    from mattohf_gb300.driver import run
+    from oracle import mattohf_oracle as O
+    from oracle.mattohf_program import run_program
+    text = INPUT.replace("'LP'", f"'{field}'").replace("NB\n  2\n", f"NB\n  {nb}\n")
+    (tmp_path / "input.dat").write_text(text)
+    dirs = {k: tmp_path / k for k in ("oracle", "cpp", "py")}
+    for d in dirs.values():
+        d.mkdir()
+    ocfg = O.read_input(str(tmp_path / "input.dat"))
+    assert ocfg.NB == nb
+    run_program(ocfg, str(dirs["oracle"]))
+    r = _run_cpp("'input.dat'", dirs["cpp"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    run(read_input(str(tmp_path / "input.dat")), out_dir=str(dirs["py"]), log=lambda *a: None)
+    ref_files = sorted(os.listdir(dirs["oracle"]))
+    assert ("tiny_sigmaeps.out" in ref_files) == (field == "LR")
+    for drv in ("cpp", "py"):
+        files = set(os.listdir(dirs[drv]))
+        assert files == set(ref_files) | {"tiny_dipole.out"}, (drv, files)   # the dipole is an extension
+        for f in ref_files:
+            _compare_with_oracle(dirs[drv] / f, dirs["oracle"] / f, fixed_width=f not in ("potential.out", "vk.out"))
