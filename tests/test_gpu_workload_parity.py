@@ -220,10 +220,11 @@ def test_c1_ground_state_against_oracle():
     dense FP64 DFT instead of its FFT (a different but equally FP64
     computation, as FFTW's in the reference is) moves Etot by 5e-4 and epsbk
     by 2e-3 within these three iterations.  The bound is therefore
-    self-calibrated: the oracle is rerun with unit-roundoff noise (2.2e-16 of
-    each h-apply's largest entry, the size of a transform's round-off) added
-    to every h-apply, and the GPU may differ from the oracle by at most 10x
-    what that noise moves."""
+    self-calibrated: the oracle is rerun three times with unit-roundoff noise
+    (2.2e-16 of each h-apply's largest entry, the size of a transform's
+    round-off; three seeds, since one draw's effect on Etot varies twentyfold)
+    added to every h-apply, and the GPU may differ from the oracle by at most
+    10x the largest move."""
     from oracle import mattohf_oracle as O
     cfg, ctx = context("c1")
     vCG, vCq = ctx.coulomb()
@@ -233,23 +234,27 @@ def test_c1_ground_state_against_oracle():
     u0 = O.gram_schmidt(S, O.init_wf(S))
     ref = O.gs_calculation(S, u0, nscf=3)
     exact = O.ubkwbk_hwbk
-    rng = np.random.default_rng(5)
+    sens = None
+    for seed in (5, 6, 7):
+        rng = np.random.default_rng(seed)
 
-    def rounded(S_, u, w, A):
-        h = exact(S_, u, w, A)
-        noise = rng.standard_normal(h.shape) + 1j * rng.standard_normal(h.shape)
-        return h + 2.2e-16 * np.max(np.abs(h)) * noise / np.sqrt(2.0)
+        def rounded(S_, u, w, A):
+            h = exact(S_, u, w, A)
+            noise = rng.standard_normal(h.shape) + 1j * rng.standard_normal(h.shape)
+            return h + 2.2e-16 * np.max(np.abs(h)) * noise / np.sqrt(2.0)
 
-    O.ubkwbk_hwbk = rounded
-    try:
-        pert = O.gs_calculation(S, u0, nscf=3)
-    finally:
-        O.ubkwbk_hwbk = exact
-    sens = _gs_deviation(S, {"Etot": pert.Etot, "epsbk": pert.epsbk, "epserrorbk": pert.epserrorbk,
-                             "Je": pert.Je}, O.ubk_dns(S, pert.ubk), ref)
+        O.ubkwbk_hwbk = rounded
+        try:
+            pert = O.gs_calculation(S, u0, nscf=3)
+        finally:
+            O.ubkwbk_hwbk = exact
+        d = _gs_deviation(S, {"Etot": pert.Etot, "epsbk": pert.epsbk, "epserrorbk": pert.epserrorbk,
+                              "Je": pert.Je}, O.ubk_dns(S, pert.ubk), ref)
+        sens = d if sens is None else {k: max(sens[k], d[k]) for k in d}
     errs = _gs_deviation(S, gs, ctx.ubk_dns(u_gpu), ref)
     print("c1 ground state (3 iterations) vs oracle: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
-    print("  oracle moved by unit-roundoff noise:    " + ", ".join(f"{k} {v:.2e}" for k, v in sens.items()))
+    print("  oracle moved by unit-roundoff noise (largest of 3 draws): " +
+          ", ".join(f"{k} {v:.2e}" for k, v in sens.items()))
     for k, v in errs.items():
         assert v <= 10.0 * sens[k] + 1e-12, (k, v, sens[k])
 
