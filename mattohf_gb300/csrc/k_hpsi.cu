@@ -675,7 +675,11 @@ static cudaError_t fock_sym_impl(const FockSymArgs& a, cudaStream_t s) {
 
 template <int N>
 static cudaError_t configure_impl() {
-  return cudaFuncSetAttribute(k_fock_sym<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sym_smem<N>());
+  // the single-run and the batched symmetric exchange (above 48 KB at NG = 512)
+  const cudaError_t e =
+      cudaFuncSetAttribute(k_fock_sym<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sym_smem<N>());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_fock_sym_batch<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sym_smem<N>());
 }
 
 template <int N>

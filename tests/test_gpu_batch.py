@@ -166,3 +166,29 @@ def test_batch_adjoint_matches_single_runs(built_lib, ckpt):
             assert np.max(np.abs(g[r] - gr)) <= 1e-11 * np.max(np.abs(gr))
             assert np.max(np.abs(gv[r] - gvr)) <= 1e-11 * np.max(np.abs(gvr))
         assert b.last_run_ms() > 0
+
+
+def test_batch_at_ng512_matches_single_runs(built_lib):
+    """A batch at the largest grid (its symmetric-exchange CTAs use more than
+    48 KB of dynamic shared memory) against each member run alone."""
+    from mattohf_gb300 import Batch, Context, RunConfig
+    cfgs = [RunConfig(acell=12.0, NG=512, NK=k, NB=b, NBocc=b, Zeff=[1.0], alpha=[1.0], Rion=[1 / 6, 0.5, 5 / 6],
+                      Kion=[1, 1, 1]) for k, b in [(2, 2), (3, 1)]]
+    nt = 3
+    A = 0.01 * np.arange(1, nt + 1)[None, :] * np.array([[1.0], [-0.5]])
+    Aave = np.concatenate([0.5 * A[:, :1], 0.5 * (A[:, 1:] + A[:, :-1])], axis=1)
+    dt = 2.5e-4
+    with Batch(cfgs) as b:
+        u0 = []
+        for r in range(len(cfgs)):
+            b[r].Init_wf()
+            b[r].Gram_Schmidt()
+            u0.append(b[r].get_orbitals())
+        E, J, N = b.rk4_run(A, Aave, dt)
+        ub = [b[r].get_orbitals() for r in range(len(cfgs))]
+    for r, cfg in enumerate(cfgs):
+        with Context(cfg) as c:
+            c.set_orbitals(u0[r])
+            e, j, n = c.rk4_run(A[r], Aave[r], dt)
+            assert np.max(np.abs(E[r] - e)) <= 1e-12 * np.max(np.abs(e))
+            assert np.max(np.abs(ub[r] - c.get_orbitals())) <= 1e-12 * np.max(np.abs(ub[r]))
