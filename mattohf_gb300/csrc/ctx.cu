@@ -579,20 +579,20 @@ bool use_small(const mattohf_ctx* ctx) {
   return ctx->NK * ctx->NB <= 64 && M * M * ctx->NG <= ((size_t)1 << 17);
 }
 
-// CTAs per column.  A warp's teams run their pairs in the same instructions,
-// and a lone warp's FP64 work is bound by its SM sub-partition: so each CTA
-// takes as many pairs as the teams of two warps (on two sub-partitions) hold,
-// at least 4, unless that needs more CTAs than there are multiprocessors.
+// CTAs per column.  A lone warp's FP64 work is bound by its SM sub-partition,
+// so a column's pairs are spread until each sub-partition holds one warp's
+// teams: the first CTA takes half the share of the others (its sub-partitions
+// 2 and 3 carry the kinetic and Hartree transforms), so with Q = the teams of
+// one warp per sub-partition (4 warps) each of the other CTAs takes up to Q
+// pairs, 2M/(2P-1) <= Q, unless that needs more CTAs than there are
+// multiprocessors.
 int small_ctas_per_column(const mattohf_ctx* ctx) {
   const int ncols = ctx->NK * ctx->NB, M = ctx->NK * ctx->NBocc;
   const int pair_teams = small_pair_teams(ctx->NG);   // 6 warps' teams
   if (ctx->opt_small_ctas > 0)  // set (or tuned): at most M and a cluster's CTAs
     return std::max(1, std::min(std::min(ctx->opt_small_ctas, std::max(1, M)), kSmallMaxCtas));
-  // two warps' teams, and at least 4 pairs (with one team per warp, as in the
-  // 32-lane transforms, fewer pairs per CTA only add CTAs: measured with
-  // mattohf_autotune at NG=64, NK=8, Nocc=2)
-  const int two_warps = std::max(4, pair_teams / 3);
-  int P = (M + two_warps - 1) / two_warps;
+  const int Q = std::max(1, 4 * (pair_teams / 6));
+  int P = (2 * M + Q) / (2 * Q) + ((2 * M + Q) % (2 * Q) != 0);   // ceil((2M/Q + 1) / 2)
   if (ncols * P > ctx->nsm) P = std::max(1, ctx->nsm / ncols);
   P = std::max(P, (M + pair_teams - 1) / pair_teams);  // one round of all pair teams at most
   return std::max(1, std::min(std::min(P, M), kSmallMaxCtas));  // one cluster per column
@@ -1516,8 +1516,8 @@ int mattohf_rk4_run(mattohf_ctx* ctx, int nt, double dt, const double* A, const 
 //     k_sym_reduce, or the double-float kernels) for S = 1, 2, 4, ... up to the
 //     teams of a CTA;
 //   * fused-stage CTAs per column P, for the grids the fused stages support:
-//     graph-replayed mattohf_rk4_run steps for P from one round of all pair
-//     teams up to the multiprocessors (powers of two and the default);
+//     graph-replayed mattohf_rk4_run steps for every P from one round of all
+//     pair teams up to twice the multiprocessors over the columns (at most 8);
 //   * fused stages vs the tiled step: the faster of the best of each.
 // out: [0] S, [1] P (0 when the fused stages do not apply), [2] 1 when the
 // fused stages won; us: [0] exchange apply at S, [1] step of the tiled path,
@@ -1601,8 +1601,8 @@ extern "C" int mattohf_autotune(mattohf_ctx* ctx, int steps, int* out, double* u
     ctx->opt_small = 1;
     ctx->opt_small_ctas = 0;
     std::vector<int> cand{small_ctas_per_column(ctx)};
-    for (int P = 1; P <= hi; P <<= 1)
-      if (P >= lo && P != cand[0]) cand.push_back(P);
+    for (int P = lo; P <= hi; ++P)
+      if (P != cand[0]) cand.push_back(P);
     double best = 1e300;
     for (int P : cand) {
       ctx->opt_small_ctas = P;

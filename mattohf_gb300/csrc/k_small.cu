@@ -12,9 +12,12 @@
 //     potential (F:147-162).  One warp alone would queue about 4 us of FP64
 //     work on its SM sub-partition for the sum, and that backlog held up the
 //     whole CTA after the phase;
-//   * the other warps apply the exchange of column c against the CTA's chunk of
-//     the occupied orbitals (F:237-261, ordered pairs, no symmetry), one pair
-//     per team, and the CTA keeps its partial sum in shared memory;
+//   * the CTAs apply the exchange of column c against their chunks of the
+//     occupied orbitals (F:237-261, ordered pairs, no symmetry), one pair per
+//     team, and each keeps its partial sum in shared memory.  The first CTA,
+//     whose warps 6 and 7 hold SM sub-partitions 2 and 3 with the kinetic and
+//     Hartree transforms, takes half the others' share on warps 0 and 1; the
+//     others use all eight warps;
 //   * in the column's first CTA, warp 6 does the kinetic transform of the
 //     column (F:212-234);
 //   * after a cluster barrier each CTA of the column adds the P partials in
@@ -56,8 +59,9 @@ template <int N>
 struct SmallLayout {
   static constexpr int PW = Team<N, kSmallPlan<N>>::PER_WARP;
   static constexpr int NTEAM = kSmallWarps * PW;
-  // warps 0..5 apply exchange pairs; in the column's first CTA warp 6 does the
-  // kinetic transform and warp 7 the density and Hartree potential
+  // pair teams of a single CTA (warps 0..5; warp 6 does the kinetic
+  // transform and warp 7 the density and Hartree potential), the autotuner's
+  // lower bound on the CTAs per column
   static constexpr int PAIR_TEAMS = (kSmallWarps - 2) * PW;
   // tw[N], bufs[NTEAM][N], F[N] (double2); rho[N], vh[N] (double); K[N] (double2)
   static constexpr size_t bytes = sizeof(double2) * (size_t)N * (3 + NTEAM) + sizeof(double) * 2 * (size_t)N;
@@ -117,7 +121,6 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   using TM = Team<N, kSmallPlan<N>>;
   constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
   constexpr int NTEAM = SmallLayout<N>::NTEAM;
-  constexpr int PAIR_TEAMS = SmallLayout<N>::PAIR_TEAMS;
   namespace cg = cooperative_groups;
   extern __shared__ double2 sm2[];
   double2* tw_s = sm2;                     // N
@@ -137,8 +140,16 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   const int chunk = blockIdx.x % a.P;      // rank in the column's cluster
   const int kr = c / a.nb, ib = c % a.nb;
   const int M = a.nk * a.nbocc;
-  const int ppc = (M + a.P - 1) / a.P;     // pairs per CTA
-  const int p0 = chunk * ppc, p1 = min(M, p0 + ppc);
+  // This CTA's exchange pairs.  In the column's first CTA warps 6 and 7 carry
+  // the kinetic and the Hartree transforms on SM sub-partitions 2 and 3, so
+  // with more than one CTA per column it takes half the share of the others
+  // and runs it on warps 0 and 1 (sub-partitions 0 and 1) only; the other
+  // CTAs run their pairs on all eight warps.  A single CTA keeps warps 0-5.
+  const int wsum = 1 + 2 * (a.P - 1);
+  const int p0 = chunk == 0 ? 0 : (M * (2 * chunk - 1)) / wsum;
+  const int p1 = chunk + 1 == a.P ? M : (M * (2 * chunk + 1)) / wsum;
+  const int workers = chunk == 0 ? (a.P == 1 ? kSmallWarps - 2 : 2) : kSmallWarps;  // pair warps 0 .. workers-1
+  const int worker_teams = workers * PW;
   const bool occupied = ib < a.nbocc;
   const bool obs = a.mode == 0 || a.mode == 4;
   const double2* wcol = a.u + (size_t)c * N;
@@ -170,8 +181,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     dslice[j * N + ig] = s;
   }
   __syncthreads();
-  if (warp == kSmallWarps - 1) {
-    if (chunk == 0) {
+  if (chunk == 0 && warp == kSmallWarps - 1) {
+    {
       // density (slices in order; with 3 or more slices rho_s[ig] is slice
       // 2's entry for ig, read by this lane before it is overwritten) and vH
       for (int ig = lane; ig < N; ig += 32) {
@@ -191,8 +202,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
         for (int e = 0; e < E; ++e) vh_s[TM::pos(tl, e)] = x[e].x / (double)N;
       }
     }
-  } else if (warp == kSmallWarps - 2) {
-    if (chunk == 0) {
+  } else if (chunk == 0 && warp == kSmallWarps - 2) {
+    {
       // kinetic term T_A w of column c at the stage field (F:212-234) and, for
       // stage 0 and the closing pass, Ekin and Je of the input column at the
       // previous step's field by Parseval on the same forward transform
@@ -235,13 +246,13 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
         }
       }
     }
-  } else if (a.hf && (a.mode != 4 || occupied)) {
+  } else if (warp < workers && a.hf && (a.mode != 4 || occupied)) {
     // this CTA's exchange pairs of column c, one pair per team per round
     double2 acc[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) acc[e] = make_double2(0.0, 0.0);
     // warp-uniform trip count: every team of a warp runs the same rounds
-    for (int base = p0 + warp * PW; base < p1; base += PAIR_TEAMS) {
+    for (int base = p0 + warp * PW; base < p1; base += worker_teams) {
       const int p = base + lane / T;
       const bool valid = p < p1;
       const int pp = valid ? p : p0;
@@ -259,7 +270,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     __syncwarp();
 #pragma unroll
     for (int e = 0; e < E; ++e) buf[TM::pos(tl, e)] = acc[e];
-  } else {
+  } else if (warp < workers) {
 #pragma unroll
     for (int e = 0; e < E; ++e) buf[TM::pos(tl, e)] = make_double2(0.0, 0.0);
   }
@@ -267,7 +278,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   // this CTA's partial (pair teams in order), kept in its shared memory
   for (int i = tid; i < N; i += kSmallThreads) {
     double2 f = bufs[i];
-    for (int t2 = 1; t2 < PAIR_TEAMS; ++t2) f = cadd(f, bufs[(size_t)t2 * N + i]);
+    for (int t2 = 1; t2 < worker_teams; ++t2) f = cadd(f, bufs[(size_t)t2 * N + i]);
     F_s[i] = f;
   }
   // the column's P CTAs form a cluster: after this barrier every CTA reads the
