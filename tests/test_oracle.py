@@ -348,3 +348,30 @@ def test_dipole_helper_matches_oracle_quadrature():
     P = dipole_from_current(g["rt_Jtot"], J0, cfg.dt)
     assert np.array_equal(P, O.dipole_from_current(None, g["rt_Jtot"], J0, cfg.dt))
     assert P.shape == g["rt_Jtot"].shape and np.all(np.isfinite(P))
+
+
+def test_oracle_edit_descriptors():
+    """The oracle's Ew.d / Ew.dEe / Fw.d restatement (oracle/mattohf_program.py)
+    on values whose Fortran output the standard fixes, and against the
+    drivers' own formatter on random values (two independent writers)."""
+    from oracle.mattohf_program import ew, fw, band_record
+    from mattohf_gb300.driver import fortran_e, fortran_f
+    assert ew(1.0) == "  0.100000000000E+01"
+    assert ew(-0.00123456789012345) == " -0.123456789012E-02"
+    assert ew(0.0) == "  0.000000000000E+00"
+    assert ew(1.5e123) == "  0.150000000000+124"          # a 3-digit exponent drops the E
+    assert ew(1.7976931348623157e308) == "  0.179769313486+309"
+    assert ew(2.5, e=3) == " 0.250000000000E+001"
+    assert fw(-1.2345) == " -1.23450000"
+    assert fw(1.7976931348623157e308) == "*" * 12
+    assert fw(float("inf")) == "    Infinity" and fw(float("-inf")) == "   -Infinity"
+    # '(i5,3e20.12,4x,1e20.12,4x,1000e20.12)': kx, the residual and band 1 share the first group
+    rec = band_record(3, 0.5, 0.25, [1.0, 2.0, 3.0])
+    assert rec == "    3" + ew(0.5) + ew(0.25) + ew(1.0) + "    " + ew(2.0) + "    " + ew(3.0)
+    assert band_record(1, 0.5, 0.25, [1.0]) == "    1" + ew(0.5) + ew(0.25) + ew(1.0)
+    rng = np.random.default_rng(4)
+    for x in np.concatenate([rng.standard_normal(200) * 10.0 ** rng.integers(-30, 30, 200), [0.0, -0.0]]):
+        assert ew(x) == fortran_e(x), x
+        assert ew(x, e=3) == fortran_e(x, e=3), x
+        if abs(x) < 1e3:
+            assert fw(x) == fortran_f(x), x
