@@ -499,8 +499,8 @@ def measure_adjoint(nt: int, fd_samples: int) -> dict:
     and the interval the library fits to free memory.  The gradient is checked
     by central differences of the plain forward on `fd_samples` random samples:
     at h = 1e-6 (the workload's step) with each sample's round-off bound, the
-    spread between the quotients at h and 1.25 h, and at h = 1e-4, where
-    round-off is 100x smaller and truncation is O(h^2).
+    larger spread between the quotient at h and those at 1.25 h and 0.8 h, and
+    at h = 1e-4, where round-off is 100x smaller and truncation is O(h^2).
     """
     from mattohf_gb300 import Context, RunConfig, define_afield, aave_from_samples
     cfg = RunConfig.from_pulse(0.05, 0.057, 100.0, acell=10.0, NG=128, NK=16, NB=2, NBocc=2, Zeff=[2.0],
@@ -540,12 +540,13 @@ def measure_adjoint(nt: int, fd_samples: int) -> dict:
         for i, n in enumerate(rng.choice(nt, size=fd_samples, replace=False)):
             q = {}
             # h = 1e-4 on the first 8 samples only (it serves as a cross-check)
-            for h in ((1e-4, 1e-6, 1.25e-6) if i < 8 else (1e-6, 1.25e-6)):
+            for h in ((1e-4, 1e-6, 1.25e-6, 0.8e-6) if i < 8 else (1e-6, 1.25e-6, 0.8e-6)):
                 Ap, Am = A.copy(), A.copy()
                 Ap[n] += h
                 Am[n] -= h
                 q[h] = (obj(Ap) - obj(Am)) / (2 * h)
-            rows.append((g[n], q.get(1e-4, np.nan), q[1e-6], abs(q[1e-6] - q[1.25e-6])))
+            rows.append((g[n], q.get(1e-4, np.nan), q[1e-6],
+                         max(abs(q[1e-6] - q[1.25e-6]), abs(q[1e-6] - q[0.8e-6]))))
     rows = np.array(rows)
     gs_, f4, f6, spread = rows.T
     rel6 = np.abs(gs_ - f6) / np.abs(f6)
@@ -564,7 +565,7 @@ def measure_adjoint(nt: int, fd_samples: int) -> dict:
                              "normwise_rel_err": float(np.max(np.abs(gs_ - f6)) / np.max(np.abs(f6))),
                              "within_1e-6_plus_roundoff": int(np.sum(rel6 <= bound6)),
                              "max_roundoff_bound_rel": float((3 * spread / np.abs(f6)).max()),
-                             "note": "round-off bound per sample = 3 x |fd(h) - fd(1.25 h)|"},
+                             "note": "round-off bound per sample = 3 x max(|fd(h) - fd(1.25 h)|, |fd(h) - fd(0.8 h)|)"},
                    "h1e-4": {"samples": int(m4.sum()), "max_rel_err_per_sample": float(rel4.max())}},
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"a=10, NK=16, Nocc=2, NG=128, {nt} steps, pulse+N(0,1e-3), "

@@ -65,18 +65,19 @@ def fd_check(obj, A, g, samples, h_small=1e-6, h_large=1e-4):
     sample, so that is the bound.  h_small = 1e-6: the quotient carries the
     round-off of two full propagations (about 1e-15 absolute in L, so ~1e-9 in
     the quotient), which exceeds 1e-6 of the smaller samples; its size is
-    estimated per sample from the spread between the quotients at h and
-    1.25 h (independent round-off, negligible truncation), and the bound is
-    1e-6 |fd| + 3 x that spread.  Returns the per-sample table."""
+    estimated per sample from the larger spread between the quotient at h
+    and those at 1.25 h and 0.8 h (independent round-off, negligible
+    truncation), and the bound is 1e-6 |fd| + 3 x that spread.  Returns the
+    per-sample table."""
     rows = []
     for n in samples:
         q = {}
-        for h in (h_large, h_small, 1.25 * h_small):
+        for h in (h_large, h_small, 1.25 * h_small, 0.8 * h_small):
             Ap, Am = A.copy(), A.copy()
             Ap[n] += h
             Am[n] -= h
             q[h] = (obj(Ap) - obj(Am)) / (2 * h)
-        spread = abs(q[h_small] - q[1.25 * h_small])
+        spread = max(abs(q[h_small] - q[1.25 * h_small]), abs(q[h_small] - q[0.8 * h_small]))
         rows.append((int(n), g[n], q[h_large], q[h_small], spread))
     print("  n        g              fd(1e-4) rel     fd(1e-6) rel     round-off bound (rel)")
     for n, gn, fl, fs, sp in rows:
