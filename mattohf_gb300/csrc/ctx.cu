@@ -114,6 +114,7 @@ struct mattohf_ctx {
   size_t small_part_cap = 0;
   int small_P = 1;                // CTAs per column of the fused stages
   int small_P_adj = 1;            // CTAs per column of the fused reverse stages
+  double* d_small_obs = nullptr;  // [2][NG] density and vH of a fused step's input (observables)
   int nsm = 0;                    // multiprocessors of the device
   int* d_int = nullptr;  // [0] = step counter, [1] = non-finite flag, [2] = solver flag
   // RT series
@@ -628,6 +629,10 @@ int ensure_small_buffers(mattohf_ctx* ctx) {
     CKR(dalloc(ctx, &ctx->d_small_part, need));
     ctx->small_part_cap = need;
   }
+  if (!ctx->d_small_obs) {
+    if (ctx->capturing) return fail(ctx, MATTOHF_ERR_STATE, "fused-stage scratch growth during capture");
+    CKR(dalloc(ctx, &ctx->d_small_obs, 2 * (size_t)ctx->NG));
+  }
   return MATTOHF_OK;
 }
 
@@ -660,6 +665,7 @@ SmallStageArgs small_base(mattohf_ctx* ctx, double dt) {
   a.it = ctx->d_int;
   a.nonfinite = ctx->d_int + 1;
   a.ticket = ctx->d_ticket;
+  a.obs_dens = ctx->d_small_obs;
   return a;
 }
 
@@ -1015,7 +1021,7 @@ int mattohf_destroy(mattohf_ctx* ctx) {
                   ctx->d_sJ, ctx->d_sN, ctx->d_work, ctx->d_hwork, ctx->d_M, ctx->d_V, ctx->d_evals,
                   ctx->d_eps, ctx->d_err, ctx->d_sym, ctx->d_symF, ctx->d_dpart,
                   ctx->d_udf, ctx->d_kern_df, ctx->d_tw_df, ctx->d_hpre, ctx->d_ticket,
-                  ctx->d_small_part};
+                  ctx->d_small_part, ctx->d_small_obs};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);

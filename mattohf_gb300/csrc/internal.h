@@ -220,6 +220,7 @@ struct SmallStageArgs {
   int* nonfinite;
   unsigned* ticket;         // [1 + ncols]: global, then per-column completion counters
   double* out_obs;          // mode 4: [7] Etot, Ekin, Eion, EH, Ex, Je, Nele
+  double* obs_dens;         // [2][NG]: density and vH of stage 0's input (column 0), read by stage 1
 };
 // CTAs per column of the fused stages: one thread-block cluster per column
 // (the portable cluster size)

@@ -25,11 +25,15 @@
 //     memory), takes vH and T_A w from the first CTA the same way, and forms
 //     h w and the stage's RK4 update element by element, into a buffer that is
 //     never the stage input;
-//   * stage 0 (or the closing pass, mode 4) also gives the observables of its
-//     input, i.e. of the previous step (F:74-119, F:165-183, F:289-318): Ekin
-//     and Je from warp 6's forward transform at the previous step's field,
-//     <u|F u> from the CTAs' shares, and the density scalars; the last column
-//     to finish (global ticket) writes Etot, Je, Nele.
+//   * stage 0 (or the closing pass, mode 4) also gathers the observables of
+//     its input, i.e. of the previous step (F:74-119, F:165-183, F:289-318):
+//     Ekin and Je per column by Parseval on a forward transform of the column
+//     at the previous step's field (warp 3 of the first CTA, idle when a
+//     column has several CTAs, else warp 6 with its kinetic transform),
+//     <u|F u> from the CTAs' shares, and column 0's copy of the density and
+//     vH.  Stage 1 then forms Etot, Je, Nele on an idle warp of column 0's
+//     first CTA, so no stage-0 CTA waits for a global ticket; the closing pass
+//     still has the last column to finish (global ticket) write them.
 //     In stage 3 the last column to finish advances the step counter (the
 //     columns' first CTAs read it for the stage field until then).
 // A ticket is an atomic counter taken after a fence; the CTA that draws the
@@ -201,6 +205,15 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
 #pragma unroll
         for (int e = 0; e < E; ++e) vh_s[TM::pos(tl, e)] = x[e].x / (double)N;
       }
+      if (a.mode == 0 && c == 0) {
+        // the density and vH of this stage input (the previous step's state)
+        // for its observables, which stage 1 completes off this critical path
+        __syncwarp();
+        for (int ig = lane; ig < N; ig += 32) {
+          a.obs_dens[ig] = rho_s[ig];
+          a.obs_dens[N + ig] = vh_s[ig];
+        }
+      }
     }
   } else if (chunk == 0 && warp == kSmallWarps - 2) {
     {
@@ -211,7 +224,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
 #pragma unroll
       for (int e = 0; e < E; ++e) x[e] = wcol[TM::pos(tl, e)];
       fft_team<N, -1, kSmallPlan<N>>(x, buf, tw_s, tl);
-      if (obs) {
+      if (obs && !(a.mode == 0 && a.P > 1)) {
         const int itn = *a.it;
         const double Ao = (itn >= 1 && a.Aobs) ? a.Aobs[itn - 1] : 0.0;
         const double kAx = a.kx[kr] + Ao, kA2 = kAx * kAx;
@@ -246,6 +259,30 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
         }
       }
     }
+  } else if (chunk == 0 && a.P > 1 && warp == 3 && a.mode == 0) {
+    // Ekin and Je of the input column at the previous step's field (Parseval
+    // on its forward transform), beside warp 6's kinetic transforms
+    double2 x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) x[e] = wcol[TM::pos(tl, e)];
+    fft_team<N, -1, kSmallPlan<N>>(x, buf, tw_s, tl);
+    const int itn = *a.it;
+    const double Ao = (itn >= 1 && a.Aobs) ? a.Aobs[itn - 1] : 0.0;
+    const double kAx = a.kx[kr] + Ao, kA2 = kAx * kAx;
+    double ek = 0.0, je = 0.0;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const double G = a.Gx[TM::pos(tl, e)];
+      const double m2 = x[e].x * x[e].x + x[e].y * x[e].y;
+      ek += 0.5 * (G * G + 2.0 * G * kAx + kA2) * m2;
+      je += (G + a.kx[kr] + Ao) * m2;
+    }
+    ek = team_sum<T>(ek) / (double)N;
+    je = team_sum<T>(je) / (double)N;
+    if (lane == 0) {
+      a.colbuf[(size_t)c * 4] = ek;
+      a.colbuf[(size_t)c * 4 + 1] = je;
+    }
   } else if (warp < workers && a.hf && (a.mode != 4 || occupied)) {
     // this CTA's exchange pairs of column c, one pair per team per round
     double2 acc[E];
@@ -274,6 +311,11 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
 #pragma unroll
     for (int e = 0; e < E; ++e) buf[TM::pos(tl, e)] = make_double2(0.0, 0.0);
   }
+  // stage 1: the observables of the previous step's state, from the column
+  // buffer and the density stage 0 left (stage 0 completed before this grid
+  // passed griddepcontrol.wait), on an idle warp of column 0's first CTA
+  if (a.mode == 1 && c == 0 && chunk == 0 && warp == (a.P > 1 ? 2 : kSmallWarps - 1))
+    small_finalize(a, a.obs_dens, a.obs_dens + N, N);
   __syncthreads();
   // this CTA's partial (pair teams in order), kept in its shared memory
   for (int i = tid; i < N; i += kSmallThreads) {
@@ -291,8 +333,14 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   double exr = 0.0, exi = 0.0;
   bool bad = false;
   if (tid < per && q < N) {
-    double2 f = cluster.map_shared_rank(F_s, 0)[q];
-    for (int r = 1; r < a.P; ++r) f = cadd(f, cluster.map_shared_rank(F_s, r)[q]);
+    double2 pr[kSmallMaxCtas];
+#pragma unroll
+    for (int r = 0; r < kSmallMaxCtas; ++r)
+      if (r < a.P) pr[r] = cluster.map_shared_rank(F_s, r)[q];
+    double2 f = pr[0];
+#pragma unroll
+    for (int r = 1; r < kSmallMaxCtas; ++r)
+      if (r < a.P) f = cadd(f, pr[r]);
     const size_t o = (size_t)c * N + q;
     const double2 wq = wcol[q];
     if (obs) {
@@ -364,7 +412,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   // stages 1 and 2 end here.  Stage 3 advances the step counter, but the
   // first CTA of every column reads it (the stage field A[it]): only the last
   // column to finish, when every column has passed this point, may change it.
-  if ((!obs && a.mode != 3) || chunk != 0) return;
+  if ((a.mode != 3 && a.mode != 4) || chunk != 0) return;
   // the last column to finish finalizes (nothing waits on another column)
   __syncthreads();
   if (tid == 0) {
