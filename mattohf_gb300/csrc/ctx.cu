@@ -116,7 +116,8 @@ struct mattohf_ctx {
   int small_P_adj = 1;            // CTAs per column of the fused reverse stages
   double* d_small_obs = nullptr;  // [2][NG] density and vH of a fused step's input (observables)
   int nsm = 0;                    // multiprocessors of the device
-  int* d_int = nullptr;  // [0] = step counter, [1] = non-finite flag, [2] = solver flag
+  int* d_int = nullptr;  // [0] = step counter, [1] = non-finite flag, [2] = solver flag,
+                         // [3] = the fused stages' shadow of the step counter
   // RT series
   double *d_A = nullptr, *d_Aave = nullptr, *d_sE = nullptr, *d_sJ = nullptr, *d_sN = nullptr;
   int series_cap = 0;
@@ -673,17 +674,26 @@ SmallStageArgs small_base(mattohf_ctx* ctx, double dt) {
 // alternate between d_us and d_hpre so that no launch writes its own input.
 // Stage 0 also writes the observables of the previous step (its input).
 // With `store`, each stage input also goes to the adjoint's stage store.
+// The step counter d_int[0] holds the step index between steps (the host,
+// the checkpoint and store copies read and set it there).  Stage 0 copies it
+// to the shadow d_int[3]; stage 3 reads its field at the shadow's index and
+// writes index + 1 to d_int[0], which none of its CTAs reads.
 int enq_small_step(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt, bool store = false) {
   SmallStageArgs a = small_base(ctx, dt);
   const double2* in[4] = {ctx->d_u, ctx->d_us, ctx->d_hpre, ctx->d_us};
   double2* out[4] = {ctx->d_us, ctx->d_hpre, ctx->d_us, nullptr};
-  const AField fs[4] = {f_m, f_ave, f_ave, f_cur};
+  AField fs[4] = {f_m, f_ave, f_ave, f_cur};
+  int* const shadow = ctx->d_int + 3;
+  fs[3].it = shadow;
   for (int s = 0; s < 4; ++s) {
     if (store) CKR(launch_store_stage(ctx, in[s], s));
     a.u = in[s];
     a.out = out[s];
     a.mode = s;
     a.af = fs[s];
+    a.it = s == 3 ? shadow : ctx->d_int;
+    a.it_out = s == 0 ? shadow : s == 3 ? ctx->d_int : nullptr;
+    a.it_inc = s == 3 ? 1 : 0;
     CK(launch_small_stage(ctx->NG, a, ctx->st));
   }
   return MATTOHF_OK;

@@ -216,7 +216,10 @@ struct SmallStageArgs {
   double* series_E;         // per-step observables, indexed by the step counter
   double* series_J;
   double* series_N;
-  int* it;                  // step counter
+  int* it;                  // step counter read by this stage
+  int* it_out;              // if set, block 0 writes *it + it_inc here (a counter no CTA of
+  int it_inc;               // this stage reads): stage 0 copies the counter to its shadow,
+                            // stage 3 reads the shadow and writes the next step's index
   int* nonfinite;
   unsigned* ticket;         // [1 + ncols]: global, then per-column completion counters
   double* out_obs;          // mode 4: [7] Etot, Ekin, Eion, EH, Ex, Je, Nele

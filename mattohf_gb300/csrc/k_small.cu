@@ -34,8 +34,10 @@
 //     vH.  Stage 1 then forms Etot, Je, Nele on an idle warp of column 0's
 //     first CTA, so no stage-0 CTA waits for a global ticket; the closing pass
 //     still has the last column to finish (global ticket) write them.
-//     In stage 3 the last column to finish advances the step counter (the
-//     columns' first CTAs read it for the stage field until then).
+//     The step counter has a shadow: stage 0 copies the counter to it and
+//     stage 3 reads the shadow (for its field) while block 0 writes the next
+//     step's index to the counter, so no stage waits for a global ticket to
+//     advance it.
 // A ticket is an atomic counter taken after a fence; the CTA that draws the
 // last number does the follow-up work.  No CTA waits on another column.
 #include <cooperative_groups.h>
@@ -166,6 +168,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   // without a programmatic dependency.
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;");
+  if (a.it_out && blockIdx.x == 0 && tid == 0) *a.it_out = *a.it + a.it_inc;
   // density, first part: sum of |u|^2 over slice j of the occupied orbitals at
   // point ig, one (j, ig) per thread.  F_s, rho_s and vh_s (4N contiguous
   // doubles) are free during the first phase and hold the slices.
@@ -409,11 +412,9 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     }
     cluster.sync();  // the other CTAs stay until their shares are read
   }
-  // stages 1 and 2 end here.  Stage 3 advances the step counter, but the
-  // first CTA of every column reads it (the stage field A[it]): only the last
-  // column to finish, when every column has passed this point, may change it.
-  if ((a.mode != 3 && a.mode != 4) || chunk != 0) return;
-  // the last column to finish finalizes (nothing waits on another column)
+  // the RK4 stages end here; in the closing pass the last column to finish
+  // finalizes (nothing waits on another column)
+  if (a.mode != 4 || chunk != 0) return;
   __syncthreads();
   if (tid == 0) {
     __threadfence();
@@ -423,11 +424,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   __syncthreads();
   if (last_s && warp == 0) {
     __threadfence();
-    if (a.mode == 3) {
-      if (lane == 0) *a.it = *a.it + 1;
-    } else {
-      small_finalize(a, rho_s, vh_s, N);
-    }
+    small_finalize(a, rho_s, vh_s, N);
     if (lane == 0) *a.ticket = 0u;
   }
 }
