@@ -582,12 +582,14 @@ bool use_small(const mattohf_ctx* ctx) {
   return ctx->NK * ctx->NB <= 64 && M * M * ctx->NG <= ((size_t)1 << 17);
 }
 
-// CTAs per column.  A lone warp's FP64 work is bound by its SM sub-partition,
-// so a column's pairs are spread until each sub-partition holds one warp's
-// teams: the first CTA takes half the share of the others (its sub-partitions
-// 2 and 3 carry the kinetic and Hartree transforms), so with Q = the teams of
-// one warp per sub-partition (4 warps) each of the other CTAs takes up to Q
-// pairs, 2M/(2P-1) <= Q, unless that needs more CTAs than there are
+// CTAs per column.  A warp issues at most one FP64 instruction per ~64
+// cycles and an SM about one per 19 cycles in all (measured on GB300 with
+// independent FMA chains: 2 warps run at the single-warp rate, 4 at 76 cycles
+// each, 8 at 152), so a pair chain is fastest with about 4 FP64-busy warps per
+// SM.  With more than one CTA per column the first CTA takes no pairs (it
+// carries the density, the kinetic and Hartree transforms), so with Q = the
+// teams of 4 warps each of the other P - 1 CTAs takes up to Q pairs,
+// P = 1 + ceil(M / Q), unless that needs more CTAs than there are
 // multiprocessors.
 int small_ctas_per_column(const mattohf_ctx* ctx) {
   const int ncols = ctx->NK * ctx->NB, M = ctx->NK * ctx->NBocc;
@@ -595,10 +597,12 @@ int small_ctas_per_column(const mattohf_ctx* ctx) {
   if (ctx->opt_small_ctas > 0)  // set (or tuned): at most M and a cluster's CTAs
     return std::max(1, std::min(std::min(ctx->opt_small_ctas, std::max(1, M)), kSmallMaxCtas));
   const int Q = std::max(1, 4 * (pair_teams / 6));
-  int P = (2 * M + Q) / (2 * Q) + ((2 * M + Q) % (2 * Q) != 0);   // ceil((2M/Q + 1) / 2)
+  const int full = std::max(1, 8 * (pair_teams / 6));  // teams of a CTA's eight warps
+  int P = 1 + (M + Q - 1) / Q;
   if (ncols * P > ctx->nsm) P = std::max(1, ctx->nsm / ncols);
-  P = std::max(P, (M + pair_teams - 1) / pair_teams);  // one round of all pair teams at most
-  return std::max(1, std::min(std::min(P, M), kSmallMaxCtas));  // one cluster per column
+  // one round of the pair teams at most
+  if ((P == 1 && M > pair_teams) || (P > 1 && (P - 1) * full < M)) P = 1 + (M + full - 1) / full;
+  return std::max(1, std::min(std::min(P, std::max(1, M)), kSmallMaxCtas));  // one cluster per column
 }
 
 // CTAs per column of the fused reverse stages: one round of the pass teams

@@ -168,10 +168,10 @@ template <int N, int L = 0> struct FftPlan;
 template <> struct FftPlan<16, 0>  { static constexpr int NP = 2; static constexpr int R[8] = {4, 4}; };
 template <> struct FftPlan<32, 0>  { static constexpr int NP = 3; static constexpr int R[8] = {4, 2, 4}; };
 // N = 64 takes three radix-4 passes on 16 lanes rather than two radix-8 passes
-// on 8: 3 % more FP64 instructions in total, but half as many per lane.  Each
-// FP64 warp instruction occupies an SM sub-partition for ~64 cycles, so the
-// small grids, which run few transforms at a time, finish a transform in about
-// half the time.
+// on 8: 3 % more FP64 instructions in total, but half as many per lane.  A
+// warp issues at most one FP64 instruction per ~64 cycles, even with
+// independent operands, so the small grids, which run few transforms at a
+// time, finish a transform in about half the time.
 template <> struct FftPlan<64, 0>  { static constexpr int NP = 3; static constexpr int R[8] = {4, 4, 4}; };
 template <> struct FftPlan<128, 0> { static constexpr int NP = 3; static constexpr int R[8] = {4, 8, 4}; };
 template <> struct FftPlan<256, 0> { static constexpr int NP = 3; static constexpr int R[8] = {8, 4, 8}; };

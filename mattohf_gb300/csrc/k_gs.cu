@@ -15,10 +15,9 @@ constexpr int kGsThreads = 256;
 // Fixed-order CTA sum of a complex value (kGsThreads threads), times `scale`.
 // Two barriers: every thread stores its partial, warp 0 adds the eight warp
 // partials of its lane (a fixed pairwise tree) and then its 32 lanes (a
-// shuffle tree), and lane 0 publishes the scaled result.  On this part one
-// FP64 warp instruction occupies a sub-partition's FP64 pipe for many cycles,
-// so the tree runs in one warp and only once, not redundantly in every
-// thread.  `red` and `res` are safe to reuse on the next call without a
+// shuffle tree), and lane 0 publishes the scaled result.  On this part an SM
+// issues about one FP64 warp instruction per 19 cycles in all, so the tree
+// runs in one warp and only once, not redundantly in every thread.  `red` and `res` are safe to reuse on the next call without a
 // third barrier: warp 0 reads `red` before the second barrier, and every
 // thread reads `res` before it reaches the next call's first barrier.
 __device__ double2 block_sum2(double2 v, double scale, double2* red, double2* res) {
@@ -55,7 +54,8 @@ __device__ double2 block_sum2(double2 v, double scale, double2* red, double2* re
 //     Gram-Schmidt applied twice ("twice is enough": Giraud, Langou and
 //     Rozloznik, 2005).  Each pass projects a column on all earlier columns at
 //     once; the dot products are summed eight at a time, one per warp, so the
-//     reductions use every sub-partition instead of serialising in one warp.
+//     reductions run side by side instead of serialising in one warp (a warp
+//     issues at most one FP64 instruction per ~64 cycles).
 // Thread t owns the grid points t, t + kGsThreads, ... of every column, so
 // between reductions no thread reads what another wrote and only the
 // reductions synchronise.  STAGE: the k-point's nb columns are held in shared

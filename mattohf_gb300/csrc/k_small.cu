@@ -6,18 +6,19 @@
 // 154-173).  Output column c = (k, b) is served by P CTAs (c, chunk) that form
 // one thread-block cluster:
 //   * the column's first CTA computes the density of the stage input
-//     (F:55-71): all its threads first sum |u|^2 over slices of the occupied
+//     (F:55-71): all its warps but the kinetic one (all threads when the
+//     column has one CTA) first sum |u|^2 over slices of the occupied
 //     orbitals (in ik -> ib order within a slice, the uniform occupation
 //     applied once); then its last warp adds the slices and forms the Hartree
-//     potential (F:147-162).  One warp alone would queue about 4 us of FP64
-//     work on its SM sub-partition for the sum, and that backlog held up the
-//     whole CTA after the phase;
+//     potential (F:147-162).  A warp issues at most one FP64 instruction per
+//     ~64 cycles, so one warp alone would take about 4 us for the sum.  The
+//     kinetic warp does not wait for the density;
 //   * the CTAs apply the exchange of column c against their chunks of the
 //     occupied orbitals (F:237-261, ordered pairs, no symmetry), one pair per
-//     team, and each keeps its partial sum in shared memory.  The first CTA,
-//     whose warps 6 and 7 hold SM sub-partitions 2 and 3 with the kinetic and
-//     Hartree transforms, takes half the others' share on warps 0 and 1; the
-//     others use all eight warps;
+//     team, and each keeps its partial sum in shared memory.  With more than
+//     one CTA per column the first CTA, which carries the density, the
+//     kinetic and Hartree transforms and the Parseval sums, takes no pairs;
+//     the others split them evenly on all eight warps;
 //   * in the column's first CTA, warp 6 does the kinetic transform of the
 //     column (F:212-234);
 //   * after a cluster barrier each CTA of the column adds the P partials in
@@ -146,21 +147,20 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   const int chunk = blockIdx.x % a.P;      // rank in the column's cluster
   const int kr = c / a.nb, ib = c % a.nb;
   const int M = a.nk * a.nbocc;
-  // This CTA's exchange pairs.  In the column's first CTA warps 6 and 7 carry
-  // the kinetic and the Hartree transforms on SM sub-partitions 2 and 3, so
-  // with more than one CTA per column it takes half the share of the others
-  // and runs it on warps 0 and 1 (sub-partitions 0 and 1) only; the other
-  // CTAs run their pairs on all eight warps.  A single CTA keeps warps 0-5.
-  const int wsum = 1 + 2 * (a.P - 1);
-  const int p0 = chunk == 0 ? 0 : (M * (2 * chunk - 1)) / wsum;
-  const int p1 = chunk + 1 == a.P ? M : (M * (2 * chunk + 1)) / wsum;
-  const int workers = chunk == 0 ? (a.P == 1 ? kSmallWarps - 2 : 2) : kSmallWarps;  // pair warps 0 .. workers-1
+  // This CTA's exchange pairs.  With more than one CTA per column the first
+  // CTA takes none: its warps carry the density, the kinetic and Hartree
+  // transforms and the Parseval sums, and the other CTAs split the pairs
+  // evenly on all eight warps.  A single CTA runs them on warps 0-5.
+  const int p0 = (a.P == 1 || chunk == 0) ? 0 : (M * (chunk - 1)) / (a.P - 1);
+  const int p1 = a.P == 1 ? M : chunk == 0 ? 0 : (M * chunk) / (a.P - 1);
+  const int workers = a.P == 1 ? kSmallWarps - 2 : chunk == 0 ? 0 : kSmallWarps;  // pair warps 0 .. workers-1
   const int worker_teams = workers * PW;
   const bool occupied = ib < a.nbocc;
   const bool obs = a.mode == 0 || a.mode == 4;
   const double2* wcol = a.u + (size_t)c * N;
 
   for (int i = tid; i < N; i += kSmallThreads) tw_s[i] = a.tw[i];
+  __syncthreads();
   // Launched as a programmatic dependent of the previous stage: everything
   // above reads only constant tables.  Wait for the previous grid to complete
   // (and its writes to be visible) before touching the state or the scratch,
@@ -170,24 +170,38 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   asm volatile("griddepcontrol.launch_dependents;");
   if (a.it_out && blockIdx.x == 0 && tid == 0) *a.it_out = *a.it + a.it_inc;
   // density, first part: sum of |u|^2 over slice j of the occupied orbitals at
-  // point ig, one (j, ig) per thread.  F_s, rho_s and vh_s (4N contiguous
-  // doubles) are free during the first phase and hold the slices.
+  // point ig, one (j, ig) per thread and round.  F_s, rho_s and vh_s (4N
+  // contiguous doubles) are free during the first phase and hold the slices.
+  // Only the Hartree warp waits for them.  A single CTA sums them on all its
+  // threads; with several CTAs per column the first CTA's kinetic warp (6)
+  // starts its transforms at once and the other seven warps sum the slices.
   constexpr int NSUB = (kSmallThreads / N) < 4 ? (kSmallThreads / N) : 4;
   double* dslice = reinterpret_cast<double*>(F_s);  // [NSUB][N]
-  if (chunk == 0 && tid < NSUB * N) {
-    const int ig = tid % N, j = tid / N;
+  auto density_slices = [&](int t0, int nthreads) {
     const int per = (M + NSUB - 1) / NSUB;
-    const int q1 = min(M, (j + 1) * per);
-    double s = 0.0;
+    for (int slot = t0; slot < NSUB * N; slot += nthreads) {
+      const int ig = slot % N, j = slot / N;
+      const int q1 = min(M, (j + 1) * per);
+      double s = 0.0;
 #pragma unroll 4
-    for (int p = j * per; p < q1; ++p) {
-      const int ik = p / a.nbocc, b = p % a.nbocc;
-      const double2 z = a.u[((size_t)ik * a.nb + b) * N + ig];
-      s = fma(z.y, z.y, fma(z.x, z.x, s));
+      for (int p = j * per; p < q1; ++p) {
+        const int ik = p / a.nbocc, b = p % a.nbocc;
+        const double2 z = a.u[((size_t)ik * a.nb + b) * N + ig];
+        s = fma(z.y, z.y, fma(z.x, z.x, s));
+      }
+      dslice[j * N + ig] = s;
     }
-    dslice[j * N + ig] = s;
+  };
+  if (chunk == 0) {
+    if (a.P == 1) {
+      density_slices(tid, kSmallThreads);
+      __syncthreads();
+    } else if (warp != kSmallWarps - 2) {
+      const int dw = warp < kSmallWarps - 2 ? warp : warp - 1;
+      density_slices(dw * 32 + lane, kSmallThreads - 32);
+      asm volatile("bar.sync 1, %0;" ::"n"(kSmallThreads - 32) : "memory");
+    }
   }
-  __syncthreads();
   if (chunk == 0 && warp == kSmallWarps - 1) {
     {
       // density (slices in order; with 3 or more slices rho_s[ig] is slice
@@ -310,20 +324,36 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     __syncwarp();
 #pragma unroll
     for (int e = 0; e < E; ++e) buf[TM::pos(tl, e)] = acc[e];
-  } else if (warp < workers) {
-#pragma unroll
-    for (int e = 0; e < E; ++e) buf[TM::pos(tl, e)] = make_double2(0.0, 0.0);
   }
   // stage 1: the observables of the previous step's state, from the column
   // buffer and the density stage 0 left (stage 0 completed before this grid
   // passed griddepcontrol.wait), on an idle warp of column 0's first CTA
   if (a.mode == 1 && c == 0 && chunk == 0 && warp == (a.P > 1 ? 2 : kSmallWarps - 1))
     small_finalize(a, a.obs_dens, a.obs_dens + N, N);
+  // this element's inputs of the epilogue that no other CTA writes
+  const int per = (N + a.P - 1) / a.P;
+  const int q = chunk * per + tid;
+  const bool mine = tid < per && q < N;
+  const size_t o = (size_t)c * N + q;
+  double2 wq = make_double2(0.0, 0.0), u0 = wq, kp[3] = {wq, wq, wq};
+  double vi = 0.0;
+  if (mine) {
+    wq = wcol[q];
+    if (a.mode != 4) {
+      vi = a.vion[q];
+      u0 = a.u0[o];
+      if (a.mode == 3)
+        for (int s3 = 0; s3 < 3; ++s3) kp[s3] = a.kbuf[s3][o];
+    }
+  }
   __syncthreads();
-  // this CTA's partial (pair teams in order), kept in its shared memory
+  // this CTA's partial (pair teams in order; a team past the CTA's pair count
+  // holds none), kept in its shared memory
+  const int act = (a.hf && (a.mode != 4 || occupied)) ? min(worker_teams, p1 - p0) : 0;
   for (int i = tid; i < N; i += kSmallThreads) {
-    double2 f = bufs[i];
-    for (int t2 = 1; t2 < worker_teams; ++t2) f = cadd(f, bufs[(size_t)t2 * N + i]);
+    double2 f = make_double2(0.0, 0.0);
+    if (act > 0) f = bufs[i];
+    for (int t2 = 1; t2 < act; ++t2) f = cadd(f, bufs[(size_t)t2 * N + i]);
     F_s[i] = f;
   }
   // the column's P CTAs form a cluster: after this barrier every CTA reads the
@@ -331,11 +361,9 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   // memory, and does h w and the RK4 update for its own share of the grid
   cg::cluster_group cluster = cg::this_cluster();
   cluster.sync();
-  const int per = (N + a.P - 1) / a.P;
-  const int q = chunk * per + tid;
   double exr = 0.0, exi = 0.0;
   bool bad = false;
-  if (tid < per && q < N) {
+  if (mine) {
     double2 pr[kSmallMaxCtas];
 #pragma unroll
     for (int r = 0; r < kSmallMaxCtas; ++r)
@@ -344,19 +372,16 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
 #pragma unroll
     for (int r = 1; r < kSmallMaxCtas; ++r)
       if (r < a.P) f = cadd(f, pr[r]);
-    const size_t o = (size_t)c * N + q;
-    const double2 wq = wcol[q];
     if (obs) {
       exr = wq.x * f.x + wq.y * f.y;
       exi = wq.x * f.y - wq.y * f.x;
     }
     if (a.mode != 4) {
-      const double v = cluster.map_shared_rank(vh_s, 0)[q] + a.vion[q];
+      const double v = cluster.map_shared_rank(vh_s, 0)[q] + vi;
       const double2 kin = cluster.map_shared_rank(K_s, 0)[q];
       double2 h = make_double2(kin.x + v * wq.x, kin.y + v * wq.y);
       h = cadd(h, f);
       const double2 k = make_double2(h.y, -h.x);  // -i h
-      const double2 u0 = a.u0[o];
       double2 nx;
       if (a.mode < 3) {
         const double cdt = (a.mode == 2) ? a.dt : 0.5 * a.dt;
@@ -364,7 +389,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
         a.kbuf[a.mode][o] = k;
         a.out[o] = nx;
       } else {
-        const double2 k0 = a.kbuf[0][o], k1 = a.kbuf[1][o], k2 = a.kbuf[2][o];
+        const double2 k0 = kp[0], k1 = kp[1], k2 = kp[2];
         double sx = k0.x + 2.0 * k1.x, sy = k0.y + 2.0 * k1.y;
         sx = sx + 2.0 * k2.x;
         sy = sy + 2.0 * k2.y;
