@@ -211,7 +211,9 @@ def run(cfg: RunConfig, out_dir: str = ".", rt_chunk: int = 1000, log=print) -> 
                         eps[:, NBocc:].max() if NBocc < NB else -HUGE),
                        ("#Fundamental gap: ", fund),
                        ("#Min. gap among same k-point: ", opt)):
-            lines.append(lab + fortran_f(v) + " =" + fortran_f(v * HARTREE) + " [eV]")
+            # +-huge(1.d0) in eV overflows to +-Infinity, as the reference's
+            # own product does (Python floats overflow without a warning)
+            lines.append(lab + fortran_f(v) + " =" + fortran_f(float(v) * HARTREE) + " [eV]")
     with open(p(f"{sysn}_GSinfo.out"), "w") as fh:
         fh.write("\n".join(lines) + "\n")
     if eps is not None:
