@@ -330,31 +330,53 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   // passed griddepcontrol.wait), on an idle warp of column 0's first CTA
   if (a.mode == 1 && c == 0 && chunk == 0 && warp == (a.P > 1 ? 2 : kSmallWarps - 1))
     small_finalize(a, a.obs_dens, a.obs_dens + N, N);
-  // this element's inputs of the epilogue that no other CTA writes
+  // The epilogue runs one real component per lane: lane slot idx = 2 e + cc
+  // takes component cc of h = T_A w + v w + F at this CTA's element e and
+  // writes the other component, dd = 1 - cc, of k = -i h and of the stage
+  // output (k.x = h.y, k.y = -h.x).  A warp issues at most one FP64
+  // instruction per ~64 cycles, so halving each lane's chain halves the
+  // epilogue's time.  These are its inputs that no other CTA writes.
+  constexpr int EPI = (2 * N + kSmallThreads - 1) / kSmallThreads;  // lane slots per thread
   const int per = (N + a.P - 1) / a.P;
-  const int q = chunk * per + tid;
-  const bool mine = tid < per && q < N;
-  const size_t o = (size_t)c * N + q;
-  double2 wq = make_double2(0.0, 0.0), u0 = wq, kp[3] = {wq, wq, wq};
-  double vi = 0.0;
-  if (mine) {
-    wq = wcol[q];
-    if (a.mode != 4) {
-      vi = a.vion[q];
-      u0 = a.u0[o];
-      if (a.mode == 3)
-        for (int s3 = 0; s3 < 3; ++s3) kp[s3] = a.kbuf[s3][o];
+  const double cdt = a.mode == 2 ? a.dt : 0.5 * a.dt;
+  double wc[EPI], wd[EPI], vi[EPI], ud[EPI], ks[EPI];
+#pragma unroll
+  for (int r = 0; r < EPI; ++r) {
+    wc[r] = wd[r] = vi[r] = ud[r] = ks[r] = 0.0;
+    const int idx = tid + r * kSmallThreads, e = idx >> 1, cc = idx & 1, dd = 1 - cc;
+    const int q = chunk * per + e;
+    if (e < per && q < N) {
+      const double* w2 = reinterpret_cast<const double*>(wcol + q);
+      wc[r] = w2[cc];
+      wd[r] = cc ? w2[dd] : -w2[dd];  // sg w_dd, sg = +1 for cc = 1, -1 for cc = 0
+      if (a.mode != 4) {
+        const size_t od = 2 * ((size_t)c * N + q) + dd;
+        vi[r] = a.vion[q];
+        ud[r] = reinterpret_cast<const double*>(a.u0)[od];
+        if (a.mode == 3) {
+          // k0 + 2 k1 + 2 k2, formed before the barrier (the order of
+          // ubk + (k1 + 2 k2 + 2 k3 + k4) * dt / 6, RT:165-170, is kept)
+          const double k0 = reinterpret_cast<const double*>(a.kbuf[0])[od];
+          const double k1 = reinterpret_cast<const double*>(a.kbuf[1])[od];
+          const double k2 = reinterpret_cast<const double*>(a.kbuf[2])[od];
+          ks[r] = fma(2.0, k2, fma(2.0, k1, k0));
+        }
+      }
     }
   }
   __syncthreads();
   // this CTA's partial (pair teams in order; a team past the CTA's pair count
-  // holds none), kept in its shared memory
+  // holds none), kept in its shared memory, one real component per thread
   const int act = (a.hf && (a.mode != 4 || occupied)) ? min(worker_teams, p1 - p0) : 0;
-  for (int i = tid; i < N; i += kSmallThreads) {
-    double2 f = make_double2(0.0, 0.0);
-    if (act > 0) f = bufs[i];
-    for (int t2 = 1; t2 < act; ++t2) f = cadd(f, bufs[(size_t)t2 * N + i]);
-    F_s[i] = f;
+  {
+    const double* bd = reinterpret_cast<const double*>(bufs);
+    double* Fd = reinterpret_cast<double*>(F_s);
+    for (int i = tid; i < 2 * N; i += kSmallThreads) {
+      double f = 0.0;
+      if (act > 0) f = bd[i];
+      for (int t2 = 1; t2 < act; ++t2) f += bd[(size_t)t2 * 2 * N + i];
+      Fd[i] = f;
+    }
   }
   // the column's P CTAs form a cluster: after this barrier every CTA reads the
   // P partials and the first CTA's vH and T_A w through distributed shared
@@ -363,44 +385,41 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   cluster.sync();
   double exr = 0.0, exi = 0.0;
   bool bad = false;
-  if (mine) {
-    double2 pr[kSmallMaxCtas];
 #pragma unroll
-    for (int r = 0; r < kSmallMaxCtas; ++r)
-      if (r < a.P) pr[r] = cluster.map_shared_rank(F_s, r)[q];
-    double2 f = pr[0];
+  for (int r = 0; r < EPI; ++r) {
+    const int idx = tid + r * kSmallThreads, e = idx >> 1, cc = idx & 1, dd = 1 - cc;
+    const int q = chunk * per + e;
+    if (!(e < per && q < N)) continue;
+    const double scdt = cc ? cdt : -cdt;  // k_dd = sg h_cc with sg = +1 (cc = 1) or -1 (cc = 0)
+    double pr[kSmallMaxCtas];
 #pragma unroll
-    for (int r = 1; r < kSmallMaxCtas; ++r)
-      if (r < a.P) f = cadd(f, pr[r]);
+    for (int rr = 0; rr < kSmallMaxCtas; ++rr)
+      if (rr < a.P) pr[rr] = reinterpret_cast<const double*>(cluster.map_shared_rank(F_s, rr))[2 * q + cc];
+    double f = pr[0];
+#pragma unroll
+    for (int rr = 1; rr < kSmallMaxCtas; ++rr)
+      if (rr < a.P) f += pr[rr];
     if (obs) {
-      exr = wq.x * f.x + wq.y * f.y;
-      exi = wq.x * f.y - wq.y * f.x;
+      // <w|F> = sum over components: Re gets w_cc F_cc, Im gets sg w_dd F_cc
+      exr = fma(wc[r], f, exr);
+      exi = fma(wd[r], f, exi);
     }
     if (a.mode != 4) {
-      const double v = cluster.map_shared_rank(vh_s, 0)[q] + vi;
-      const double2 kin = cluster.map_shared_rank(K_s, 0)[q];
-      double2 h = make_double2(kin.x + v * wq.x, kin.y + v * wq.y);
-      h = cadd(h, f);
-      const double2 k = make_double2(h.y, -h.x);  // -i h
-      double2 nx;
+      const double v = cluster.map_shared_rank(vh_s, 0)[q] + vi[r];
+      const double kin = reinterpret_cast<const double*>(cluster.map_shared_rank(K_s, 0))[2 * q + cc];
+      const double h = fma(v, wc[r], kin) + f;
+      const size_t od = 2 * ((size_t)c * N + q) + dd;
+      double nx;
       if (a.mode < 3) {
-        const double cdt = (a.mode == 2) ? a.dt : 0.5 * a.dt;
-        nx = make_double2(u0.x + cdt * k.x, u0.y + cdt * k.y);
-        a.kbuf[a.mode][o] = k;
-        a.out[o] = nx;
+        nx = fma(scdt, h, ud[r]);
+        reinterpret_cast<double*>(a.kbuf[a.mode])[od] = cc ? h : -h;
+        reinterpret_cast<double*>(a.out)[od] = nx;
       } else {
-        const double2 k0 = kp[0], k1 = kp[1], k2 = kp[2];
-        double sx = k0.x + 2.0 * k1.x, sy = k0.y + 2.0 * k1.y;
-        sx = sx + 2.0 * k2.x;
-        sy = sy + 2.0 * k2.y;
-        sx = sx + k.x;
-        sy = sy + k.y;
-        sx = sx * a.dt / 6.0;
-        sy = sy * a.dt / 6.0;
-        nx = make_double2(u0.x + sx, u0.y + sy);
-        a.u0[o] = nx;  // this element only, read just above by this thread
+        const double kd = cc ? h : -h;
+        nx = ud[r] + (ks[r] + kd) * a.dt / 6.0;
+        reinterpret_cast<double*>(a.u0)[od] = nx;  // this component only, read above by this thread
       }
-      bad = !(isfinite(nx.x) && isfinite(nx.y));
+      bad = bad || !isfinite(nx);
     }
   }
   if (bad && a.nonfinite) *a.nonfinite = 1;
