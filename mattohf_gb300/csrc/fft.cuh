@@ -329,6 +329,50 @@ __device__ __forceinline__ void fft_team(double2 (&x)[Team<N, L>::E], double2* b
   fft_team_in<N, DIR, L>(InPlain{x}, x, buf, tw, tl);
 }
 
+// Radix-2 decimation-in-time transform of N = 32 W points held one per lane
+// by W consecutive warps (lane index L = 32 * (warp - first warp) + lane, W
+// = 1 or 2): the input is X[bitrev(L)], the output Y[L] in natural order.
+// Every lane forms its own output of each butterfly, A + (+-w) B, in 4 FMA
+// (2 in the first stage), against 6 per two outputs in the team transforms
+// above: a warp issues at most one FP64 instruction per ~64 cycles, so this
+// shortens the chain of a transform that runs alone by a third.  Partners
+// within a warp come by shuffle; with W = 2 the last stage goes through
+// `xbuf` (N double2) and named barrier `bar` over the N threads.
+template <int N, int DIR>
+__device__ __forceinline__ double2 fft_lane(double2 x, int L, const double2* __restrict__ tw, double2* xbuf,
+                                            int bar) {
+  static_assert(N == 32 || N == 64, "one lane per point on one or two warps");
+#pragma unroll
+  for (int half = 1; half < N; half <<= 1) {
+    double2 xp;
+    if (half < 32) {
+      xp.x = __shfl_xor_sync(0xffffffffu, x.x, half);
+      xp.y = __shfl_xor_sync(0xffffffffu, x.y, half);
+    } else {
+      xbuf[L] = x;
+      asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(N) : "memory");
+      xp = xbuf[L ^ half];
+      asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(N) : "memory");
+    }
+    const bool top = (L & half) == 0;
+    const double2 A = top ? x : xp, B = top ? xp : x;
+    if (half == 1) {
+      const double sg = top ? 1.0 : -1.0;
+      x = make_double2(fma(sg, B.x, A.x), fma(sg, B.y, A.y));
+    } else {
+      // w = W_{2 half}^j (conjugated for the inverse), negated for the bottom
+      // output; the sign flips are bit operations, not FP64 instructions
+      double2 w = tw[(L & (half - 1)) * (N / (2 * half))];
+      const unsigned long long sx = top ? 0ull : 0x8000000000000000ull;
+      const unsigned long long sy = sx ^ (DIR > 0 ? 0x8000000000000000ull : 0ull);
+      w.x = __longlong_as_double(__double_as_longlong(w.x) ^ sx);
+      w.y = __longlong_as_double(__double_as_longlong(w.y) ^ sy);
+      x = make_double2(fma(w.x, B.x, fma(-w.y, B.y, A.x)), fma(w.x, B.y, fma(w.y, B.x, A.y)));
+    }
+  }
+  return x;
+}
+
 // Team-wide sum of one double; team lanes are contiguous within a warp.
 template <int T>
 __device__ __forceinline__ double team_sum(double v) {

@@ -192,17 +192,72 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       dslice[j * N + ig] = s;
     }
   };
+  // At NG = 64 with several CTAs per column the first CTA's Hartree (warps 0
+  // and 1) and kinetic (warps 6 and 7) chains each run on two warps, one
+  // point per lane (fft_lane); warps 0-5 sum the density slices.
+  const bool two_warp = N == 64 && a.P > 1 && a.mode != 4;
   if (chunk == 0) {
     if (a.P == 1) {
       density_slices(tid, kSmallThreads);
       __syncthreads();
+    } else if (two_warp) {
+      if (warp < kSmallWarps - 2) {
+        density_slices(tid, kSmallThreads - 64);
+        asm volatile("bar.sync 1, %0;" ::"n"(kSmallThreads - 64) : "memory");
+      }
     } else if (warp != kSmallWarps - 2) {
       const int dw = warp < kSmallWarps - 2 ? warp : warp - 1;
       density_slices(dw * 32 + lane, kSmallThreads - 32);
       asm volatile("bar.sync 1, %0;" ::"n"(kSmallThreads - 32) : "memory");
     }
   }
-  if (chunk == 0 && warp == kSmallWarps - 1) {
+  if constexpr (N == 64) {
+    if (two_warp && chunk == 0 && warp >= kSmallWarps - 2) {
+      // kinetic term T_A w of column c at the stage field (F:212-234), on
+      // warps 6 and 7, one point per lane
+      const int L = (warp - (kSmallWarps - 2)) * 32 + lane;
+      const int rb = (int)(__brev((unsigned)L) >> 26);
+      double2* kb = bufs + (size_t)((kSmallWarps - 2) * PW) * N;
+      double2 x = fft_lane<N, -1>(wcol[rb], L, tw_s, kb, 3);
+      const double A = afield_value(a.af);
+      const double kAx = a.kx[kr] + A, kA2 = kAx * kAx;
+      const double G = a.Gx[L];
+      const double m = 0.5 * (G * G + 2.0 * G * kAx + kA2);
+      kb[L] = make_double2(m * x.x / (double)N, m * x.y / (double)N);
+      asm volatile("bar.sync 3, %0;" ::"n"(N) : "memory");
+      x = kb[rb];
+      asm volatile("bar.sync 3, %0;" ::"n"(N) : "memory");
+      K_s[L] = fft_lane<N, +1>(x, L, tw_s, kb, 3);
+    } else if (two_warp && chunk == 0 && warp < 2) {
+      // density (slices in order; lane L sums point bitrev(L), so rho_s's
+      // entry, slice 2's, is read by this lane before it is overwritten) and
+      // vH (F:147-162) on warps 0 and 1, one point per lane
+      const int L = warp * 32 + lane;
+      const int rb = (int)(__brev((unsigned)L) >> 26);
+      double s = dslice[rb];
+#pragma unroll
+      for (int j = 1; j < NSUB; ++j) s += dslice[j * N + rb];
+      const double rho = a.occ * s;
+      rho_s[rb] = rho;
+      double2* hb = bufs;
+      double2 x = fft_lane<N, -1>(make_double2(rho, 0.0), L, tw_s, hb, 2);
+      const double g = a.vCG[L];
+      hb[L] = make_double2(g * x.x, g * x.y);
+      asm volatile("bar.sync 2, %0;" ::"n"(N) : "memory");
+      x = hb[rb];
+      asm volatile("bar.sync 2, %0;" ::"n"(N) : "memory");
+      x = fft_lane<N, +1>(x, L, tw_s, hb, 2);
+      const double vh = x.x / (double)N;
+      vh_s[L] = vh;  // slice 3's entry L, read by lane bitrev(L) before the barriers above
+      if (a.mode == 0 && c == 0) {
+        a.obs_dens[rb] = rho;
+        a.obs_dens[N + L] = vh;
+      }
+    }
+  }
+  if (two_warp && chunk == 0 && (warp < 2 || warp >= kSmallWarps - 2)) {
+    // done above
+  } else if (chunk == 0 && warp == kSmallWarps - 1) {
     {
       // density (slices in order; with 3 or more slices rho_s[ig] is slice
       // 2's entry for ig, read by this lane before it is overwritten) and vH
