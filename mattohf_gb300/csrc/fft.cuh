@@ -221,6 +221,19 @@ struct InScaled {
   }
 };
 
+// X_e = f_e * x_e with the factors already in registers, f_e for register
+// slot e (loaded before a transform that precedes this one, so that their
+// latency overlaps it)
+struct InScaledRegs {
+  const double2* x;
+  const double* f;
+  __device__ __forceinline__ void pair(int i, int j, double2& s, double2& d) const {
+    const double2 t = make_double2(f[i] * x[i].x, f[i] * x[i].y);
+    s = make_double2(fma(f[j], x[j].x, t.x), fma(f[j], x[j].y, t.y));
+    d = make_double2(fma(-f[j], x[j].x, t.x), fma(-f[j], x[j].y, t.y));
+  }
+};
+
 template <int N, int L>
 struct InConjProduct {
   const double2* a;

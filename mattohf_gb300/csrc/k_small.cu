@@ -176,10 +176,12 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   // threads; with several CTAs per column the first CTA's kinetic warp (6)
   // starts its transforms at once and the other seven warps sum the slices.
   constexpr int NSUB = (kSmallThreads / N) < 4 ? (kSmallThreads / N) : 4;
+  // with the two-warp chains at NG = 64, six warps hold one slot each
+  constexpr int kTwoWarpSlices = (kSmallThreads - 64) / 64;
   double* dslice = reinterpret_cast<double*>(F_s);  // [NSUB][N]
-  auto density_slices = [&](int t0, int nthreads) {
-    const int per = (M + NSUB - 1) / NSUB;
-    for (int slot = t0; slot < NSUB * N; slot += nthreads) {
+  auto density_slices = [&](int t0, int nthreads, int nsub) {
+    const int per = (M + nsub - 1) / nsub;
+    for (int slot = t0; slot < nsub * N; slot += nthreads) {
       const int ig = slot % N, j = slot / N;
       const int q1 = min(M, (j + 1) * per);
       double s = 0.0;
@@ -198,16 +200,16 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   const bool two_warp = N == 64 && a.P > 1 && a.mode != 4;
   if (chunk == 0) {
     if (a.P == 1) {
-      density_slices(tid, kSmallThreads);
+      density_slices(tid, kSmallThreads, NSUB);
       __syncthreads();
     } else if (two_warp) {
       if (warp < kSmallWarps - 2) {
-        density_slices(tid, kSmallThreads - 64);
+        density_slices(tid, kSmallThreads - 64, kTwoWarpSlices);
         asm volatile("bar.sync 1, %0;" ::"n"(kSmallThreads - 64) : "memory");
       }
     } else if (warp != kSmallWarps - 2) {
       const int dw = warp < kSmallWarps - 2 ? warp : warp - 1;
-      density_slices(dw * 32 + lane, kSmallThreads - 32);
+      density_slices(dw * 32 + lane, kSmallThreads - 32, NSUB);
       asm volatile("bar.sync 1, %0;" ::"n"(kSmallThreads - 32) : "memory");
     }
   }
@@ -229,14 +231,15 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       asm volatile("bar.sync 3, %0;" ::"n"(N) : "memory");
       K_s[L] = fft_lane<N, +1>(x, L, tw_s, kb, 3);
     } else if (two_warp && chunk == 0 && warp < 2) {
-      // density (slices in order; lane L sums point bitrev(L), so rho_s's
-      // entry, slice 2's, is read by this lane before it is overwritten) and
+      // density (three slices in order; lane L sums point bitrev(L), so
+      // rho_s's entry, slice 2's, is read by this lane before it is
+      // overwritten) and
       // vH (F:147-162) on warps 0 and 1, one point per lane
       const int L = warp * 32 + lane;
       const int rb = (int)(__brev((unsigned)L) >> 26);
       double s = dslice[rb];
 #pragma unroll
-      for (int j = 1; j < NSUB; ++j) s += dslice[j * N + rb];
+      for (int j = 1; j < kTwoWarpSlices; ++j) s += dslice[j * N + rb];
       const double rho = a.occ * s;
       rho_s[rb] = rho;
       double2* hb = bufs;
@@ -368,9 +371,13 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       const int kc = pp / a.nbocc, bc = pp % a.nbocc;
       const double2* ucol = a.u + ((size_t)kc * a.nb + bc) * N;
       const double* kern = a.kern + (size_t)(kr - kc + a.nk - 1) * N;
+      // the pair's kernel row, loaded while the forward transform runs
+      double kf[E];
+#pragma unroll
+      for (int e = 0; e < E; ++e) kf[e] = __ldg(kern + TM::pos(tl, e));
       double2 x[E];
       fft_team_in<N, -1, kSmallPlan<N>>(InConjProduct<N, kSmallPlan<N>>{wcol, ucol, tl}, x, buf, tw_s, tl);
-      fft_team_in<N, +1, kSmallPlan<N>>(InScaled<N, kSmallPlan<N>>{x, kern, tl}, x, buf, tw_s, tl);
+      fft_team_in<N, +1, kSmallPlan<N>>(InScaledRegs{x, kf}, x, buf, tw_s, tl);
       if (valid) {
 #pragma unroll
         for (int e = 0; e < E; ++e) acc[e] = cfma(x[e], ucol[TM::pos(tl, e)], acc[e]);
