@@ -447,12 +447,14 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   cluster.sync();
   double exr = 0.0, exi = 0.0;
   bool bad = false;
+  // F (the P partials in chunk order) and h, from the other CTAs' shared memory
+  double fr[EPI], hr[EPI];
 #pragma unroll
   for (int r = 0; r < EPI; ++r) {
-    const int idx = tid + r * kSmallThreads, e = idx >> 1, cc = idx & 1, dd = 1 - cc;
+    fr[r] = hr[r] = 0.0;
+    const int idx = tid + r * kSmallThreads, e = idx >> 1, cc = idx & 1;
     const int q = chunk * per + e;
     if (!(e < per && q < N)) continue;
-    const double scdt = cc ? cdt : -cdt;  // k_dd = sg h_cc with sg = +1 (cc = 1) or -1 (cc = 0)
     double pr[kSmallMaxCtas];
 #pragma unroll
     for (int rr = 0; rr < kSmallMaxCtas; ++rr)
@@ -461,15 +463,32 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
 #pragma unroll
     for (int rr = 1; rr < kSmallMaxCtas; ++rr)
       if (rr < a.P) f += pr[rr];
+    fr[r] = f;
+    if (a.mode != 4) {
+      const double v = cluster.map_shared_rank(vh_s, 0)[q] + vi[r];
+      const double kin = reinterpret_cast<const double*>(cluster.map_shared_rank(K_s, 0))[2 * q + cc];
+      hr[r] = fma(v, wc[r], kin) + f;
+    }
+  }
+  // Every read of another CTA's shared memory has been consumed above.  The RK4
+  // stages arrive at the cluster barrier now and wait for it only at the end
+  // (a CTA may not exit while another still reads its shared memory), so the
+  // rest of the epilogue overlaps the barrier.
+  if (!obs) asm volatile("barrier.cluster.arrive.release;" ::: "memory");
+#pragma unroll
+  for (int r = 0; r < EPI; ++r) {
+    const int idx = tid + r * kSmallThreads, e = idx >> 1, cc = idx & 1, dd = 1 - cc;
+    const int q = chunk * per + e;
+    if (!(e < per && q < N)) continue;
+    const double scdt = cc ? cdt : -cdt;  // k_dd = sg h_cc with sg = +1 (cc = 1) or -1 (cc = 0)
+    const double f = fr[r];
     if (obs) {
       // <w|F> = sum over components: Re gets w_cc F_cc, Im gets sg w_dd F_cc
       exr = fma(wc[r], f, exr);
       exi = fma(wd[r], f, exi);
     }
     if (a.mode != 4) {
-      const double v = cluster.map_shared_rank(vh_s, 0)[q] + vi[r];
-      const double kin = reinterpret_cast<const double*>(cluster.map_shared_rank(K_s, 0))[2 * q + cc];
-      const double h = fma(v, wc[r], kin) + f;
+      const double h = hr[r];
       const size_t od = 2 * ((size_t)c * N + q) + dd;
       double nx;
       if (a.mode < 3) {
@@ -504,9 +523,13 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       ex_s[1] = si;
     }
   }
+  if (!obs) {
+    asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
+    return;
+  }
   // every read of another CTA's shared memory above is done after this barrier
   cluster.sync();
-  if (obs) {
+  {
     if (chunk == 0 && tid == 0 && occupied) {
       double sr = ex_s[0], si = ex_s[1];
       for (int r = 1; r < a.P; ++r) {
@@ -518,7 +541,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     }
     cluster.sync();  // the other CTAs stay until their shares are read
   }
-  // the RK4 stages end here; in the closing pass the last column to finish
+  // stage 0 ends here; in the closing pass the last column to finish
   // finalizes (nothing waits on another column)
   if (a.mode != 4 || chunk != 0) return;
   __syncthreads();
