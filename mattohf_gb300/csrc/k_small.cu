@@ -21,11 +21,12 @@
 //     the others split them evenly on all eight warps;
 //   * in the column's first CTA, warp 6 does the kinetic transform of the
 //     column (F:212-234);
-//   * after a cluster barrier each CTA of the column adds the P partials in
-//     chunk order for its share of the grid points (distributed shared
-//     memory), takes vH and T_A w from the first CTA the same way, and forms
-//     h w and the stage's RK4 update element by element, into a buffer that is
-//     never the stage input;
+//   * each CTA pushes its partial into the shared memory of the CTAs that own
+//     the grid points (distributed shared memory), the first CTA also vH and
+//     T_A w; after a cluster barrier each CTA adds the P partials of its
+//     points in chunk order and forms h w and the stage's RK4 update element
+//     by element, into a buffer that is never the stage input, reading only
+//     its own shared memory;
 //   * stage 0 (or the closing pass, mode 4) also gathers the observables of
 //     its input, i.e. of the previous step (F:74-119, F:165-183, F:289-318):
 //     Ekin and Je per column by Parseval on a forward transform of the column
@@ -70,8 +71,13 @@ struct SmallLayout {
   // transform and warp 7 the density and Hartree potential), the autotuner's
   // lower bound on the CTAs per column
   static constexpr int PAIR_TEAMS = (kSmallWarps - 2) * PW;
-  // tw[N], bufs[NTEAM][N], F[N] (double2); rho[N], vh[N] (double); K[N] (double2)
-  static constexpr size_t bytes = sizeof(double2) * (size_t)N * (3 + NTEAM) + sizeof(double) * 2 * (size_t)N;
+  // tw[N], bufs[NTEAM][N], F[N] (double2); rho[N], vh[N] (double); K[N] (double2);
+  // then what the cluster's CTAs push to this one for its share of the grid
+  // points: the P exchange partials (at most 2N + 2 kSmallMaxCtas doubles),
+  // vH and T_A w (N and 2N doubles)
+  static constexpr int RECV_F = 2 * N + 2 * kSmallMaxCtas;
+  static constexpr size_t bytes = sizeof(double2) * (size_t)N * (3 + NTEAM) + sizeof(double) * 2 * (size_t)N +
+                                  sizeof(double) * ((size_t)RECV_F + 3 * (size_t)N);
 };
 
 // The global last CTA of an observable stage: the observables of the stage
@@ -136,9 +142,12 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   double* rho_s = reinterpret_cast<double*>(F_s + N);
   double* vh_s = rho_s + N;
   double2* K_s = reinterpret_cast<double2*>(vh_s + N);  // N: T_A w (the column's first CTA)
+  double* recvF = reinterpret_cast<double*>(K_s + N);   // [P][2 per]: the partials of this CTA's points
+  double* recvV = recvF + SmallLayout<N>::RECV_F;       // [per]: vH at this CTA's points
+  double* recvK = recvV + N;                            // [2 per]: T_A w at this CTA's points
   __shared__ int last_s;
   __shared__ double red_s[2][kSmallWarps];
-  __shared__ double ex_s[2];               // this CTA's share of <w|F>
+  __shared__ double ex_s[kSmallMaxCtas][2];  // the first CTA: every CTA's share of <w|F>
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int tl = lane % T, team = warp * PW + lane / T;
   double2* buf = bufs + team * N;
@@ -168,6 +177,9 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   // without a programmatic dependency.
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;");
+  // every CTA of the cluster has started once this barrier phase completes;
+  // it is waited for only before the first store to another CTA's memory
+  asm volatile("barrier.cluster.arrive.relaxed;" ::: "memory");
   if (a.it_out && blockIdx.x == 0 && tid == 0) *a.it_out = *a.it + a.it_inc;
   // density, first part: sum of |u|^2 over slice j of the occupied orbitals at
   // point ig, one (j, ig) per thread and round.  F_s, rho_s and vh_s (4N
@@ -427,27 +439,38 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     }
   }
   __syncthreads();
-  // this CTA's partial (pair teams in order; a team past the CTA's pair count
-  // holds none), kept in its shared memory, one real component per thread
+  // This CTA's partial (pair teams in order; a team past the CTA's pair count
+  // holds none), one real component per thread, pushed into the shared memory
+  // of the CTA that owns the point (distributed shared memory); the first CTA
+  // also pushes vH and T_A w.  After the cluster barrier every CTA finds the
+  // P partials of its points in its own shared memory and does h w and the
+  // RK4 update for its share of the grid, with no remote reads.
+  cg::cluster_group cluster = cg::this_cluster();
+  asm volatile("barrier.cluster.wait;" ::: "memory");
   const int act = (a.hf && (a.mode != 4 || occupied)) ? min(worker_teams, p1 - p0) : 0;
   {
     const double* bd = reinterpret_cast<const double*>(bufs);
-    double* Fd = reinterpret_cast<double*>(F_s);
     for (int i = tid; i < 2 * N; i += kSmallThreads) {
       double f = 0.0;
       if (act > 0) f = bd[i];
       for (int t2 = 1; t2 < act; ++t2) f += bd[(size_t)t2 * 2 * N + i];
-      Fd[i] = f;
+      const int q = i >> 1, owner = q / per, e = q - owner * per;
+      cluster.map_shared_rank(recvF, owner)[chunk * 2 * per + 2 * e + (i & 1)] = f;
+    }
+    if (chunk == 0 && a.mode != 4) {
+      for (int q = tid; q < N; q += kSmallThreads) {
+        const int owner = q / per, e = q - owner * per;
+        cluster.map_shared_rank(recvV, owner)[e] = vh_s[q];
+        double* rk = cluster.map_shared_rank(recvK, owner);
+        rk[2 * e] = K_s[q].x;
+        rk[2 * e + 1] = K_s[q].y;
+      }
     }
   }
-  // the column's P CTAs form a cluster: after this barrier every CTA reads the
-  // P partials and the first CTA's vH and T_A w through distributed shared
-  // memory, and does h w and the RK4 update for its own share of the grid
-  cg::cluster_group cluster = cg::this_cluster();
   cluster.sync();
   double exr = 0.0, exi = 0.0;
   bool bad = false;
-  // F (the P partials in chunk order) and h, from the other CTAs' shared memory
+  // F (the P partials in chunk order) and h, from this CTA's shared memory
   double fr[EPI], hr[EPI];
 #pragma unroll
   for (int r = 0; r < EPI; ++r) {
@@ -455,26 +478,13 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     const int idx = tid + r * kSmallThreads, e = idx >> 1, cc = idx & 1;
     const int q = chunk * per + e;
     if (!(e < per && q < N)) continue;
-    double pr[kSmallMaxCtas];
-#pragma unroll
-    for (int rr = 0; rr < kSmallMaxCtas; ++rr)
-      if (rr < a.P) pr[rr] = reinterpret_cast<const double*>(cluster.map_shared_rank(F_s, rr))[2 * q + cc];
-    double f = pr[0];
+    double f = recvF[2 * e + cc];
 #pragma unroll
     for (int rr = 1; rr < kSmallMaxCtas; ++rr)
-      if (rr < a.P) f += pr[rr];
+      if (rr < a.P) f += recvF[rr * 2 * per + 2 * e + cc];
     fr[r] = f;
-    if (a.mode != 4) {
-      const double v = cluster.map_shared_rank(vh_s, 0)[q] + vi[r];
-      const double kin = reinterpret_cast<const double*>(cluster.map_shared_rank(K_s, 0))[2 * q + cc];
-      hr[r] = fma(v, wc[r], kin) + f;
-    }
+    if (a.mode != 4) hr[r] = fma(recvV[e] + vi[r], wc[r], recvK[2 * e + cc]) + f;
   }
-  // Every read of another CTA's shared memory has been consumed above.  The RK4
-  // stages arrive at the cluster barrier now and wait for it only at the end
-  // (a CTA may not exit while another still reads its shared memory), so the
-  // rest of the epilogue overlaps the barrier.
-  if (!obs) asm volatile("barrier.cluster.arrive.release;" ::: "memory");
 #pragma unroll
   for (int r = 0; r < EPI; ++r) {
     const int idx = tid + r * kSmallThreads, e = idx >> 1, cc = idx & 1, dd = 1 - cc;
@@ -519,27 +529,23 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
         sr += red_s[0][w2];
         si += red_s[1][w2];
       }
-      ex_s[0] = sr;
-      ex_s[1] = si;
+      double* dst = cluster.map_shared_rank(&ex_s[0][0], 0) + 2 * chunk;  // the first CTA's slot
+      dst[0] = sr;
+      dst[1] = si;
     }
   }
-  if (!obs) {
-    asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
-    return;
-  }
-  // every read of another CTA's shared memory above is done after this barrier
+  // No CTA touches another's shared memory after the barrier above, so the
+  // RK4 stages are done; stage 0 and the closing pass collect <w|F> once more
+  if (!obs) return;
   cluster.sync();
-  {
-    if (chunk == 0 && tid == 0 && occupied) {
-      double sr = ex_s[0], si = ex_s[1];
-      for (int r = 1; r < a.P; ++r) {
-        sr += cluster.map_shared_rank(ex_s, r)[0];
-        si += cluster.map_shared_rank(ex_s, r)[1];
-      }
-      a.colbuf[(size_t)c * 4 + 2] = sr;
-      a.colbuf[(size_t)c * 4 + 3] = si;
+  if (chunk == 0 && tid == 0 && occupied) {
+    double sr = ex_s[0][0], si = ex_s[0][1];
+    for (int r = 1; r < a.P; ++r) {
+      sr += ex_s[r][0];
+      si += ex_s[r][1];
     }
-    cluster.sync();  // the other CTAs stay until their shares are read
+    a.colbuf[(size_t)c * 4 + 2] = sr;
+    a.colbuf[(size_t)c * 4 + 3] = si;
   }
   // stage 0 ends here; in the closing pass the last column to finish
   // finalizes (nothing waits on another column)
