@@ -547,26 +547,28 @@ def measure_adjoint(nt: int, fd_samples: int) -> dict:
                 q[h] = (obj(Ap) - obj(Am)) / (2 * h)
             rows.append((g[n], q.get(1e-4, np.nan), q[1e-6],
                          max(abs(q[1e-6] - q[1.25e-6]), abs(q[1e-6] - q[0.8e-6]))))
-    rows = np.array(rows)
-    gs_, f4, f6, spread = rows.T
-    rel6 = np.abs(gs_ - f6) / np.abs(f6)
-    bound6 = 1e-6 + 3 * spread / np.abs(f6)
-    m4 = np.isfinite(f4)
-    rel4 = np.abs(gs_[m4] - f4[m4]) / np.abs(f4[m4])
+    fd = {"samples": 0}
+    if rows:
+        gs_, f4, f6, spread = np.array(rows).T
+        rel6 = np.abs(gs_ - f6) / np.abs(f6)
+        bound6 = 1e-6 + 3 * spread / np.abs(f6)
+        m4 = np.isfinite(f4)
+        rel4 = np.abs(gs_[m4] - f4[m4]) / np.abs(f4[m4])
+        fd = {"samples": int(fd_samples),
+              "h1e-6": {"max_rel_err_per_sample": float(rel6.max()),
+                        "median_rel_err": float(np.median(rel6)),
+                        "normwise_rel_err": float(np.max(np.abs(gs_ - f6)) / np.max(np.abs(f6))),
+                        "within_1e-6_plus_roundoff": int(np.sum(rel6 <= bound6)),
+                        "max_roundoff_bound_rel": float((3 * spread / np.abs(f6)).max()),
+                        "note": "round-off bound per sample = 3 x max(|fd(h) - fd(1.25 h)|, |fd(h) - fd(0.8 h)|)"},
+              "h1e-4": {"samples": int(m4.sum()), "max_rel_err_per_sample": float(rel4.max())}}
     return {"metric": "adjoint-gradient/forward time ratio", "value": t_adj / t_fwd, "unit": "ratio",
             "higher_is_better": False, "forward_ms": t_fwd, "adjoint_ms": t_adj, "steps": nt,
             "objective": L,
             "auto_checkpoint": {"value": t_adj_auto / t_fwd, "adjoint_ms": t_adj_auto,
                                 "note": "ckpt_every=0: all stage inputs stored, no recomputation",
                                 "grad_rel_diff_vs_ckpt100": auto_diff},
-            "fd": {"samples": int(fd_samples),
-                   "h1e-6": {"max_rel_err_per_sample": float(rel6.max()),
-                             "median_rel_err": float(np.median(rel6)),
-                             "normwise_rel_err": float(np.max(np.abs(gs_ - f6)) / np.max(np.abs(f6))),
-                             "within_1e-6_plus_roundoff": int(np.sum(rel6 <= bound6)),
-                             "max_roundoff_bound_rel": float((3 * spread / np.abs(f6)).max()),
-                             "note": "round-off bound per sample = 3 x max(|fd(h) - fd(1.25 h)|, |fd(h) - fd(0.8 h)|)"},
-                   "h1e-4": {"samples": int(m4.sum()), "max_rel_err_per_sample": float(rel4.max())}},
+            "fd": fd,
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": f"a=10, NK=16, Nocc=2, NG=128, {nt} steps, pulse+N(0,1e-3), "
                                    "checkpoints every 100", "dt": cfg.dt}}
