@@ -188,8 +188,6 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   // threads; with several CTAs per column the first CTA's kinetic warp (6)
   // starts its transforms at once and the other seven warps sum the slices.
   constexpr int NSUB = (kSmallThreads / N) < 4 ? (kSmallThreads / N) : 4;
-  // with the two-warp chains at NG = 64, six warps hold one slot each
-  constexpr int kTwoWarpSlices = (kSmallThreads - 64) / 64;
   double* dslice = reinterpret_cast<double*>(F_s);  // [NSUB][N]
   auto density_slices = [&](int t0, int nthreads, int nsub) {
     const int per = (M + nsub - 1) / nsub;
@@ -208,17 +206,14 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   };
   // At NG = 64 with several CTAs per column the first CTA's Hartree (warps 0
   // and 1) and kinetic (warps 6 and 7) chains each run on two warps, one
-  // point per lane (fft_lane); warps 0-5 sum the density slices.
+  // point per lane (fft_lane), after all eight warps have summed the density
+  // slices (the kinetic chain could start at once, but its FP64 issue would
+  // slow the density down, and the Hartree chain waits for that).
   const bool two_warp = N == 64 && a.P > 1 && a.mode != 4;
   if (chunk == 0) {
-    if (a.P == 1) {
+    if (a.P == 1 || two_warp) {
       density_slices(tid, kSmallThreads, NSUB);
       __syncthreads();
-    } else if (two_warp) {
-      if (warp < kSmallWarps - 2) {
-        density_slices(tid, kSmallThreads - 64, kTwoWarpSlices);
-        asm volatile("bar.sync 1, %0;" ::"n"(kSmallThreads - 64) : "memory");
-      }
     } else if (warp != kSmallWarps - 2) {
       const int dw = warp < kSmallWarps - 2 ? warp : warp - 1;
       density_slices(dw * 32 + lane, kSmallThreads - 32, NSUB);
@@ -243,15 +238,15 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
       asm volatile("bar.sync 3, %0;" ::"n"(N) : "memory");
       K_s[L] = fft_lane<N, +1>(x, L, tw_s, kb, 3);
     } else if (two_warp && chunk == 0 && warp < 2) {
-      // density (three slices in order; lane L sums point bitrev(L), so
-      // rho_s's entry, slice 2's, is read by this lane before it is
-      // overwritten) and
+      // density (slices in order; lane L sums point bitrev(L), so rho_s's
+      // entry, slice 2's, is read by this lane before it is overwritten, and
+      // vh_s's, slice 3's, before the barriers inside fft_lane) and
       // vH (F:147-162) on warps 0 and 1, one point per lane
       const int L = warp * 32 + lane;
       const int rb = (int)(__brev((unsigned)L) >> 26);
       double s = dslice[rb];
 #pragma unroll
-      for (int j = 1; j < kTwoWarpSlices; ++j) s += dslice[j * N + rb];
+      for (int j = 1; j < NSUB; ++j) s += dslice[j * N + rb];
       const double rho = a.occ * s;
       rho_s[rb] = rho;
       double2* hb = bufs;
