@@ -247,6 +247,16 @@ struct InConjProduct {
   }
 };
 
+// Slot of element i in the team buffer: i ^ ((i >> 3) & 7), a permutation
+// inside each aligned group of 8 double2 (128 bytes, one row of the 32
+// shared-memory banks).  The first pass stores R0 consecutive elements per
+// lane; in natural order lane j's element r sits at j R0 + r, so with R0 = 8
+// every lane of the warp hits the same banks (32 wavefronts per store
+// instead of 4).  Swizzled, the 8 lanes of a wavefront hit 8 different
+// 16-byte bank groups, and the unit-stride accesses of the other passes
+// stay conflict-free (a permutation within an aligned group of 8).
+__device__ __forceinline__ int fft_slot(int i) { return i ^ ((i >> 3) & 7); }
+
 // One Stockham pass reading and writing the team buffer.
 template <int N, int R, int NS, int DIR, int T>
 __device__ __forceinline__ void fft_mid_pass(double2* buf, const double2* __restrict__ tw, int tl) {
@@ -260,7 +270,7 @@ __device__ __forceinline__ void fft_mid_pass(double2* buf, const double2* __rest
     const int k = j % NS;
     double2 w[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[p][r] = buf[j + r * NBF];
+    for (int r = 0; r < R; ++r) v[p][r] = buf[fft_slot(j + r * NBF)];
 #pragma unroll
     for (int r = 1; r < R; ++r) {
       w[r] = tw[(r * k) * (N / (NS * R))];
@@ -274,7 +284,7 @@ __device__ __forceinline__ void fft_mid_pass(double2* buf, const double2* __rest
     const int j = tl + T * p;
     const int base = (j / NS) * NS * R + (j % NS);
 #pragma unroll
-    for (int r = 0; r < R; ++r) buf[base + r * NS] = v[p][r];
+    for (int r = 0; r < R; ++r) buf[fft_slot(base + r * NS)] = v[p][r];
   }
   __syncwarp();
 }
@@ -310,7 +320,7 @@ __device__ __forceinline__ void fft_team_in(const In& in, double2 (&x)[Team<N, L
   for (int p = 0; p < TM::PER; ++p) {
     const int j = tl + T * p;
 #pragma unroll
-    for (int r = 0; r < R0; ++r) buf[j * R0 + r] = x[p * R0 + r];
+    for (int r = 0; r < R0; ++r) buf[fft_slot(j * R0 + r)] = x[p * R0 + r];
   }
   __syncwarp();
   fft_mid_passes<N, L, DIR, T, 1, R0>(buf, tw, tl);
@@ -324,7 +334,7 @@ __device__ __forceinline__ void fft_team_in(const In& in, double2 (&x)[Team<N, L
     const int k = j;  // j < NS
     double2 w[RL];
 #pragma unroll
-    for (int r = 0; r < RL; ++r) x[p * RL + r] = buf[j + r * NS];
+    for (int r = 0; r < RL; ++r) x[p * RL + r] = buf[fft_slot(j + r * NS)];
 #pragma unroll
     for (int r = 1; r < RL; ++r) {
       w[r] = tw[r * k];  // N/(NS*RL) == 1
