@@ -540,6 +540,7 @@ def test_autotune_restores_state_and_keeps_results(NG, NK, NB):
         ctx.Gram_Schmidt()
         u0 = ctx.get_orbitals()
         E0, J0, N0 = ctx.rk4_run(A, Aave, dt)
+        u_end0 = ctx.get_orbitals()
         ctx.set_orbitals(u0)
         res = ctx.autotune(steps=8)
         assert np.array_equal(ctx.get_orbitals(), u0)
@@ -553,9 +554,11 @@ def test_autotune_restores_state_and_keeps_results(NG, NK, NB):
         # every CTAs-per-column setting of the fused stages gives the same run,
         # including grids far beyond one wave (the stage field is read by each
         # column's first CTA while other columns finish)
-        for P in (1, 2, 3, 8, 12, 24):
+        for P in (1, 2, 3, 4, 5, 6, 8, 12, 24):
             ctx.set_option(_capi.OPT_SMALL_STAGES, 1)
             ctx.set_option(_capi.OPT_SMALL_CTAS, P)
             ctx.set_orbitals(u0)
             E, J, N = ctx.rk4_run(A, Aave, dt)
             assert rel(E, E0) <= 1e-12 and rel(N, N0) <= 1e-12, P
+            assert np.max(np.abs(J - J0)) <= 1e-12 * max(1.0, np.max(np.abs(J0))), P
+            assert rel(ctx.get_orbitals(), u_end0) <= 1e-12, P
