@@ -408,16 +408,28 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   constexpr int EPI = (2 * N + kSmallThreads - 1) / kSmallThreads;  // lane slots per thread
   const int per = (N + a.P - 1) / a.P;
   const double cdt = a.mode == 2 ? a.dt : 0.5 * a.dt;
-  double wc[EPI], wd[EPI], vi[EPI], ud[EPI], ks[EPI];
+  double wc[EPI], vi[EPI], ud[EPI], ks[EPI];
+  // stage 0 and the closing pass: the w factors of this thread's components
+  // in the partial sum below (component i = 2 q + cc of every point)
+  double wt[EPI][2];
 #pragma unroll
   for (int r = 0; r < EPI; ++r) {
-    wc[r] = wd[r] = vi[r] = ud[r] = ks[r] = 0.0;
+    wt[r][0] = wt[r][1] = 0.0;
+    const int i = tid + r * kSmallThreads;
+    if (obs && i < 2 * N) {
+      const double* w2 = reinterpret_cast<const double*>(wcol + (i >> 1));
+      wt[r][0] = w2[i & 1];
+      wt[r][1] = (i & 1) ? w2[0] : -w2[1];
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < EPI; ++r) {
+    wc[r] = vi[r] = ud[r] = ks[r] = 0.0;
     const int idx = tid + r * kSmallThreads, e = idx >> 1, cc = idx & 1, dd = 1 - cc;
     const int q = chunk * per + e;
     if (e < per && q < N) {
       const double* w2 = reinterpret_cast<const double*>(wcol + q);
       wc[r] = w2[cc];
-      wd[r] = cc ? w2[dd] : -w2[dd];  // sg w_dd, sg = +1 for cc = 1, -1 for cc = 0
       if (a.mode != 4) {
         const size_t od = 2 * ((size_t)c * N + q) + dd;
         vi[r] = a.vion[q];
@@ -445,12 +457,43 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   const int act = (a.hf && (a.mode != 4 || occupied)) ? min(worker_teams, p1 - p0) : 0;
   {
     const double* bd = reinterpret_cast<const double*>(bufs);
-    for (int i = tid; i < 2 * N; i += kSmallThreads) {
+    // stage 0 and the closing pass: this CTA's share of <w|F> = sum over all
+    // points of conj(w) F_chunk, one real component per thread (Re gets
+    // w_cc F_cc, Im gets sg w_dd F_cc with sg = +1 for cc = 1, -1 for cc = 0)
+    double exr = 0.0, exi = 0.0;
+#pragma unroll
+    for (int r = 0; r < EPI; ++r) {
+      const int i = tid + r * kSmallThreads;
+      if (i >= 2 * N) continue;
       double f = 0.0;
       if (act > 0) f = bd[i];
       for (int t2 = 1; t2 < act; ++t2) f += bd[(size_t)t2 * 2 * N + i];
-      const int q = i >> 1, owner = q / per, e = q - owner * per;
-      cluster.map_shared_rank(recvF, owner)[chunk * 2 * per + 2 * e + (i & 1)] = f;
+      const int q = i >> 1, cc = i & 1, owner = q / per, e = q - owner * per;
+      cluster.map_shared_rank(recvF, owner)[chunk * 2 * per + 2 * e + cc] = f;
+      if (obs) {
+        exr = fma(wt[r][0], f, exr);
+        exi = fma(wt[r][1], f, exi);
+      }
+    }
+    if (obs) {
+      // warp tree, then warps in order, pushed to the first CTA's slot
+      exr = small_warp_sum(exr);
+      exi = small_warp_sum(exi);
+      if (lane == 0) {
+        red_s[0][warp] = exr;
+        red_s[1][warp] = exi;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        double sr = red_s[0][0], si = red_s[1][0];
+        for (int w2 = 1; w2 < kSmallWarps; ++w2) {
+          sr += red_s[0][w2];
+          si += red_s[1][w2];
+        }
+        double* dst = cluster.map_shared_rank(&ex_s[0][0], 0) + 2 * chunk;
+        dst[0] = sr;
+        dst[1] = si;
+      }
     }
     if (chunk == 0 && a.mode != 4) {
       for (int q = tid; q < N; q += kSmallThreads) {
@@ -463,13 +506,21 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     }
   }
   cluster.sync();
-  double exr = 0.0, exi = 0.0;
+  if (obs && chunk == 0 && tid == 0 && occupied) {
+    double sr = ex_s[0][0], si = ex_s[0][1];
+    for (int r = 1; r < a.P; ++r) {
+      sr += ex_s[r][0];
+      si += ex_s[r][1];
+    }
+    a.colbuf[(size_t)c * 4 + 2] = sr;
+    a.colbuf[(size_t)c * 4 + 3] = si;
+  }
   bool bad = false;
   // F (the P partials in chunk order) and h, from this CTA's shared memory
-  double fr[EPI], hr[EPI];
+  double hr[EPI];
 #pragma unroll
   for (int r = 0; r < EPI; ++r) {
-    fr[r] = hr[r] = 0.0;
+    hr[r] = 0.0;
     const int idx = tid + r * kSmallThreads, e = idx >> 1, cc = idx & 1;
     const int q = chunk * per + e;
     if (!(e < per && q < N)) continue;
@@ -477,7 +528,6 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
 #pragma unroll
     for (int rr = 1; rr < kSmallMaxCtas; ++rr)
       if (rr < a.P) f += recvF[rr * 2 * per + 2 * e + cc];
-    fr[r] = f;
     if (a.mode != 4) hr[r] = fma(recvV[e] + vi[r], wc[r], recvK[2 * e + cc]) + f;
   }
 #pragma unroll
@@ -486,12 +536,6 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     const int q = chunk * per + e;
     if (!(e < per && q < N)) continue;
     const double scdt = cc ? cdt : -cdt;  // k_dd = sg h_cc with sg = +1 (cc = 1) or -1 (cc = 0)
-    const double f = fr[r];
-    if (obs) {
-      // <w|F> = sum over components: Re gets w_cc F_cc, Im gets sg w_dd F_cc
-      exr = fma(wc[r], f, exr);
-      exi = fma(wd[r], f, exi);
-    }
     if (a.mode != 4) {
       const double h = hr[r];
       const size_t od = 2 * ((size_t)c * N + q) + dd;
@@ -509,40 +553,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     }
   }
   if (bad && a.nonfinite) *a.nonfinite = 1;
-  if (obs) {
-    // <w|F>: this CTA's elements in thread order (warp tree, then warps in order)
-    exr = small_warp_sum(exr);
-    exi = small_warp_sum(exi);
-    if (lane == 0) {
-      red_s[0][warp] = exr;
-      red_s[1][warp] = exi;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      double sr = red_s[0][0], si = red_s[1][0];
-      for (int w2 = 1; w2 < kSmallWarps; ++w2) {
-        sr += red_s[0][w2];
-        si += red_s[1][w2];
-      }
-      double* dst = cluster.map_shared_rank(&ex_s[0][0], 0) + 2 * chunk;  // the first CTA's slot
-      dst[0] = sr;
-      dst[1] = si;
-    }
-  }
-  // No CTA touches another's shared memory after the barrier above, so the
-  // RK4 stages are done; stage 0 and the closing pass collect <w|F> once more
-  if (!obs) return;
-  cluster.sync();
-  if (chunk == 0 && tid == 0 && occupied) {
-    double sr = ex_s[0][0], si = ex_s[0][1];
-    for (int r = 1; r < a.P; ++r) {
-      sr += ex_s[r][0];
-      si += ex_s[r][1];
-    }
-    a.colbuf[(size_t)c * 4 + 2] = sr;
-    a.colbuf[(size_t)c * 4 + 3] = si;
-  }
-  // stage 0 ends here; in the closing pass the last column to finish
+  // No CTA touches another's shared memory after the cluster barrier, so the
+  // stage is done; in the closing pass the last column to finish
   // finalizes (nothing waits on another column)
   if (a.mode != 4 || chunk != 0) return;
   __syncthreads();
