@@ -6,21 +6,24 @@
 // 154-173).  Output column c = (k, b) is served by P CTAs (c, chunk) that form
 // one thread-block cluster:
 //   * the column's first CTA computes the density of the stage input
-//     (F:55-71): all its warps but the kinetic one (all threads when the
-//     column has one CTA) first sum |u|^2 over slices of the occupied
+//     (F:55-71): its warps first sum |u|^2 over slices of the occupied
 //     orbitals (in ik -> ib order within a slice, the uniform occupation
-//     applied once); then its last warp adds the slices and forms the Hartree
-//     potential (F:147-162).  A warp issues at most one FP64 instruction per
-//     ~64 cycles, so one warp alone would take about 4 us for the sum.  The
-//     kinetic warp does not wait for the density;
+//     applied once); then the slices are added and the Hartree potential
+//     formed (F:147-162).  At NG = 64 with several CTAs per column all eight
+//     warps sum the slices and warps 0-1 then form vH as one 64-lane
+//     transform pair (one point per lane); otherwise the kinetic warp skips
+//     the slices and warp 7 forms vH.  A warp issues at most one FP64
+//     instruction per ~64 cycles, so one warp alone would take about 4 us
+//     for the sum;
 //   * the CTAs apply the exchange of column c against their chunks of the
 //     occupied orbitals (F:237-261, ordered pairs, no symmetry), one pair per
 //     team, and each keeps its partial sum in shared memory.  With more than
 //     one CTA per column the first CTA, which carries the density, the
 //     kinetic and Hartree transforms and the Parseval sums, takes no pairs;
 //     the others split them evenly on all eight warps;
-//   * in the column's first CTA, warp 6 does the kinetic transform of the
-//     column (F:212-234);
+//   * in the column's first CTA, warp 6 (at NG = 64 with several CTAs per
+//     column, warps 6-7 as one 64-lane team) does the kinetic transform of
+//     the column (F:212-234);
 //   * each CTA pushes its partial into the shared memory of the CTAs that own
 //     the grid points (distributed shared memory), the first CTA also vH and
 //     T_A w; after a cluster barrier each CTA adds the P partials of its
@@ -32,8 +35,10 @@
 //     Ekin and Je per column by Parseval on a forward transform of the column
 //     at the previous step's field (warp 3 of the first CTA, idle when a
 //     column has several CTAs, else warp 6 with its kinetic transform),
-//     <u|F u> from the CTAs' shares, and column 0's copy of the density and
-//     vH.  Stage 1 then forms Etot, Je, Nele on an idle warp of column 0's
+//     <u|F u> from the CTAs' shares (each CTA's partial against w over all
+//     points, pushed to the first CTA before the cluster barrier), and column
+//     0's copy of the density and vH.  Stage 1 then forms Etot, Je, Nele on
+//     an idle warp of column 0's
 //     first CTA, so no stage-0 CTA waits for a global ticket; the closing pass
 //     still has the last column to finish (global ticket) write them.
 //     The step counter has a shadow: stage 0 copies the counter to it and
