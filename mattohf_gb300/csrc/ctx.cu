@@ -677,7 +677,8 @@ SmallStageArgs small_base(mattohf_ctx* ctx, double dt) {
 // One RK4 step as four fused stage launches.  Stage inputs and outputs
 // alternate between d_us and d_hpre so that no launch writes its own input.
 // Stage 0 also writes the observables of the previous step (its input).
-// With `store`, each stage input also goes to the adjoint's stage store.
+// With `store`, each stage input also goes to the adjoint's stage store (the
+// stage kernel copies it).
 // The step counter d_int[0] holds the step index between steps (the host,
 // the checkpoint and store copies read and set it there).  Stage 0 copies it
 // to the shadow d_int[3]; stage 3 reads its field at the shadow's index and
@@ -690,7 +691,11 @@ int enq_small_step(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, dou
   int* const shadow = ctx->d_int + 3;
   fs[3].it = shadow;
   for (int s = 0; s < 4; ++s) {
-    if (store) CKR(launch_store_stage(ctx, in[s], s));
+    // with `store`, each stage copies its input into the adjoint's stage
+    // store itself (no separate copy launch between the stages)
+    a.store = store ? ctx->d_store : nullptr;
+    a.seg0 = ctx->d_adj_int + 1;
+    a.store_slot = s;
     a.u = in[s];
     a.out = out[s];
     a.mode = s;

@@ -224,6 +224,9 @@ struct SmallStageArgs {
   unsigned* ticket;         // [1 + ncols]: global, then per-column completion counters
   double* out_obs;          // mode 4: [7] Etot, Ekin, Eion, EH, Ex, Je, Nele
   double* obs_dens;         // [2][NG]: density and vH of stage 0's input (column 0), read by stage 1
+  double2* store;           // if set: the adjoint's stage store; the stage input goes to slot
+  const int* seg0;          // ((*it - *seg0) * 4 + store_slot) (each CTA copies its points)
+  int store_slot;
 };
 // CTAs per column of the fused stages: one thread-block cluster per column
 // (the portable cluster size)

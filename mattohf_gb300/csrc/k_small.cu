@@ -81,8 +81,9 @@ struct SmallLayout {
   // points: the P exchange partials (at most 2N + 2 kSmallMaxCtas doubles),
   // vH and T_A w (N and 2N doubles)
   static constexpr int RECV_F = 2 * N + 2 * kSmallMaxCtas;
+  // (and N double2 staging the adjoint's stage-store copy)
   static constexpr size_t bytes = sizeof(double2) * (size_t)N * (3 + NTEAM) + sizeof(double) * 2 * (size_t)N +
-                                  sizeof(double) * ((size_t)RECV_F + 3 * (size_t)N);
+                                  sizeof(double) * ((size_t)RECV_F + 3 * (size_t)N) + sizeof(double2) * (size_t)N;
 };
 
 // The global last CTA of an observable stage: the observables of the stage
@@ -150,6 +151,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   double* recvF = reinterpret_cast<double*>(K_s + N);   // [P][2 per]: the partials of this CTA's points
   double* recvV = recvF + SmallLayout<N>::RECV_F;       // [per]: vH at this CTA's points
   double* recvK = recvV + N;                            // [2 per]: T_A w at this CTA's points
+  double2* st_s = reinterpret_cast<double2*>(recvK + 2 * N);  // [per]: staged stage-store copy
   __shared__ int last_s;
   __shared__ double red_s[2][kSmallWarps];
   __shared__ double ex_s[kSmallMaxCtas][2];  // the first CTA: every CTA's share of <w|F>
@@ -186,6 +188,17 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   // it is waited for only before the first store to another CTA's memory
   asm volatile("barrier.cluster.arrive.relaxed;" ::: "memory");
   if (a.it_out && blockIdx.x == 0 && tid == 0) *a.it_out = *a.it + a.it_inc;
+  // the adjoint's recompute: this CTA's points of the stage input, staged in
+  // shared memory by an asynchronous copy now and written to the stage store
+  // once the first phase is done (no registers held, no latency exposed)
+  if (a.store) {
+    const int per_pts = (N + a.P - 1) / a.P, q_st = chunk * per_pts + tid;
+    if (tid < per_pts && q_st < N) {
+      const unsigned dst = (unsigned)__cvta_generic_to_shared(st_s + tid);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(wcol + q_st) : "memory");
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+  }
   // density, first part: sum of |u|^2 over slice j of the occupied orbitals at
   // point ig, one (j, ig) per thread and round.  F_s, rho_s and vh_s (4N
   // contiguous doubles) are free during the first phase and hold the slices.
@@ -451,6 +464,11 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     }
   }
   __syncthreads();
+  if (a.store && tid < per && chunk * per + tid < N) {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    const size_t elems = (size_t)ncols * N;
+    a.store[((size_t)(*a.it - *a.seg0) * 4 + a.store_slot) * elems + (size_t)c * N + chunk * per + tid] = st_s[tid];
+  }
   // This CTA's partial (pair teams in order; a team past the CTA's pair count
   // holds none), one real component per thread, pushed into the shared memory
   // of the CTA that owns the point (distributed shared memory); the first CTA
