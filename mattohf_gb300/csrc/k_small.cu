@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   extern __shared__ double2 sm2[];
   double2* tw_s = sm2;                     // N
   double2* bufs = tw_s + N;                // NTEAM * N
-  double2* F_s = bufs + NTEAM * N;         // N: this CTA's exchange partial
+  double2* F_s = bufs + NTEAM * N;         // N: with rho_s and vh_s, the density slices
   double* rho_s = reinterpret_cast<double*>(F_s + N);
   double* vh_s = rho_s + N;
   double2* K_s = reinterpret_cast<double2*>(vh_s + N);  // N: T_A w (the column's first CTA)
@@ -202,9 +202,10 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   // density, first part: sum of |u|^2 over slice j of the occupied orbitals at
   // point ig, one (j, ig) per thread and round.  F_s, rho_s and vh_s (4N
   // contiguous doubles) are free during the first phase and hold the slices.
-  // Only the Hartree warp waits for them.  A single CTA sums them on all its
-  // threads; with several CTAs per column the first CTA's kinetic warp (6)
-  // starts its transforms at once and the other seven warps sum the slices.
+  // Only the Hartree chain waits for them.  A single CTA, and the first CTA at
+  // NG = 64 with several CTAs per column, sums them on all its threads;
+  // otherwise the first CTA's kinetic warp (6) starts its transforms at once
+  // and the other seven warps sum the slices.
   constexpr int NSUB = (kSmallThreads / N) < 4 ? (kSmallThreads / N) : 4;
   double* dslice = reinterpret_cast<double*>(F_s);  // [NSUB][N]
   auto density_slices = [&](int t0, int nthreads, int nsub) {
