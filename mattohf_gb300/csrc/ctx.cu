@@ -683,7 +683,10 @@ SmallStageArgs small_base(mattohf_ctx* ctx, double dt) {
 // the checkpoint and store copies read and set it there).  Stage 0 copies it
 // to the shadow d_int[3]; stage 3 reads its field at the shadow's index and
 // writes index + 1 to d_int[0], which none of its CTAs reads.
-int enq_small_step(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt, bool store = false) {
+// With `ckpt_every` > 0, stage 0 also writes its input to checkpoint
+// (it + ckpt_phase) / ckpt_every when it is a segment start (as k_checkpoint).
+int enq_small_step(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, double dt, bool store = false,
+                   int ckpt_every = 0, int ckpt_phase = 0) {
   SmallStageArgs a = small_base(ctx, dt);
   const double2* in[4] = {ctx->d_u, ctx->d_us, ctx->d_hpre, ctx->d_us};
   double2* out[4] = {ctx->d_us, ctx->d_hpre, ctx->d_us, nullptr};
@@ -696,6 +699,9 @@ int enq_small_step(mattohf_ctx* ctx, AField f_m, AField f_ave, AField f_cur, dou
     a.store = store ? ctx->d_store : nullptr;
     a.seg0 = ctx->d_adj_int + 1;
     a.store_slot = s;
+    a.ckpt = (ckpt_every > 0 && s == 0) ? ctx->d_ckpt : nullptr;
+    a.ckpt_every = ckpt_every;
+    a.ckpt_phase = ckpt_phase;
     a.u = in[s];
     a.out = out[s];
     a.mode = s;
@@ -2148,8 +2154,9 @@ extern "C" int mattohf_adjoint(mattohf_ctx* ctx, int objective, int nt, double d
   int rc = MATTOHF_OK;
   if (nseg > 1)
     rc = capture_steps(&gfwd, &gfwd8, [&]() {
+      // the fused stage 0 writes the checkpoint itself
+      if (use_small(ctx)) return enq_small_step(ctx, fm, fave, fcur, dt, false, C, phase);
       CK(launch_checkpoint(ctx->d_ckpt, ctx->d_u, ctx->d_int, C, phase, elems, ctx->st));
-      if (use_small(ctx)) return enq_small_step(ctx, fm, fave, fcur, dt);
       CKR(enq_rk4(ctx, fm, fave, fcur, dt, nullptr));
       CK(launch_counter_add(ctx->d_int, 1, ctx->st));
       return MATTOHF_OK;

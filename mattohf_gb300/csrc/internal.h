@@ -227,6 +227,9 @@ struct SmallStageArgs {
   double2* store;           // if set: the adjoint's stage store; the stage input goes to slot
   const int* seg0;          // ((*it - *seg0) * 4 + store_slot) (each CTA copies its points)
   int store_slot;
+  double2* ckpt;            // stage 0, if set: the input goes to checkpoint (it + ckpt_phase) /
+  int ckpt_every;           // ckpt_every when it == 0 or (it + ckpt_phase) % ckpt_every == 0
+  int ckpt_phase;
 };
 // CTAs per column of the fused stages: one thread-block cluster per column
 // (the portable cluster size)

@@ -81,9 +81,10 @@ struct SmallLayout {
   // points: the P exchange partials (at most 2N + 2 kSmallMaxCtas doubles),
   // vH and T_A w (N and 2N doubles)
   static constexpr int RECV_F = 2 * N + 2 * kSmallMaxCtas;
-  // (and N double2 staging the adjoint's stage-store copy)
   static constexpr size_t bytes = sizeof(double2) * (size_t)N * (3 + NTEAM) + sizeof(double) * 2 * (size_t)N +
-                                  sizeof(double) * ((size_t)RECV_F + 3 * (size_t)N) + sizeof(double2) * (size_t)N;
+                                  sizeof(double) * ((size_t)RECV_F + 3 * (size_t)N);
+  // the adjoint's variant also stages its stage-store copy (N double2)
+  static constexpr size_t bytes_adj = bytes + sizeof(double2) * (size_t)N;
 };
 
 // The global last CTA of an observable stage: the observables of the stage
@@ -135,7 +136,10 @@ __device__ void small_finalize(const SmallStageArgs& a, const double* rho_s, con
   if (!(isfinite(Etot) && isfinite(Je) && isfinite(Nele)) && a.nonfinite) *a.nonfinite = 1;
 }
 
-template <int N>
+// ADJ: the variant for the adjoint's forward and recompute passes, which also
+// copies the stage input to the stage store or a checkpoint; the plain
+// forward's variant carries none of that code or shared memory.
+template <int N, bool ADJ>
 __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a) {
   using TM = Team<N, kSmallPlan<N>>;
   constexpr int E = TM::E, T = TM::T, PW = TM::PER_WARP;
@@ -151,7 +155,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   double* recvF = reinterpret_cast<double*>(K_s + N);   // [P][2 per]: the partials of this CTA's points
   double* recvV = recvF + SmallLayout<N>::RECV_F;       // [per]: vH at this CTA's points
   double* recvK = recvV + N;                            // [2 per]: T_A w at this CTA's points
-  double2* st_s = reinterpret_cast<double2*>(recvK + 2 * N);  // [per]: staged stage-store copy
+  double2* st_s = reinterpret_cast<double2*>(recvK + 2 * N);  // [per]: staged stage-store copy (ADJ)
   __shared__ int last_s;
   __shared__ double red_s[2][kSmallWarps];
   __shared__ double ex_s[kSmallMaxCtas][2];  // the first CTA: every CTA's share of <w|F>
@@ -188,10 +192,16 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   // it is waited for only before the first store to another CTA's memory
   asm volatile("barrier.cluster.arrive.relaxed;" ::: "memory");
   if (a.it_out && blockIdx.x == 0 && tid == 0) *a.it_out = *a.it + a.it_inc;
-  // the adjoint's recompute: this CTA's points of the stage input, staged in
+  // the adjoint's passes: this CTA's points of the stage input, staged in
   // shared memory by an asynchronous copy now and written to the stage store
-  // once the first phase is done (no registers held, no latency exposed)
-  if (a.store) {
+  // (recompute) or to a checkpoint (stage 0 of the forward pass) once the
+  // first phase is done (no registers held, no latency exposed)
+  auto ckpt_step = [&]() {
+    if (!a.ckpt || a.mode != 0) return false;
+    const int t = *a.it;
+    return t == 0 || (t + a.ckpt_phase) % a.ckpt_every == 0;
+  };
+  if (ADJ && (a.store || ckpt_step())) {
     const int per_pts = (N + a.P - 1) / a.P, q_st = chunk * per_pts + tid;
     if (tid < per_pts && q_st < N) {
       const unsigned dst = (unsigned)__cvta_generic_to_shared(st_s + tid);
@@ -465,10 +475,12 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
     }
   }
   __syncthreads();
-  if (a.store && tid < per && chunk * per + tid < N) {
+  if (ADJ && (a.store || ckpt_step()) && tid < per && chunk * per + tid < N) {
     asm volatile("cp.async.wait_all;" ::: "memory");
-    const size_t elems = (size_t)ncols * N;
-    a.store[((size_t)(*a.it - *a.seg0) * 4 + a.store_slot) * elems + (size_t)c * N + chunk * per + tid] = st_s[tid];
+    const size_t elems = (size_t)ncols * N, o = (size_t)c * N + chunk * per + tid;
+    const int t = *a.it;
+    if (a.store) a.store[((size_t)(t - *a.seg0) * 4 + a.store_slot) * elems + o] = st_s[tid];
+    if (ckpt_step()) a.ckpt[(size_t)((t + a.ckpt_phase) / a.ckpt_every) * elems + o] = st_s[tid];
   }
   // This CTA's partial (pair teams in order; a team past the CTA's pair count
   // holds none), one real component per thread, pushed into the shared memory
@@ -595,12 +607,12 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_stage(SmallStageArgs a)
   }
 }
 
-template <int N>
+template <int N, bool ADJ>
 static cudaError_t small_impl(const SmallStageArgs& a, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(a.nk * a.nb * a.P);
   cfg.blockDim = dim3(kSmallThreads);
-  cfg.dynamicSmemBytes = SmallLayout<N>::bytes;
+  cfg.dynamicSmemBytes = ADJ ? SmallLayout<N>::bytes_adj : SmallLayout<N>::bytes;
   cfg.stream = s;
   cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -611,12 +623,15 @@ static cudaError_t small_impl(const SmallStageArgs& a, cudaStream_t s) {
   attr[1].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 2;
-  return cudaLaunchKernelEx(&cfg, k_small_stage<N>, a);
+  return cudaLaunchKernelEx(&cfg, k_small_stage<N, ADJ>, a);
 }
 
 template <int N>
 static cudaError_t small_configure() {
-  return cudaFuncSetAttribute(k_small_stage<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(k_small_stage<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)SmallLayout<N>::bytes_adj);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_small_stage<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)SmallLayout<N>::bytes);
 }
 
@@ -635,12 +650,13 @@ int small_pair_teams(int NG) {
 
 cudaError_t launch_small_stage(int NG, const SmallStageArgs& a, cudaStream_t s) {
   if (a.P < 1 || a.P > kSmallMaxCtas) return cudaErrorInvalidValue;
+  const bool adj = a.store != nullptr || a.ckpt != nullptr;
   switch (NG) {
-    case 16: return small_impl<16>(a, s);
-    case 32: return small_impl<32>(a, s);
-    case 64: return small_impl<64>(a, s);
-    case 128: return small_impl<128>(a, s);
-    case 256: return small_impl<256>(a, s);
+    case 16: return adj ? small_impl<16, true>(a, s) : small_impl<16, false>(a, s);
+    case 32: return adj ? small_impl<32, true>(a, s) : small_impl<32, false>(a, s);
+    case 64: return adj ? small_impl<64, true>(a, s) : small_impl<64, false>(a, s);
+    case 128: return adj ? small_impl<128, true>(a, s) : small_impl<128, false>(a, s);
+    case 256: return adj ? small_impl<256, true>(a, s) : small_impl<256, false>(a, s);
     default: return cudaErrorInvalidValue;
   }
 }
