@@ -575,11 +575,13 @@ bool use_small(const mattohf_ctx* ctx) {
   if (ctx->opt_small == 0 || ctx->opt_df || ctx->opt_timing || !small_stage_supported(ctx->NG)) return false;
   if (ctx->opt_small == 1) return true;
   // measured on GB300 with mattohf_autotune (us per step, fused vs tiled):
-  // NG=128 NK=16 Nocc=2 126 vs 238 and NG=128 NK=8 Nocc=4 125 vs 242 (M^2 NG =
-  // 2^17); NG=64 NK=16 Nocc=4 196 vs 158, NG=64 NK=32 Nocc=2 196 vs 159 (2^18);
-  // NG=256 NK=8 Nocc=4 249 vs 262 (2^18); NG=128 NK=32 Nocc=2 451 vs 283 (2^19)
+  // NG=64 NK=8 Nocc=2 29 vs 129; NG=128 NK=16 Nocc=2 and NK=8 Nocc=4 96 vs 235
+  // (M^2 NG = 2^17); NG=64 NK=16 Nocc=4 171 vs 156, NG=64 NK=32 Nocc=2 173 vs
+  // 158 (2^18); NG=256 NK=8 Nocc=4 178 vs 253 (2^18, M = 32); NG=128 NK=32
+  // Nocc=2 320 vs 285 (2^19)
   const size_t M = (size_t)ctx->NK * ctx->NBocc;
-  return ctx->NK * ctx->NB <= 64 && M * M * ctx->NG <= ((size_t)1 << 17);
+  if (ctx->NK * ctx->NB > 64) return false;
+  return M * M * ctx->NG <= ((size_t)1 << 17) || (ctx->NG == 256 && M <= 32);
 }
 
 // CTAs per column.  A warp issues at most one FP64 instruction per ~64
